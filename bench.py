@@ -1,0 +1,392 @@
+"""Decoded frames/s on 1080p 4:2:2 MJPEG: batched GPU decode vs the plain
+one-frame-per-call GPU form, bit-exact against the reference algorithm.
+
+Workload (per GPU): 300 seeded synthetic frames, 1920x1080, 8-bit 4:2:2,
+quality 90, Annex K Huffman tables, restart interval = one MCU row (120 MCUs of
+16x8), decoded to interleaved RGB24. One step decodes the whole batch.
+
+  value   frames/s with packets and outputs resident in HBM (host plans headers,
+          kernels run, no host<->device payload copies), wall clock over K steps
+          bracketed by barrier + device synchronize.
+  e2e     the same through mmr_gpu_decode_batch with pinned HOST buffers: the
+          packets' H2D and the RGB frames' D2H are inside every step.
+  plain   one frame per mmr_gpu_decode_batch call (host buffers), the plain GPU form.
+
+Inputs (337 MB) and outputs (1.87 GB) per step exceed the 129 MB L2, so no L2
+flush is needed between steps.
+
+--impl reference times the reference decoder's algorithm (the C restatement in
+oracle/, the reference being Rust with no toolchain on the box) on the host
+cores, one frame per worker process, on the same workload.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+FRAMES = 300
+W, H, SUB, Q, RI = 1920, 1080, "422", 90, 120
+SEED = 20261203
+METRIC = "decoded frames/s and p50/p99 latency, batched+served vs plain GPU, bit-exact"
+WORKLOAD = "mjpeg-1080p-422-q90-ri120mcu-rgb24"
+
+
+def _oracle_decode(packet: bytes):
+    import oracle
+    t = time.perf_counter()
+    r = oracle.jpeg_decode(packet)
+    dt = time.perf_counter() - t
+    rgb = oracle.rgb24(r.frame) if r.status == 0 else None
+    return r.status, dt, rgb
+
+
+def _oracle_decode_time(packet: bytes) -> float:
+    return _oracle_decode(packet)[1]
+
+
+def _dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo", rank=rank, world_size=world)
+    return world, rank, local
+
+
+def _barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def _max_over_ranks(world, value: float) -> float:
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _sum_over_ranks(world, value: float) -> float:
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in getattr(self, "lines", []):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        p = json.load(open(path))
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def _traffic_per_block():
+    """DRAM bytes per coefficient block of the transform + colour stage, from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "jpeg_idct_rgb_1080p422.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_block:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+def make_workload(rank: int):
+    from mmrecode_gb300 import synth
+    return synth.mjpeg_stream(SEED + rank, FRAMES, W, H, SUB, Q, RI, annex_k=True)
+
+
+def reference_arm(args):
+    world, rank, _ = _dist()
+    if rank != 0:
+        return 0
+    import oracle
+    oracle.build()
+    cores = os.cpu_count() or 1
+    packets = make_workload(0)
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        def step(k):
+            sample = [packets[(k * cores + i) % FRAMES] for i in range(cores)]
+            t = time.perf_counter()
+            pool.map(_oracle_decode_time, sample, chunksize=1)
+            return time.perf_counter() - t, len(sample)
+        for k in range(args.warmup):
+            step(k)
+        total_t, total_f = 0.0, 0
+        for k in range(args.steps):
+            dt, nf = step(args.warmup + k)
+            total_t += dt
+            total_f += nf
+    fps = total_f / total_t
+    line = {
+        "impl": "reference", "metric": METRIC, "value": fps, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000 * total_t / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8/i32/f64", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "frames_per_step": cores, "width": W, "height": H, "subsampling": SUB,
+                   "quality": Q, "restart_interval_mcus": RI, "output": "rgb24"},
+        "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": cores, "kind": "port",
+                         "sample": f"{cores} frames per step of the {FRAMES}-frame workload, one per process"},
+        "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the oracle CPU-baseline sample")
+    ap.add_argument("--plain-frames", type=int, default=60)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return reference_arm(args)
+
+    world, rank, local = _dist()
+    cores = os.cpu_count() or 1
+    pool = None
+    if rank == 0 and world == 1:
+        pool = mp.get_context("spawn").Pool(cores)  # before any CUDA call
+
+    import ctypes
+
+    import torch
+
+    import __graft_entry__
+    __graft_entry__.build()
+    import mmrecode_gb300 as m
+    from mmrecode_gb300 import _lib
+
+    torch.cuda.set_device(local)
+    packets = make_workload(rank)
+    n = len(packets)
+    in_bytes = sum(len(p) for p in packets)
+    rgb_bytes = W * H * 3
+    offs, o = [], 0
+    for p in packets:
+        offs.append(o)
+        o += (len(p) + 255) // 256 * 256
+    host_in = torch.empty(o, dtype=torch.uint8, pin_memory=True)
+    hv = host_in.numpy()
+    for p, off in zip(packets, offs):
+        hv[off:off + len(p)] = memoryview(p)
+    dev_in = host_in.to(f"cuda:{local}")
+    dev_out = torch.empty(n * rgb_bytes, dtype=torch.uint8, device=f"cuda:{local}")
+    host_out = torch.empty(n * rgb_bytes, dtype=torch.uint8, pin_memory=True)
+    ctx = m.Context(local)
+
+    def items(device_resident: bool):
+        arr = (_lib.GpuItem * n)()
+        for i in range(n):
+            it = arr[i]
+            it.struct_size = ctypes.sizeof(_lib.GpuItem)
+            it.data = host_in.data_ptr() + offs[i]
+            it.device_data = dev_in.data_ptr() + offs[i] if device_resident else None
+            it.len = len(packets[i])
+            it.codec = m.CODEC_MJPEG
+            it.output = m.OUTPUT_RGB24
+            it.flags = m.ITEM_OUT_DEVICE if device_resident else 0
+            it.out = (dev_out.data_ptr() if device_resident else host_out.data_ptr()) + i * rgb_bytes
+            it.out_capacity = rgb_bytes
+        return arr
+
+    def run(arr, steps, warmup, sample_clocks=False):
+        for _ in range(warmup):
+            ctx.decode_raw(arr)
+        _barrier(world)
+        torch.cuda.synchronize()
+        launches, stages = 0, []
+        sampler = ClockSampler(local) if sample_clocks else None
+        if sampler:
+            sampler.__enter__()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            ctx.decode_raw(arr)
+            launches += ctx.last_batch_launches
+            stages.append(ctx.stats())
+        torch.cuda.synchronize()
+        _barrier(world)
+        dt = time.perf_counter() - t0
+        if sampler:
+            sampler.__exit__(None, None, None)
+        for i in range(n):
+            assert arr[i].status == 0, arr[i].message
+        return dt, launches, stages, (sampler.summary() if sampler else None)
+
+    resident = items(True)
+    dt, launches, stages, clocks = run(resident, args.steps, args.warmup, sample_clocks=True)
+    dt = _max_over_ranks(world, dt)
+    total_frames = _sum_over_ranks(world, n * args.steps)
+    value = total_frames / dt
+    ms_per_step = 1000 * dt / args.steps
+
+    hostbuf = items(False)
+    edt, _, _, _ = run(hostbuf, args.steps, args.warmup)
+    edt = _max_over_ranks(world, edt)
+    e2e = total_frames / edt
+
+    # plain GPU form: one frame per call, host buffers
+    lat = []
+    for i in range(min(args.plain_frames, n) + 3):
+        one = (_lib.GpuItem * 1)()
+        ctypes.memmove(ctypes.addressof(one), ctypes.addressof(hostbuf[i % n]), ctypes.sizeof(_lib.GpuItem))
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        ctx.decode_raw(one)
+        lat.append(time.perf_counter() - t)
+        assert one[0].status == 0
+    lat = lat[3:]
+    plain_fps = len(lat) / sum(lat)
+    lat_ms = sorted(1000 * x for x in lat)
+    pct = lambda v, q: v[min(len(v) - 1, int(q * len(v)))]
+
+    # roofline of the dominant stage (device events of the timed steps)
+    def avg(key):
+        return sum(s[key] for s in stages) / len(stages)
+    blocks = stages[-1]["jpeg_blocks"]
+    entropy_ms, idct_ms, rgb_ms, scan_ms = avg("entropy_ms"), avg("idct_ms"), avg("rgb_ms"), avg("scan_ms")
+    peak, peak_kind = _peaks()
+    transform_bytes = blocks * 128 + n * rgb_bytes
+    entropy_bytes = in_bytes + blocks * 128
+    stage_times = {"scan": scan_ms, "entropy": entropy_ms, "idct": idct_ms, "rgb": rgb_ms,
+                   "upload": avg("upload_ms"), "download": avg("download_ms")}
+    if idct_ms + rgb_ms >= entropy_ms:
+        achieved = transform_bytes / ((idct_ms + rgb_ms) / 1e3) / 1e9
+        tpb = _traffic_per_block()
+        roofline = {"bound": "hbm", "kernel": "jpeg idct + rgb (transform/colour stage)", "achieved": achieved,
+                    "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                    "traffic": tpb * blocks if tpb else None,
+                    "algorithmic_bytes_per_launch": transform_bytes}
+    else:
+        achieved = entropy_bytes / (entropy_ms / 1e3) / 1e9
+        roofline = {"bound": "hbm", "kernel": "jpeg entropy (issue-bound; HBM fraction shown)", "achieved": achieved,
+                    "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                    "algorithmic_bytes_per_launch": entropy_bytes}
+
+    cpu = None
+    bit_exact = None
+    if pool is not None:
+        # oracle sample: single core, then all cores; also checks the GPU output of those frames
+        single_t, sample = 0.0, []
+        while single_t < args.cpu_seconds / 3 and len(sample) < n:
+            st, t1, rgb = _oracle_decode(packets[len(sample)])
+            single_t += t1
+            sample.append((st, rgb))
+        k = min(n, cores)
+        t = time.perf_counter()
+        res = pool.map(_oracle_decode, packets[:k], chunksize=1)
+        multi_t = time.perf_counter() - t
+        pool.close()
+        gpu_rgb = dev_out.cpu().numpy()
+        bit_exact = True
+        for i, (st, t1, rgb) in enumerate(res):
+            bit_exact &= st == 0 and gpu_rgb[i * rgb_bytes:(i + 1) * rgb_bytes].tobytes() == rgb
+        cpu = {"value": k / multi_t, "unit": "frames/s", "cores": cores, "kind": "port",
+               "single_core_frames_per_s": len(sample) / single_t,
+               "sample": f"{len(sample)} frames on 1 core, then {k} frames on {cores} processes, "
+                         f"of the same 1080p 4:2:2 q90 workload (oracle restating the reference decoder)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u8/i32/f64", "data": "synthetic (seeded gradients+rectangles+noise)",
+            "config": {"workload": WORKLOAD, "frames_per_gpu": n, "width": W, "height": H, "subsampling": SUB,
+                       "quality": Q, "restart_interval_mcus": RI, "output": "rgb24", "huffman": "annex-k",
+                       "compressed_bytes_per_step": in_bytes, "l2": "inputs/outputs per step exceed L2; no flush",
+                       "parallelism": f"replicas x{world}"},
+            "e2e": {"value": e2e, "unit": "frames/s", "h2d_bytes_per_step": in_bytes,
+                    "d2h_bytes_per_step": n * rgb_bytes},
+            "compressed_MBps": value * in_bytes / n / 1e6,
+            "plain_gpu": {"value": plain_fps, "unit": "frames/s", "p50_ms": pct(lat_ms, 0.5), "p99_ms": pct(lat_ms, 0.99),
+                          "frames": len(lat)},
+            "batched_over_plain": value / plain_fps,
+            "latency_ms": {"batched_p50": ms_per_step, "batched_p99": ms_per_step},
+            "stage_ms": stage_times,
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "bit_exact_sample": bit_exact,
+            "gpu_launches": launches,
+            "clocks": clocks,
+        }
+        print(json.dumps(line))
+    ctx.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

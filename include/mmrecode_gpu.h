@@ -1,0 +1,132 @@
+/*
+ * GB300 batch / context API for the MJPEG and DV25 decode path.
+ *
+ * Additive to the v1 ABI in mmrecode.h (which it includes); none of these
+ * symbols exist in the reference library. The reference decodes one packet per
+ * call on one CPU thread (crates/capi/src/lib.rs:331-359, decode_jpeg in
+ * crates/codecs/mjpeg/src/decoder.rs:140 and decode_video in
+ * crates/codecs/dv/src/decoder.rs:78); this API hands many packets to the GPU
+ * at once. Every output sample equals what the reference decoder produces for
+ * the same packet; every status equals the reference's status.
+ */
+#ifndef MMRECODE_GPU_H
+#define MMRECODE_GPU_H
+
+#include "mmrecode.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Codec of a packet. */
+#define MMR_CODEC_MJPEG 1u
+#define MMR_CODEC_DV 2u
+
+/* Output layout of a decoded packet. */
+#define MMR_OUTPUT_PLANAR 0u /* native planes, Y | Cb | Cr concatenated, stride == plane width */
+#define MMR_OUTPUT_RGB24 1u  /* interleaved RGB at 1:1, integer BT.601 (crates/cli/src/terminal_preview.rs:7159-7330) */
+
+/* Item flags. */
+#define MMR_ITEM_CONCEAL 1u      /* DV: fill undecodable segments with black instead of failing
+                                    (decode_video_with_options, crates/codecs/dv/src/decoder.rs:87-150) */
+#define MMR_ITEM_OUT_DEVICE 2u   /* `out` is device memory */
+
+typedef struct mmr_gpu_context mmr_gpu_context;
+
+typedef struct mmr_gpu_config {
+    size_t struct_size;
+    int32_t device; /* CUDA device ordinal */
+    uint32_t flags; /* reserved, 0 */
+} mmr_gpu_config;
+
+/* Creates a decode context (one CUDA stream and its device arenas) on a device. */
+MMR_API mmr_status mmr_gpu_context_create(const mmr_gpu_config *config, mmr_gpu_context **out_context);
+
+/* Destroys a context; NULL is ignored. */
+MMR_API void mmr_gpu_context_destroy(mmr_gpu_context *context);
+
+/* Output geometry of one packet, from its headers only. */
+typedef struct mmr_gpu_frame_info {
+    size_t struct_size;
+    mmr_status status; /* header-level status; decoding can still fail later */
+    mmr_pixel_format format;
+    mmr_color_range range;
+    size_t width, height;
+    size_t plane_count;
+    size_t plane_width[MMR_MAX_PLANES], plane_height[MMR_MAX_PLANES];
+    size_t planar_bytes; /* output size with MMR_OUTPUT_PLANAR */
+    size_t rgb_bytes;    /* output size with MMR_OUTPUT_RGB24 */
+} mmr_gpu_frame_info;
+
+/* Reads a packet's headers on the host and reports its output geometry. */
+MMR_API mmr_status mmr_gpu_probe(uint32_t codec, const uint8_t *data, size_t len, mmr_gpu_frame_info *info);
+
+/* One packet of a batch. */
+typedef struct mmr_gpu_item {
+    size_t struct_size;
+    const uint8_t *data;        /* host copy of the packet (headers are read on the host) */
+    const uint8_t *device_data; /* optional device copy of the same bytes; skips the upload */
+    size_t len;
+    uint32_t codec;
+    uint32_t output;
+    uint32_t flags;
+    uint8_t *out;               /* output buffer (host, or device with MMR_ITEM_OUT_DEVICE) */
+    size_t out_capacity;
+    /* filled in by the call */
+    mmr_status status;
+    mmr_pixel_format format;
+    mmr_color_range range;
+    size_t width, height;
+    size_t plane_count;
+    size_t plane_offset[MMR_MAX_PLANES], plane_width[MMR_MAX_PLANES], plane_height[MMR_MAX_PLANES];
+    size_t out_bytes;
+    uint32_t concealed_segments; /* DV with MMR_ITEM_CONCEAL: segments filled with black */
+    char message[200];           /* per-item diagnostic, "" on success */
+} mmr_gpu_item;
+
+/*
+ * Decodes `count` packets in one pass on the context's stream and returns when
+ * all are done. Per-item status is in items[i].status; the call itself returns
+ * MMR_STATUS_OK unless its arguments are invalid or the device failed.
+ */
+MMR_API mmr_status mmr_gpu_decode_batch(mmr_gpu_context *context, mmr_gpu_item *items, size_t count);
+
+/* Device time (CUDA events on the context stream) of the last batch, in ms. */
+MMR_API double mmr_gpu_last_batch_ms(const mmr_gpu_context *context);
+
+/* Kernel launches of the last batch. */
+MMR_API uint32_t mmr_gpu_last_batch_launches(const mmr_gpu_context *context);
+
+/* Stage times of the last batch (CUDA events on the context stream) and its sizes. */
+typedef struct mmr_gpu_batch_stats {
+    size_t struct_size;
+    double total_ms, upload_ms, scan_ms, entropy_ms, idct_ms, dv_ms, rgb_ms, download_ms;
+    uint64_t input_bytes, output_bytes, jpeg_blocks, dv_blocks, rgb_pixels;
+    uint32_t launches;
+} mmr_gpu_batch_stats;
+
+MMR_API mmr_status mmr_gpu_last_batch_stats(const mmr_gpu_context *context, mmr_gpu_batch_stats *stats);
+
+/* Stream generation: the reference encoders plus the options the decode benchmarks need. */
+typedef struct mmr_jpeg_encode_options {
+    size_t struct_size;
+    uint8_t quality;           /* 1..100 */
+    uint8_t annex_k_huffman;   /* 1: ITU-T T.81 Annex K.3 tables (luma/chroma); 0: the reference's tables */
+    uint16_t restart_interval; /* MCUs per restart interval, 0 = none */
+} mmr_jpeg_encode_options;
+
+/* mmr_mjpeg_encode (crates/codecs/mjpeg/src/encoder.rs:44-87) with Annex K Huffman and DRI options. */
+MMR_API mmr_status mmr_mjpeg_encode_ex(const mmr_video_frame_view *frame, const mmr_jpeg_encode_options *options,
+                                       mmr_buffer *out_buffer);
+
+#define MMR_DV_MODE_88 0u       /* every block 8-8 (the reference encoder) */
+#define MMR_DV_MODE_ACTIVITY 1u /* 2-4-8 where inter-field activity exceeds intra-field activity */
+
+/* mmr_dv_encode (crates/codecs/dv/src/encoder.rs:67-103) with a DCT-mode policy. */
+MMR_API mmr_status mmr_dv_encode_ex(const mmr_video_frame_view *frame, uint32_t mode_policy, mmr_buffer *out_buffer);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

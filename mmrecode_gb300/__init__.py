@@ -1,0 +1,410 @@
+"""GB300 MJPEG / DV25 intra-frame decoder: Python host API.
+
+Mirrors the reference's decode interface for this path:
+
+* ``decode_jpeg`` / ``decode_dv``: one packet -> ``VideoFrame`` through the C ABI
+  (``mmr_mjpeg_decode`` / ``mmr_dv_decode``; crates/capi/src/lib.rs:331-359).
+* ``MjpegDecoder`` / ``DvDecoder``: the ``Decoder`` trait
+  (crates/core/src/codec.rs:102-130) -- configure / send_packet /
+  receive_frame / flush, with the reference wrappers' state errors
+  (crates/codecs/mjpeg/src/codec.rs:16-71, crates/codecs/dv/src/codec.rs:16-66).
+  With ``batch > 1`` packets queue until a batch is full (or ``flush``) and
+  decode together on the GPU.
+* ``Context``: many packets per GPU pass (``mmr_gpu_decode_batch``).
+
+All decoding runs in CUDA kernels inside libmmrecode_gpu.so; there is no CPU
+decode path.
+"""
+
+from __future__ import annotations
+
+import collections
+import ctypes
+from dataclasses import dataclass, field
+
+from . import _lib
+
+STATUS_OK, INVALID_ARGUMENT, INVALID_DATA, UNSUPPORTED, INVALID_STATE, IO_ERROR, INTERNAL = 0, 1, 2, 3, 4, 5, 100
+GRAY8, YUV420P8, YUV422P8, YUV444P8, YUV411P8 = 1, 2, 3, 4, 5
+RANGE_UNSPECIFIED, RANGE_FULL, RANGE_LIMITED = 0, 1, 2
+CODEC_MJPEG, CODEC_DV = 1, 2
+OUTPUT_PLANAR, OUTPUT_RGB24 = 0, 1
+ITEM_CONCEAL, ITEM_OUT_DEVICE = 1, 2
+DV_MODE_88, DV_MODE_ACTIVITY = 0, 1
+
+MJPEG_CODEC_NAME = "video/mjpeg"  # crates/codecs/mjpeg/src/codec.rs:12
+DV_CODEC_NAME = "video/dv"        # crates/codecs/dv/src/codec.rs:12
+
+
+class MmrError(Exception):
+    """A failed call: ``status`` is the C ABI status, ``message`` its diagnostic."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(message)
+        self.status = status
+        self.message = message
+
+
+@dataclass
+class Plane:
+    data: bytes
+    stride: int
+    width: int
+    height: int
+
+
+@dataclass
+class VideoFrame:
+    format: int
+    width: int
+    height: int
+    planes: list
+    range: int = RANGE_UNSPECIFIED
+    pts: object = None
+    duration: object = None
+
+
+@dataclass
+class CodecDescriptor:
+    codec_id: str
+    media_type: str = "video"
+
+
+@dataclass
+class Packet:
+    data: bytes
+    pts: object = None
+    duration: object = None
+
+
+def version() -> str:
+    return _lib.load().mmr_version().decode()
+
+
+def abi_version() -> int:
+    return _lib.load().mmr_abi_version()
+
+
+def _frame_from_c(fr: _lib.VideoFrameC) -> VideoFrame:
+    planes = []
+    for i in range(fr.plane_count):
+        p = fr.planes[i]
+        planes.append(Plane(ctypes.string_at(p.data, p.data_len), p.stride, p.width, p.height))
+    return VideoFrame(fr.format, fr.width, fr.height, planes, fr.range)
+
+
+def _decode_one(fn, data: bytes) -> VideoFrame:
+    lib = _lib.load()
+    fr = _lib.VideoFrameC()
+    fr.struct_size = ctypes.sizeof(_lib.VideoFrameC)
+    buf = bytes(data)
+    st = fn(buf, len(buf), ctypes.byref(fr))
+    if st != STATUS_OK:
+        raise MmrError(st, _lib.last_error())
+    try:
+        return _frame_from_c(fr)
+    finally:
+        lib.mmr_video_frame_free(ctypes.byref(fr))
+
+
+def decode_jpeg(data: bytes) -> VideoFrame:
+    """decode_jpeg(...).into_video_frame() on the GPU (crates/codecs/mjpeg/src/decoder.rs:140-167)."""
+    return _decode_one(_lib.load().mmr_mjpeg_decode, data)
+
+
+def decode_dv(data: bytes) -> VideoFrame:
+    """parse_frame + decode_video on the GPU (crates/codecs/dv/src/{dif,decoder}.rs)."""
+    return _decode_one(_lib.load().mmr_dv_decode, data)
+
+
+def _view(frame: VideoFrame, keep: list) -> _lib.VideoFrameView:
+    v = _lib.VideoFrameView()
+    v.struct_size = ctypes.sizeof(_lib.VideoFrameView)
+    v.format, v.range, v.width, v.height = frame.format, frame.range, frame.width, frame.height
+    v.plane_count = len(frame.planes)
+    for i, p in enumerate(frame.planes):
+        data = bytes(p.data)
+        arr = (ctypes.c_uint8 * max(len(data), 1)).from_buffer_copy(data or b"\0")
+        keep.append(arr)
+        v.planes[i].data = ctypes.cast(arr, _lib.u8p)
+        v.planes[i].data_len = len(data)
+        v.planes[i].stride, v.planes[i].width, v.planes[i].height = p.stride, p.width, p.height
+    return v
+
+
+def _take_buffer(st: int, b: _lib.Buffer) -> bytes:
+    lib = _lib.load()
+    if st != STATUS_OK:
+        raise MmrError(st, _lib.last_error())
+    try:
+        return ctypes.string_at(b.data, b.len)
+    finally:
+        lib.mmr_buffer_free(ctypes.byref(b))
+
+
+def encode_jpeg(frame: VideoFrame, quality: int = 75, annex_k: bool = False, restart_interval: int = 0) -> bytes:
+    """Baseline JPEG encoder (crates/codecs/mjpeg/src/encoder.rs:44-87); the defaults reproduce it byte for byte."""
+    lib = _lib.load()
+    keep: list = []
+    v = _view(frame, keep)
+    b = _lib.Buffer()
+    b.struct_size = ctypes.sizeof(_lib.Buffer)
+    if not annex_k and not restart_interval:
+        st = lib.mmr_mjpeg_encode(ctypes.byref(v), quality, ctypes.byref(b))
+    else:
+        o = _lib.JpegEncodeOptions(ctypes.sizeof(_lib.JpegEncodeOptions), quality, 1 if annex_k else 0, restart_interval)
+        st = lib.mmr_mjpeg_encode_ex(ctypes.byref(v), ctypes.byref(o), ctypes.byref(b))
+    return _take_buffer(st, b)
+
+
+def encode_dv(frame: VideoFrame, mode_policy: int = DV_MODE_88) -> bytes:
+    """DV25 encoder (crates/codecs/dv/src/encoder.rs:67-103); DV_MODE_88 reproduces it byte for byte."""
+    lib = _lib.load()
+    keep: list = []
+    v = _view(frame, keep)
+    b = _lib.Buffer()
+    b.struct_size = ctypes.sizeof(_lib.Buffer)
+    if mode_policy == DV_MODE_88:
+        st = lib.mmr_dv_encode(ctypes.byref(v), ctypes.byref(b))
+    else:
+        st = lib.mmr_dv_encode_ex(ctypes.byref(v), mode_policy, ctypes.byref(b))
+    return _take_buffer(st, b)
+
+
+@dataclass
+class FrameInfo:
+    status: int
+    format: int
+    range: int
+    width: int
+    height: int
+    plane_count: int
+    plane_width: tuple
+    plane_height: tuple
+    planar_bytes: int
+    rgb_bytes: int
+
+
+def probe(codec: int, data: bytes) -> FrameInfo:
+    """Output geometry of one packet from its headers (mmr_gpu_probe)."""
+    lib = _lib.load()
+    info = _lib.FrameInfo()
+    info.struct_size = ctypes.sizeof(_lib.FrameInfo)
+    buf = bytes(data)
+    st = lib.mmr_gpu_probe(codec, buf, len(buf), ctypes.byref(info))
+    if st != STATUS_OK:
+        raise MmrError(st, _lib.last_error())
+    return FrameInfo(info.status, info.format, info.range, info.width, info.height, info.plane_count,
+                     tuple(info.plane_width), tuple(info.plane_height), info.planar_bytes, info.rgb_bytes)
+
+
+@dataclass
+class BatchResult:
+    status: int
+    message: str
+    format: int = 0
+    range: int = 0
+    width: int = 0
+    height: int = 0
+    plane_count: int = 0
+    plane_offset: tuple = ()
+    plane_width: tuple = ()
+    plane_height: tuple = ()
+    out_bytes: int = 0
+    concealed_segments: int = 0
+
+
+class Context:
+    """One GPU decode context (a CUDA stream with its device arenas)."""
+
+    def __init__(self, device: int = 0):
+        lib = _lib.load()
+        cfg = _lib.GpuConfig(ctypes.sizeof(_lib.GpuConfig), device, 0)
+        h = ctypes.c_void_p()
+        st = lib.mmr_gpu_context_create(ctypes.byref(cfg), ctypes.byref(h))
+        if st != STATUS_OK:
+            raise MmrError(st, _lib.last_error())
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.load().mmr_gpu_context_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def last_batch_ms(self) -> float:
+        return _lib.load().mmr_gpu_last_batch_ms(self._h)
+
+    @property
+    def last_batch_launches(self) -> int:
+        return _lib.load().mmr_gpu_last_batch_launches(self._h)
+
+    def stats(self) -> dict:
+        """Stage times (ms, CUDA events on the context stream) and sizes of the last batch."""
+        s = _lib.BatchStats()
+        s.struct_size = ctypes.sizeof(_lib.BatchStats)
+        st = _lib.load().mmr_gpu_last_batch_stats(self._h, ctypes.byref(s))
+        if st != STATUS_OK:
+            raise MmrError(st, _lib.last_error())
+        return {name: getattr(s, name) for name, _ in _lib.BatchStats._fields_ if name != "struct_size"}
+
+    def decode_raw(self, items: "ctypes.Array") -> None:
+        """Runs an already filled ``(_lib.GpuItem * n)`` array (pointers owned by the caller)."""
+        st = _lib.load().mmr_gpu_decode_batch(self._h, items, len(items))
+        if st != STATUS_OK:
+            raise MmrError(st, _lib.last_error())
+
+    def decode_batch(self, packets, codec=CODEC_MJPEG, output=OUTPUT_PLANAR, conceal=False):
+        """Decodes a list of packets (bytes). ``codec`` / ``output`` may be per-packet lists.
+        Returns ``[(BatchResult, bytes or None)]`` in packet order."""
+        n = len(packets)
+        codecs = codec if isinstance(codec, (list, tuple)) else [codec] * n
+        outputs = output if isinstance(output, (list, tuple)) else [output] * n
+        items = (_lib.GpuItem * max(n, 1))()
+        keep = []
+        outs = []
+        for i, pkt in enumerate(packets):
+            data = bytes(pkt)
+            src = (ctypes.c_uint8 * max(len(data), 1)).from_buffer_copy(data or b"\0")
+            keep.append(src)
+            try:
+                info = probe(codecs[i], data)
+                need = info.rgb_bytes if outputs[i] == OUTPUT_RGB24 else info.planar_bytes
+            except MmrError:
+                need = 0
+            dst = (ctypes.c_uint8 * max(need, 1))()
+            outs.append(dst)
+            it = items[i]
+            it.struct_size = ctypes.sizeof(_lib.GpuItem)
+            it.data = ctypes.addressof(src)
+            it.len = len(data)
+            it.codec = codecs[i]
+            it.output = outputs[i]
+            it.flags = ITEM_CONCEAL if conceal else 0
+            it.out = ctypes.addressof(dst)
+            it.out_capacity = need
+        st = _lib.load().mmr_gpu_decode_batch(self._h, items, n)
+        if st != STATUS_OK and st != INTERNAL:
+            raise MmrError(st, _lib.last_error())
+        res = []
+        for i in range(n):
+            it = items[i]
+            r = BatchResult(it.status, it.message.decode("utf-8", "replace"), it.format, it.range, it.width, it.height,
+                            it.plane_count, tuple(it.plane_offset), tuple(it.plane_width), tuple(it.plane_height),
+                            it.out_bytes, it.concealed_segments)
+            payload = ctypes.string_at(outs[i], it.out_bytes) if it.status == STATUS_OK else None
+            res.append((r, payload))
+        return res
+
+
+def frame_from_batch(r: BatchResult, payload: bytes) -> VideoFrame:
+    planes = []
+    for c in range(r.plane_count):
+        off, w, h = r.plane_offset[c], r.plane_width[c], r.plane_height[c]
+        planes.append(Plane(payload[off:off + w * h], w, w, h))
+    return VideoFrame(r.format, r.width, r.height, planes, r.range)
+
+
+class _GpuDecoder:
+    """Decoder trait (crates/core/src/codec.rs:102-130) over the GPU library."""
+
+    codec_name = ""
+    codec = 0
+    kind = ""
+
+    def __init__(self, batch: int = 1, context: Context | None = None):
+        if batch < 1:
+            raise ValueError("batch must be at least 1")
+        self._configured = False
+        self._frames = collections.deque()
+        self._pending: list[Packet] = []
+        self._batch = batch
+        self._ctx = context
+
+    def configure(self, descriptor: CodecDescriptor) -> None:
+        self._check_descriptor(descriptor)
+        self._frames.clear()
+        self._pending.clear()
+        self._configured = True
+
+    def _require(self, what: str) -> None:
+        if not self._configured:
+            raise MmrError(INVALID_STATE, f"invalid state: {self.kind} decoder must be configured before {what}")
+
+    def send_packet(self, packet: Packet) -> None:
+        self._require("receiving packets")
+        if self._batch == 1:
+            frame = self._decode_single(packet.data)
+            frame.pts, frame.duration = packet.pts, packet.duration
+            self._frames.append(frame)
+            return
+        self._pending.append(packet)
+        if len(self._pending) >= self._batch:
+            self._run_pending()
+
+    def receive_frame(self):
+        self._require("receiving frames")
+        if not self._frames:
+            return None
+        item = self._frames.popleft()
+        if isinstance(item, MmrError):
+            raise item
+        return item
+
+    def flush(self) -> None:
+        self._require("flushing")
+        if self._pending:
+            self._run_pending()
+
+    def _run_pending(self) -> None:
+        if self._ctx is None:
+            self._ctx = Context()
+        packets, self._pending = self._pending, []
+        for pkt, (r, payload) in zip(packets, self._ctx.decode_batch([p.data for p in packets], self.codec)):
+            if r.status != STATUS_OK:
+                self._frames.append(MmrError(r.status, r.message))
+                continue
+            frame = frame_from_batch(r, payload)
+            frame.pts, frame.duration = pkt.pts, pkt.duration
+            self._frames.append(frame)
+
+
+class MjpegDecoder(_GpuDecoder):
+    """MjpegDecoder (crates/codecs/mjpeg/src/codec.rs:16-71) decoding on the GPU."""
+
+    codec_name = MJPEG_CODEC_NAME
+    codec = CODEC_MJPEG
+    kind = "Motion JPEG"
+
+    def _check_descriptor(self, d: CodecDescriptor) -> None:
+        if d.codec_id != MJPEG_CODEC_NAME:
+            raise MmrError(INVALID_DATA, f"invalid data: expected {MJPEG_CODEC_NAME}, received {d.codec_id}")
+        if d.media_type != "video":
+            raise MmrError(INVALID_DATA, "invalid data: Motion JPEG decoder requires a video stream descriptor")
+
+    def _decode_single(self, data: bytes) -> VideoFrame:
+        return decode_jpeg(data)
+
+
+class DvDecoder(_GpuDecoder):
+    """DvDecoder (crates/codecs/dv/src/codec.rs:16-66) decoding on the GPU."""
+
+    codec_name = DV_CODEC_NAME
+    codec = CODEC_DV
+    kind = "DV"
+
+    def _check_descriptor(self, d: CodecDescriptor) -> None:
+        if d.codec_id != DV_CODEC_NAME or d.media_type != "video":
+            raise MmrError(INVALID_DATA, "invalid data: DV decoder requires a video/dv video descriptor")
+
+    def _decode_single(self, data: bytes) -> VideoFrame:
+        return decode_dv(data)

@@ -1,0 +1,137 @@
+"""ctypes binding of libmmrecode_gpu.so (include/mmrecode.h, include/mmrecode_gpu.h).
+
+The library is built in-tree by ``mmrecode_gb300.build.build()``. Loading never
+falls back to anything else: a missing library raises.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+
+from . import build as _build
+
+LIB_PATH = _build.LIB
+
+u8p = ctypes.POINTER(ctypes.c_uint8)
+
+
+class PlaneView(ctypes.Structure):
+    _fields_ = [("data", u8p), ("data_len", ctypes.c_size_t), ("stride", ctypes.c_size_t),
+                ("width", ctypes.c_size_t), ("height", ctypes.c_size_t)]
+
+
+class VideoFrameView(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_size_t), ("format", ctypes.c_uint32), ("range", ctypes.c_uint32),
+                ("width", ctypes.c_size_t), ("height", ctypes.c_size_t), ("plane_count", ctypes.c_size_t),
+                ("planes", PlaneView * 3)]
+
+
+class OwnedPlane(ctypes.Structure):
+    _fields_ = [("data", u8p), ("data_len", ctypes.c_size_t), ("stride", ctypes.c_size_t),
+                ("width", ctypes.c_size_t), ("height", ctypes.c_size_t)]
+
+
+class VideoFrameC(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_size_t), ("format", ctypes.c_uint32), ("range", ctypes.c_uint32),
+                ("width", ctypes.c_size_t), ("height", ctypes.c_size_t), ("plane_count", ctypes.c_size_t),
+                ("planes", OwnedPlane * 3)]
+
+
+class Buffer(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_size_t), ("data", u8p), ("len", ctypes.c_size_t)]
+
+
+class GpuConfig(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_size_t), ("device", ctypes.c_int32), ("flags", ctypes.c_uint32)]
+
+
+class FrameInfo(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_size_t), ("status", ctypes.c_int32), ("format", ctypes.c_uint32),
+                ("range", ctypes.c_uint32), ("width", ctypes.c_size_t), ("height", ctypes.c_size_t),
+                ("plane_count", ctypes.c_size_t), ("plane_width", ctypes.c_size_t * 3),
+                ("plane_height", ctypes.c_size_t * 3), ("planar_bytes", ctypes.c_size_t),
+                ("rgb_bytes", ctypes.c_size_t)]
+
+
+class GpuItem(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_size_t), ("data", ctypes.c_void_p), ("device_data", ctypes.c_void_p),
+                ("len", ctypes.c_size_t), ("codec", ctypes.c_uint32), ("output", ctypes.c_uint32),
+                ("flags", ctypes.c_uint32), ("out", ctypes.c_void_p), ("out_capacity", ctypes.c_size_t),
+                ("status", ctypes.c_int32), ("format", ctypes.c_uint32), ("range", ctypes.c_uint32),
+                ("width", ctypes.c_size_t), ("height", ctypes.c_size_t), ("plane_count", ctypes.c_size_t),
+                ("plane_offset", ctypes.c_size_t * 3), ("plane_width", ctypes.c_size_t * 3),
+                ("plane_height", ctypes.c_size_t * 3), ("out_bytes", ctypes.c_size_t),
+                ("concealed_segments", ctypes.c_uint32), ("message", ctypes.c_char * 200)]
+
+
+class BatchStats(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_size_t)] + [(n, ctypes.c_double) for n in (
+        "total_ms", "upload_ms", "scan_ms", "entropy_ms", "idct_ms", "dv_ms", "rgb_ms", "download_ms")] + [
+        (n, ctypes.c_uint64) for n in ("input_bytes", "output_bytes", "jpeg_blocks", "dv_blocks", "rgb_pixels")] + [
+        ("launches", ctypes.c_uint32)]
+
+
+class JpegEncodeOptions(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_size_t), ("quality", ctypes.c_uint8), ("annex_k_huffman", ctypes.c_uint8),
+                ("restart_interval", ctypes.c_uint16)]
+
+
+# Every function the headers declare, with its ctypes signature.
+SIGNATURES = {
+    "mmr_abi_version": ([], ctypes.c_uint32),
+    "mmr_version": ([], ctypes.c_char_p),
+    "mmr_last_error_message": ([ctypes.c_char_p, ctypes.c_size_t], ctypes.c_size_t),
+    "mmr_mjpeg_decode": ([ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(VideoFrameC)], ctypes.c_int32),
+    "mmr_dv_decode": ([ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(VideoFrameC)], ctypes.c_int32),
+    "mmr_mpeg2_picture_count": ([ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int32),
+    "mmr_mpeg2_decode_picture": ([ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t, ctypes.POINTER(VideoFrameC)],
+                                 ctypes.c_int32),
+    "mmr_video_frame_free": ([ctypes.POINTER(VideoFrameC)], None),
+    "mmr_mjpeg_encode": ([ctypes.POINTER(VideoFrameView), ctypes.c_uint8, ctypes.POINTER(Buffer)], ctypes.c_int32),
+    "mmr_dv_encode": ([ctypes.POINTER(VideoFrameView), ctypes.POINTER(Buffer)], ctypes.c_int32),
+    "mmr_mpeg2_encode": ([ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.POINTER(Buffer)], ctypes.c_int32),
+    "mmr_mpegts_mux_mpeg2": ([ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(Buffer)], ctypes.c_int32),
+    "mmr_mpegts_mux_mpeg2_mp2": ([ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
+                                 ctypes.POINTER(Buffer)], ctypes.c_int32),
+    "mmr_mpegts_demux_mpeg2": ([ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(Buffer)], ctypes.c_int32),
+    "mmr_mpegts_demux_mp2": ([ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(Buffer)], ctypes.c_int32),
+    "mmr_buffer_free": ([ctypes.POINTER(Buffer)], None),
+    "mmr_gpu_context_create": ([ctypes.POINTER(GpuConfig), ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int32),
+    "mmr_gpu_context_destroy": ([ctypes.c_void_p], None),
+    "mmr_gpu_probe": ([ctypes.c_uint32, ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(FrameInfo)], ctypes.c_int32),
+    "mmr_gpu_decode_batch": ([ctypes.c_void_p, ctypes.POINTER(GpuItem), ctypes.c_size_t], ctypes.c_int32),
+    "mmr_gpu_last_batch_ms": ([ctypes.c_void_p], ctypes.c_double),
+    "mmr_gpu_last_batch_launches": ([ctypes.c_void_p], ctypes.c_uint32),
+    "mmr_gpu_last_batch_stats": ([ctypes.c_void_p, ctypes.POINTER(BatchStats)], ctypes.c_int32),
+    "mmr_mjpeg_encode_ex": ([ctypes.POINTER(VideoFrameView), ctypes.POINTER(JpegEncodeOptions), ctypes.POINTER(Buffer)],
+                            ctypes.c_int32),
+    "mmr_dv_encode_ex": ([ctypes.POINTER(VideoFrameView), ctypes.c_uint32, ctypes.POINTER(Buffer)], ctypes.c_int32),
+}
+
+_lib = None
+
+
+def load() -> ctypes.CDLL:
+    """Loads the in-tree library, building it first if it is missing."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            _build.build()
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"libmmrecode_gpu.so is missing at {LIB_PATH}")
+        lib = ctypes.CDLL(LIB_PATH)
+        for name, (args, res) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.argtypes = args
+            fn.restype = res
+        _lib = lib
+    return _lib
+
+
+def last_error() -> str:
+    lib = load()
+    n = lib.mmr_last_error_message(None, 0)
+    buf = ctypes.create_string_buffer(n)
+    lib.mmr_last_error_message(buf, n)
+    return buf.value.decode("utf-8", "replace")

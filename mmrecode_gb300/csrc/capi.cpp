@@ -1,0 +1,500 @@
+// C ABI of libmmrecode_gpu.so: the v1 symbols of mmrecode.h (same semantics
+// as crates/capi/src/lib.rs) and the additive batch API of mmrecode_gpu.h.
+#include <cuda_runtime.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/mmrecode.h"
+#include "../../include/mmrecode_gpu.h"
+#include "encode.h"
+#include "engine.h"
+
+using mmr::Engine;
+using mmr::Item;
+
+namespace {
+
+const char kVersion[] = "0.0.1+gb300";
+
+// lib.rs:46-48: the last diagnostic is thread-local.
+thread_local std::string g_last_error;
+
+mmr_status finish(mmr_status st, const std::string &msg) {
+    g_last_error = st == MMR_STATUS_OK ? std::string() : msg;
+    return st;
+}
+
+// ApiError Display (lib.rs:73-80) and core Error Display (crates/core/src/error.rs:18-27).
+std::string with_prefix(int32_t st, const std::string &m) {
+    switch (st) {
+    case MMR_STATUS_INVALID_ARGUMENT: return "invalid argument: " + m;
+    case MMR_STATUS_INVALID_DATA: return "invalid data: " + m;
+    case MMR_STATUS_UNSUPPORTED: return "unsupported: " + m;
+    case MMR_STATUS_INVALID_STATE: return "invalid state: " + m;
+    default: return m;
+    }
+}
+
+mmr_status invalid_argument(const std::string &m) { return finish(MMR_STATUS_INVALID_ARGUMENT, "invalid argument: " + m); }
+
+// Engines for the v1 single-packet calls: each concurrent caller borrows one.
+std::mutex g_pool_mutex;
+std::vector<Engine *> g_pool;
+
+Engine *acquire_engine(std::string &err) {
+    {
+        std::lock_guard<std::mutex> lock(g_pool_mutex);
+        if (!g_pool.empty()) {
+            Engine *e = g_pool.back();
+            g_pool.pop_back();
+            return e;
+        }
+    }
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        err = "no CUDA device is available to the GPU decoder";
+        return nullptr;
+    }
+    try {
+        return new Engine(0);
+    } catch (const std::exception &e) {
+        err = std::string("could not initialise the GPU decoder: ") + e.what();
+        return nullptr;
+    }
+}
+
+void release_engine(Engine *e) {
+    std::lock_guard<std::mutex> lock(g_pool_mutex);
+    g_pool.push_back(e);
+}
+
+void reset_frame(mmr_video_frame *f) {
+    memset(f, 0, sizeof(*f));
+    f->struct_size = sizeof(mmr_video_frame);
+}
+
+void free_frame_planes(mmr_video_frame *f) {
+    size_t n = f->plane_count < MMR_MAX_PLANES ? f->plane_count : MMR_MAX_PLANES;
+    for (size_t i = 0; i < n; i++) free(f->planes[i].data);
+}
+
+// mjpeg_decode_impl / dv_decode_impl (lib.rs:594-642) on the GPU.
+mmr_status decode_one(uint32_t codec, const uint8_t *data, size_t len, mmr_video_frame *out) {
+    if (!out) return invalid_argument("out_frame is null");
+    if (out->struct_size != sizeof(mmr_video_frame)) {
+        char m[128];
+        snprintf(m, sizeof m, "out_frame struct_size is %zu, expected %zu", out->struct_size, sizeof(mmr_video_frame));
+        return invalid_argument(m);
+    }
+    reset_frame(out);
+    if (len > 0 && !data) return invalid_argument("data is null while length is nonzero");
+    mmr::Probe pr = mmr::probe_packet(codec, data, len);
+    Item it;
+    it.data = data;
+    it.len = len;
+    it.codec = codec;
+    it.output = mmr::kOutPlanar;
+    uint8_t *planes[3] = {nullptr, nullptr, nullptr};
+    bool sized = pr.status == MMR_STATUS_OK && pr.format != 0 && pr.plane_count <= 3;
+    if (sized) {
+        for (size_t c = 0; c < pr.plane_count; c++) {
+            size_t bytes = pr.plane_width[c] * pr.plane_height[c];
+            planes[c] = (uint8_t *)malloc(bytes ? bytes : 1);
+            if (!planes[c]) {
+                for (size_t k = 0; k < c; k++) free(planes[k]);
+                return finish(MMR_STATUS_INTERNAL_ERROR, "out of host memory");
+            }
+            it.plane_out[c] = planes[c];
+        }
+        it.out_capacity = pr.planar_bytes;
+    }
+    std::string err;
+    Engine *engine = acquire_engine(err);
+    if (!engine) {
+        for (auto p : planes) free(p);
+        return finish(MMR_STATUS_INTERNAL_ERROR, err);
+    }
+    engine->decode(&it, 1);
+    release_engine(engine);
+    if (it.status != MMR_STATUS_OK) {
+        for (auto p : planes) free(p);
+        return finish(it.status, with_prefix(it.status, it.message));
+    }
+    out->format = it.format;
+    out->range = it.range;
+    out->width = it.width;
+    out->height = it.height;
+    out->plane_count = it.plane_count;
+    for (size_t c = 0; c < it.plane_count && c < MMR_MAX_PLANES; c++) {
+        out->planes[c].data = planes[c];
+        out->planes[c].width = it.plane_width[c];
+        out->planes[c].height = it.plane_height[c];
+        out->planes[c].stride = it.plane_width[c];
+        out->planes[c].data_len = it.plane_width[c] * it.plane_height[c];
+    }
+    return finish(MMR_STATUS_OK, "");
+}
+
+// video_frame_from_view + validate_plane_storage (lib.rs:1061-1127).
+mmr_status frame_from_view(const mmr_video_frame_view *v, mmr::FrameIn &f) {
+    if (v->plane_count > MMR_MAX_PLANES) {
+        char m[96];
+        snprintf(m, sizeof m, "plane_count %zu exceeds %u", v->plane_count, MMR_MAX_PLANES);
+        return invalid_argument(m);
+    }
+    if (v->format < 1 || v->format > 5) {
+        char m[96];
+        snprintf(m, sizeof m, "unknown pixel format %u", v->format);
+        return invalid_argument(m);
+    }
+    if (v->range > 2) {
+        char m[96];
+        snprintf(m, sizeof m, "unknown color range %u", v->range);
+        return invalid_argument(m);
+    }
+    size_t expected = v->format == MMR_PIXEL_FORMAT_GRAY8 ? 1 : 3;
+    if (v->plane_count != expected) {
+        char m[96];
+        snprintf(m, sizeof m, "pixel format requires %zu planes, received %zu", expected, v->plane_count);
+        return invalid_argument(m);
+    }
+    f.format = v->format;
+    f.range = v->range;
+    f.width = v->width;
+    f.height = v->height;
+    f.plane_count = v->plane_count;
+    for (size_t i = 0; i < v->plane_count; i++) {
+        const mmr_plane_view &p = v->planes[i];
+        if (p.data_len > 0 && !p.data) return invalid_argument("plane data is null while length is nonzero");
+        size_t rows = p.height ? p.height - 1 : 0;
+        unsigned __int128 required = (unsigned __int128)rows * p.stride + p.width;
+        if (required > p.data_len) {
+            char m[128];
+            snprintf(m, sizeof m, "plane %zu needs %llu bytes but data_len is %zu", i, (unsigned long long)required,
+                     p.data_len);
+            return invalid_argument(m);
+        }
+        f.planes[i] = {p.data, p.data_len, p.stride, p.width, p.height};
+    }
+    return MMR_STATUS_OK;
+}
+
+mmr_status check_buffer(mmr_buffer *b) {
+    if (b->struct_size != sizeof(mmr_buffer)) {
+        char m[128];
+        snprintf(m, sizeof m, "out_buffer struct_size is %zu, expected %zu", b->struct_size, sizeof(mmr_buffer));
+        return invalid_argument(m);
+    }
+    return MMR_STATUS_OK;
+}
+
+void reset_buffer(mmr_buffer *b) {
+    b->struct_size = sizeof(mmr_buffer);
+    b->data = nullptr;
+    b->len = 0;
+}
+
+mmr_status emit_buffer(const mmr::EncodeResult &r, mmr_buffer *out) {
+    if (r.status != MMR_STATUS_OK) return finish(r.status, with_prefix(r.status, r.message));
+    out->data = (uint8_t *)malloc(r.data.size() ? r.data.size() : 1);
+    if (!out->data) return finish(MMR_STATUS_INTERNAL_ERROR, "out of host memory");
+    memcpy(out->data, r.data.data(), r.data.size());
+    out->len = r.data.size();
+    return finish(MMR_STATUS_OK, "");
+}
+
+template <typename F>
+mmr_status encode_entry(const mmr_video_frame_view *frame, mmr_buffer *out, F &&encode) {
+    if (!frame) return invalid_argument("frame is null");
+    if (!out) return invalid_argument("out_buffer is null");
+    if (frame->struct_size != sizeof(mmr_video_frame_view)) {
+        char m[128];
+        snprintf(m, sizeof m, "frame struct_size is %zu, expected %zu", frame->struct_size, sizeof(mmr_video_frame_view));
+        return invalid_argument(m);
+    }
+    if (check_buffer(out) != MMR_STATUS_OK) return MMR_STATUS_INVALID_ARGUMENT;
+    reset_buffer(out);
+    mmr::FrameIn f;
+    memset(&f, 0, sizeof(f));
+    mmr_status st = frame_from_view(frame, f);
+    if (st != MMR_STATUS_OK) return st;
+    return emit_buffer(encode(f), out);
+}
+
+mmr_status outside_scope(const char *what) {
+    return finish(MMR_STATUS_UNSUPPORTED, std::string("unsupported: ") + what +
+                                              " is outside this library, which implements the MJPEG and DV25 paths");
+}
+
+}  // namespace
+
+struct mmr_gpu_context {
+    Engine *engine;
+    double last_ms;
+    uint32_t last_launches;
+    mmr::EngineTimes times;
+};
+
+extern "C" {
+
+MMR_API uint32_t mmr_abi_version(void) { return MMR_ABI_VERSION; }
+
+MMR_API const char *mmr_version(void) { return kVersion; }
+
+MMR_API size_t mmr_last_error_message(char *buffer, size_t capacity) {
+    size_t required = g_last_error.size() + 1;
+    if (buffer && capacity > 0) {
+        size_t copied = g_last_error.size() < capacity - 1 ? g_last_error.size() : capacity - 1;
+        memcpy(buffer, g_last_error.data(), copied);
+        buffer[copied] = 0;
+    }
+    return required;
+}
+
+MMR_API mmr_status mmr_mjpeg_decode(const uint8_t *data, size_t len, mmr_video_frame *out_frame) {
+    try {
+        return decode_one(mmr::kCodecMjpeg, data, len, out_frame);
+    } catch (...) {
+        return finish(MMR_STATUS_INTERNAL_ERROR, "panic contained at MMRecode C API boundary");
+    }
+}
+
+MMR_API mmr_status mmr_dv_decode(const uint8_t *data, size_t len, mmr_video_frame *out_frame) {
+    try {
+        return decode_one(mmr::kCodecDv, data, len, out_frame);
+    } catch (...) {
+        return finish(MMR_STATUS_INTERNAL_ERROR, "panic contained at MMRecode C API boundary");
+    }
+}
+
+MMR_API mmr_status mmr_mpeg2_picture_count(const uint8_t *, size_t, size_t *out_count) {
+    if (out_count) *out_count = 0;
+    return outside_scope("MPEG-2 video");
+}
+
+MMR_API mmr_status mmr_mpeg2_decode_picture(const uint8_t *, size_t, size_t, mmr_video_frame *out_frame) {
+    if (out_frame && out_frame->struct_size == sizeof(mmr_video_frame)) reset_frame(out_frame);
+    return outside_scope("MPEG-2 video");
+}
+
+MMR_API void mmr_video_frame_free(mmr_video_frame *frame) {
+    if (!frame) return;
+    free_frame_planes(frame);
+    reset_frame(frame);
+}
+
+MMR_API mmr_status mmr_mjpeg_encode(const mmr_video_frame_view *frame, uint8_t quality, mmr_buffer *out_buffer) {
+    try {
+        return encode_entry(frame, out_buffer, [&](const mmr::FrameIn &f) {
+            mmr::JpegEncodeOptions o;
+            o.quality = quality;
+            return mmr::encode_jpeg(f, o);
+        });
+    } catch (...) {
+        return finish(MMR_STATUS_INTERNAL_ERROR, "panic contained at MMRecode C API boundary");
+    }
+}
+
+MMR_API mmr_status mmr_dv_encode(const mmr_video_frame_view *frame, mmr_buffer *out_buffer) {
+    try {
+        return encode_entry(frame, out_buffer, [&](const mmr::FrameIn &f) { return mmr::encode_dv(f, mmr::kDvMode88); });
+    } catch (...) {
+        return finish(MMR_STATUS_INTERNAL_ERROR, "panic contained at MMRecode C API boundary");
+    }
+}
+
+MMR_API mmr_status mmr_mpeg2_encode(const mmr_video_frame_view *, size_t, const mmr_mpeg2_encode_options *,
+                                    mmr_buffer *out_buffer) {
+    if (out_buffer && out_buffer->struct_size == sizeof(mmr_buffer)) reset_buffer(out_buffer);
+    return outside_scope("MPEG-2 video");
+}
+
+MMR_API mmr_status mmr_mpegts_mux_mpeg2(const uint8_t *, size_t, mmr_buffer *out_buffer) {
+    if (out_buffer && out_buffer->struct_size == sizeof(mmr_buffer)) reset_buffer(out_buffer);
+    return outside_scope("MPEG-TS");
+}
+
+MMR_API mmr_status mmr_mpegts_mux_mpeg2_mp2(const uint8_t *, size_t, const uint8_t *, size_t, mmr_buffer *out_buffer) {
+    if (out_buffer && out_buffer->struct_size == sizeof(mmr_buffer)) reset_buffer(out_buffer);
+    return outside_scope("MPEG-TS");
+}
+
+MMR_API mmr_status mmr_mpegts_demux_mpeg2(const uint8_t *, size_t, mmr_buffer *out_buffer) {
+    if (out_buffer && out_buffer->struct_size == sizeof(mmr_buffer)) reset_buffer(out_buffer);
+    return outside_scope("MPEG-TS");
+}
+
+MMR_API mmr_status mmr_mpegts_demux_mp2(const uint8_t *, size_t, mmr_buffer *out_buffer) {
+    if (out_buffer && out_buffer->struct_size == sizeof(mmr_buffer)) reset_buffer(out_buffer);
+    return outside_scope("MPEG-TS");
+}
+
+MMR_API void mmr_buffer_free(mmr_buffer *buffer) {
+    if (!buffer) return;
+    free(buffer->data);
+    reset_buffer(buffer);
+}
+
+// ------------------------------------------------------------ GPU API ---
+
+MMR_API mmr_status mmr_gpu_context_create(const mmr_gpu_config *config, mmr_gpu_context **out_context) {
+    if (!out_context) return invalid_argument("out_context is null");
+    *out_context = nullptr;
+    int device = 0;
+    if (config) {
+        if (config->struct_size != sizeof(mmr_gpu_config)) return invalid_argument("config struct_size mismatch");
+        device = config->device;
+    }
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) {
+        cudaGetLastError();
+        return finish(MMR_STATUS_INTERNAL_ERROR, "no usable CUDA device for the GPU decoder");
+    }
+    try {
+        mmr_gpu_context *c = new mmr_gpu_context{new Engine(device), 0.0, 0, mmr::EngineTimes()};
+        *out_context = c;
+        return finish(MMR_STATUS_OK, "");
+    } catch (const std::exception &e) {
+        return finish(MMR_STATUS_INTERNAL_ERROR, std::string("could not initialise the GPU decoder: ") + e.what());
+    }
+}
+
+MMR_API void mmr_gpu_context_destroy(mmr_gpu_context *context) {
+    if (!context) return;
+    delete context->engine;
+    delete context;
+}
+
+MMR_API mmr_status mmr_gpu_probe(uint32_t codec, const uint8_t *data, size_t len, mmr_gpu_frame_info *info) {
+    if (!info) return invalid_argument("info is null");
+    if (info->struct_size != sizeof(mmr_gpu_frame_info)) return invalid_argument("info struct_size mismatch");
+    if (len > 0 && !data) return invalid_argument("data is null while length is nonzero");
+    mmr::Probe p = mmr::probe_packet(codec, data, len);
+    memset(info, 0, sizeof(*info));
+    info->struct_size = sizeof(*info);
+    info->status = p.status;
+    info->format = p.format;
+    info->range = p.range;
+    info->width = p.width;
+    info->height = p.height;
+    info->plane_count = p.plane_count;
+    for (int c = 0; c < 3; c++) {
+        info->plane_width[c] = p.plane_width[c];
+        info->plane_height[c] = p.plane_height[c];
+    }
+    info->planar_bytes = p.planar_bytes;
+    info->rgb_bytes = p.rgb_bytes;
+    return finish(MMR_STATUS_OK, "");
+}
+
+MMR_API mmr_status mmr_gpu_decode_batch(mmr_gpu_context *context, mmr_gpu_item *items, size_t count) {
+    if (!context) return invalid_argument("context is null");
+    if (count && !items) return invalid_argument("items is null");
+    try {
+        std::vector<Item> v(count);
+        for (size_t i = 0; i < count; i++) {
+            const mmr_gpu_item &g = items[i];
+            if (g.struct_size != sizeof(mmr_gpu_item)) return invalid_argument("item struct_size mismatch");
+            if (g.len > 0 && !g.data) return invalid_argument("item data is null while length is nonzero");
+            v[i].data = g.data;
+            v[i].dev_data = g.device_data;
+            v[i].len = g.len;
+            v[i].codec = g.codec;
+            v[i].output = g.output;
+            v[i].flags = (g.flags & MMR_ITEM_CONCEAL) ? mmr::kFlagConceal : 0;
+            v[i].out = g.out;
+            v[i].out_capacity = g.out_capacity;
+            v[i].out_on_device = (g.flags & MMR_ITEM_OUT_DEVICE) != 0;
+        }
+        mmr::EngineTimes t;
+        int32_t st = context->engine->decode(v.data(), count, &t);
+        context->last_ms = t.device_ms;
+        context->last_launches = context->engine->last_launches();
+        context->times = t;
+        for (size_t i = 0; i < count; i++) {
+            mmr_gpu_item &g = items[i];
+            const Item &it = v[i];
+            g.status = it.status;
+            g.format = it.format;
+            g.range = it.range;
+            g.width = it.width;
+            g.height = it.height;
+            g.plane_count = it.plane_count;
+            for (int c = 0; c < 3; c++) {
+                g.plane_offset[c] = it.plane_offset[c];
+                g.plane_width[c] = it.plane_width[c];
+                g.plane_height[c] = it.plane_height[c];
+            }
+            g.out_bytes = it.out_bytes;
+            g.concealed_segments = (uint32_t)it.concealed.size();
+            std::string m = it.status == MMR_STATUS_OK ? std::string() : with_prefix(it.status, it.message);
+            snprintf(g.message, sizeof g.message, "%s", m.c_str());
+        }
+        if (st != mmr::kOk) return finish(MMR_STATUS_INTERNAL_ERROR, "CUDA device failure during batch decode");
+        return finish(MMR_STATUS_OK, "");
+    } catch (...) {
+        return finish(MMR_STATUS_INTERNAL_ERROR, "panic contained at MMRecode C API boundary");
+    }
+}
+
+MMR_API double mmr_gpu_last_batch_ms(const mmr_gpu_context *context) { return context ? context->last_ms : 0.0; }
+
+MMR_API uint32_t mmr_gpu_last_batch_launches(const mmr_gpu_context *context) {
+    return context ? context->last_launches : 0;
+}
+
+MMR_API mmr_status mmr_gpu_last_batch_stats(const mmr_gpu_context *context, mmr_gpu_batch_stats *stats) {
+    if (!context || !stats) return invalid_argument("context or stats is null");
+    if (stats->struct_size != sizeof(mmr_gpu_batch_stats)) return invalid_argument("stats struct_size mismatch");
+    const mmr::EngineTimes &t = context->times;
+    stats->total_ms = t.device_ms;
+    stats->upload_ms = t.upload_ms;
+    stats->scan_ms = t.scan_ms;
+    stats->entropy_ms = t.entropy_ms;
+    stats->idct_ms = t.idct_ms;
+    stats->dv_ms = t.dv_ms;
+    stats->rgb_ms = t.rgb_ms;
+    stats->download_ms = t.download_ms;
+    stats->input_bytes = t.input_bytes;
+    stats->output_bytes = t.output_bytes;
+    stats->jpeg_blocks = t.jpeg_blocks;
+    stats->dv_blocks = t.dv_blocks;
+    stats->rgb_pixels = t.rgb_pixels;
+    stats->launches = context->last_launches;
+    return finish(MMR_STATUS_OK, "");
+}
+
+MMR_API mmr_status mmr_mjpeg_encode_ex(const mmr_video_frame_view *frame, const mmr_jpeg_encode_options *options,
+                                       mmr_buffer *out_buffer) {
+    if (!options) return invalid_argument("options is null");
+    if (options->struct_size != sizeof(mmr_jpeg_encode_options)) return invalid_argument("options struct_size mismatch");
+    try {
+        return encode_entry(frame, out_buffer, [&](const mmr::FrameIn &f) {
+            mmr::JpegEncodeOptions o;
+            o.quality = options->quality;
+            o.annex_k = options->annex_k_huffman != 0;
+            o.restart_interval = options->restart_interval;
+            return mmr::encode_jpeg(f, o);
+        });
+    } catch (...) {
+        return finish(MMR_STATUS_INTERNAL_ERROR, "panic contained at MMRecode C API boundary");
+    }
+}
+
+MMR_API mmr_status mmr_dv_encode_ex(const mmr_video_frame_view *frame, uint32_t mode_policy, mmr_buffer *out_buffer) {
+    if (mode_policy > MMR_DV_MODE_ACTIVITY) return invalid_argument("unknown DV mode policy");
+    try {
+        return encode_entry(frame, out_buffer, [&](const mmr::FrameIn &f) { return mmr::encode_dv(f, mode_policy); });
+    } catch (...) {
+        return finish(MMR_STATUS_INTERNAL_ERROR, "panic contained at MMRecode C API boundary");
+    }
+}
+
+}  // extern "C"

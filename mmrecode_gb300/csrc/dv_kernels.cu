@@ -1,0 +1,470 @@
+// DV25 decode kernels for sm_103a.
+//
+//   dif_check  one thread per 80-byte DIF block: identifier vs canonical layout
+//              (crates/codecs/dv/src/dif.rs:181-253).
+//   segment    one thread per video segment (5 macroblocks, 30 blocks):
+//              DC/mode/class fields, VLC decode and the three-level spill of
+//              unused bits -- block region, macroblock pool, segment pool
+//              (dv/src/decoder.rs:152-317); writes dequantised coefficients.
+//   resolve    first failing segment per frame (sequential semantics).
+//   idct       one thread per sample: the reference's binary64 8-8 direct sum
+//              or 2-4-8 field transform (decoder.rs:520-602) in its exact
+//              operation order, then placement (decoder.rs:395-505).
+#include <cuda_runtime.h>
+
+#include "kernels.h"
+#include "tables.h"
+
+namespace mmr {
+
+__constant__ int c_dv_zz88[64] = MMR_ZIGZAG_INIT;
+__constant__ int c_dv_zz248[64] = MMR_DV_ZIGZAG_248_INIT;
+__constant__ uint8_t c_dv_shifts[88] = MMR_DV_QUANT_SHIFTS_INIT;
+__constant__ int c_dv_qoff[4] = MMR_DV_QUANT_OFFSET_INIT;
+__constant__ int32_t c_dv_w88[64] = MMR_DV_IWEIGHT_88_INIT;
+__constant__ int32_t c_dv_w248[64] = MMR_DV_IWEIGHT_248_INIT;
+__constant__ double c_cos16[128] = {
+#include "cos_table.inc"
+};
+
+namespace {
+
+__device__ __forceinline__ uint32_t upper_index32(const uint32_t *first, uint32_t n, uint32_t x) {
+    uint32_t lo = 0, hi = n;
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (first[mid] <= x) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// dif.rs:235-253 expected_id
+__device__ __forceinline__ void expected_id(uint32_t pos, uint32_t *section, uint32_t *number) {
+    if (pos == 0) {
+        *section = 0;
+        *number = 0;
+    } else if (pos <= 2) {
+        *section = 1;
+        *number = pos - 1;
+    } else if (pos <= 5) {
+        *section = 2;
+        *number = pos - 3;
+    } else {
+        uint32_t av = pos - 6;
+        if (av % 16 == 0) {
+            *section = 3;
+            *number = av / 16;
+        } else {
+            *section = 4;
+            *number = (av - av / 16 - 1) & 0xff;
+        }
+    }
+}
+
+__global__ void dif_check_kernel(DvLaunch L) {
+    uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= L.n_dif) return;
+    uint32_t f = upper_index32(L.dif_first, L.n_frames, g);
+    uint32_t local = g - L.dif_first[f];
+    const uint8_t *b = L.frames[f].in + (size_t)local * 80;
+    uint32_t es, en;
+    expected_id(local % 150, &es, &en);
+    bool bad = (uint32_t)(b[0] >> 5) != es || (uint32_t)(b[1] >> 4) != local / 150 || (uint32_t)b[2] != en;
+    L.flags[g] = bad ? 1 : 0;
+}
+
+// ---- bit buffers (MSB-first, 32-bit words) ----
+
+__device__ __forceinline__ uint32_t get32(const uint32_t *w, uint32_t bit) {
+    uint32_t i = bit >> 5, r = bit & 31;
+    uint32_t hi = w[i] << r;
+    return r ? hi | (w[i + 1] >> (32 - r)) : hi;
+}
+
+// Appends bits [start, start+n) of src to dst (which holds dn bits, zero beyond).
+__device__ __forceinline__ void append_bits(uint32_t *dst, uint32_t &dn, const uint32_t *src, uint32_t start,
+                                            uint32_t n) {
+    while (n) {
+        uint32_t k = n < 32 ? n : 32;
+        uint32_t v = get32(src, start) >> (32 - k);  // k bits, right-aligned
+        uint32_t i = dn >> 5, r = dn & 31;
+        // place v's k bits at bit offset r of word i
+        uint64_t sh = (uint64_t)v << (64 - r - k);
+        dst[i] |= (uint32_t)(sh >> 32);
+        if (r + k > 32) dst[i + 1] |= (uint32_t)sh;
+        dn += k;
+        start += k;
+        n -= k;
+    }
+}
+
+struct DvBlock {
+    uint8_t position;
+    uint8_t complete;
+    uint8_t mode;     // 1 = 2-4-8
+    uint8_t cls;
+    uint16_t pval;    // partial bits (< 16), right-aligned
+    uint8_t plen;
+    uint8_t pad;
+};
+
+// consume_ac (decoder.rs:245-284) on the virtual stream (partial bits ++ buf[pos, end)).
+// On completion *pos is left after the EOB; otherwise the remaining bits become the
+// block's partial and *pos == end.
+__device__ void consume_ac(DvBlock &b, const uint32_t *buf, uint32_t &pos, uint32_t end, int16_t *coef,
+                           uint32_t qno, const uint32_t *__restrict__ vlc, bool &bad_vlc) {
+    if (b.complete) return;
+    uint32_t pval = b.pval;
+    int plen = b.plen;
+    b.plen = 0;
+    b.pval = 0;
+    for (;;) {
+        uint32_t avail = (uint32_t)plen + (end - pos);
+        // next 16 bits of (partial ++ input), zero-padded
+        uint32_t w16;
+        if (plen) {
+            uint32_t rest = get32(buf, pos) >> 16;  // 16 bits from pos (beyond end: don't care, masked below)
+            w16 = ((pval << (16 - plen)) | (rest >> plen)) & 0xffffu;
+        } else {
+            w16 = get32(buf, pos) >> 16;
+        }
+        if (avail < 16) w16 &= 0xffffu << (16 - avail);
+        uint32_t e = vlc[w16 >> (16 - kDvVlcL1Bits)];
+        if (e & 0x80000000u) e = vlc[(e & 0xffffu) + (w16 & ((1u << (16 - kDvVlcL1Bits)) - 1))];
+        uint32_t len = e & 31;
+        if (len != 0 && len <= avail) {
+            // consume len bits: all partial bits first (a partial never holds a whole code)
+            if ((int)len <= plen) {
+                plen -= (int)len;
+                pval &= (1u << plen) - 1;
+            } else {
+                pos += len - (uint32_t)plen;
+                plen = 0;
+                pval = 0;
+            }
+            uint32_t run = (e >> 5) & 127;
+            int32_t level = (int32_t)((e >> 12) & 511) - 256;
+            uint32_t p = b.position + run + 1;
+            if (p >= 64) {
+                b.position = 64;
+                b.complete = 1;
+                return;
+            }
+            b.position = (uint8_t)p;
+            if (level != 0) {
+                // inverse_factor_for_encoding (decoder.rs:290-310)
+                uint32_t q = qno + (uint32_t)c_dv_qoff[b.cls];
+                uint32_t area = p <= 5 ? 0 : p <= 20 ? 1 : p <= 42 ? 2 : 3;
+                int32_t weight = b.mode ? c_dv_w248[p] : c_dv_w88[p];
+                int32_t factor = weight << (c_dv_shifts[q * 4 + area] + 1 + (b.cls == 3));
+                int32_t lv = (level * factor + 8192) >> 14;
+                coef[b.mode ? c_dv_zz248[p] : c_dv_zz88[p]] = (int16_t)lv;
+            }
+        } else if (avail < 16) {
+            // save as partial: remaining partial bits then the rest of the input
+            uint32_t v = pval;
+            int n = plen;
+            uint32_t in_n = end - pos;
+            if (in_n) {
+                v = (v << in_n) | (get32(buf, pos) >> (32 - in_n));
+                n += (int)in_n;
+            }
+            b.pval = (uint16_t)v;
+            b.plen = (uint8_t)n;
+            pos = end;
+            return;
+        } else {
+            bad_vlc = true;  // unreachable: the DV VLC code is complete (Kraft sum 1)
+            pos = end;
+            return;
+        }
+    }
+}
+
+constexpr int kSegThreads = 64;
+
+__global__ void __launch_bounds__(kSegThreads) segment_kernel(DvLaunch L) {
+    uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= L.n_segments) return;
+    uint32_t f = upper_index32(L.seg_first, L.n_frames, g);
+    const DvFrame &F = L.frames[f];
+    uint32_t local = g - L.seg_first[f];
+    uint32_t sequence = local / 27, slot = local % 27;
+    uint16_t kind = kDiagNone;
+
+    uint32_t dif[5];
+    for (int m = 0; m < 5; m++) {
+        uint32_t vn = slot * 5 + m;
+        dif[m] = sequence * 150 + 7 + (vn / 15) * 16 + vn % 15;
+        if (kind == kDiagNone && L.flags[F.dif_first + dif[m]]) kind = kDvDamagedId;
+    }
+    if (kind == kDiagNone) {
+        // payload words of the 5 macroblocks (bytes 4..80 of each DIF block)
+        uint32_t pay[5 * 19 + 1];
+        for (int m = 0; m < 5; m++) {
+            const uint8_t *src = F.in + (size_t)dif[m] * 80 + 4;
+            for (int i = 0; i < 19; i++)
+                pay[m * 19 + i] = ((uint32_t)src[4 * i] << 24) | ((uint32_t)src[4 * i + 1] << 16) |
+                                  ((uint32_t)src[4 * i + 2] << 8) | (uint32_t)src[4 * i + 3];
+        }
+        pay[95] = 0;
+        uint32_t segpool[5 * 19 + 2];
+        for (int i = 0; i < 97; i++) segpool[i] = 0;
+        uint32_t segn = 0;
+        DvBlock blk[30];
+        int16_t *coef = L.coef + (F.blk_off + (uint64_t)local * 30) * 64;
+        bool bad_vlc = false;
+        const uint32_t kRegion[6] = {0, 112, 224, 336, 448, 528};
+        const uint32_t kBits[6] = {112, 112, 112, 112, 80, 80};
+        for (int m = 0; m < 5; m++) {
+            // decode_macroblock (decoder.rs:193-223)
+            uint32_t qno = F.in[(size_t)dif[m] * 80 + 3] & 0x0f;
+            const uint32_t *w = pay + m * 19;
+            uint32_t mbpool[20];
+            for (int i = 0; i < 20; i++) mbpool[i] = 0;
+            uint32_t mbn = 0;
+            for (int j = 0; j < 6; j++) {
+                DvBlock &b = blk[m * 6 + j];
+                uint32_t r0 = kRegion[j];
+                uint32_t head = get32(w, r0) >> 20;  // 12 bits: dc(9) mode(1) class(2)
+                int32_t dc = (int32_t)(head >> 3);
+                if (dc & 0x100) dc -= 512;
+                b.position = 0;
+                b.complete = 0;
+                b.mode = (head >> 2) & 1;
+                b.cls = head & 3;
+                b.pval = 0;
+                b.plen = 0;
+                int16_t *bc = coef + (m * 6 + j) * 64;
+                bc[0] = (int16_t)(dc * 4 + 1024);
+                uint32_t pos = r0 + 12, end = r0 + kBits[j];
+                consume_ac(b, w, pos, end, bc, qno, L.vlc, bad_vlc);
+                if (b.complete) append_bits(mbpool, mbn, w, pos, end - pos);
+            }
+            // consume_pool over the macroblock (decoder.rs:235-243)
+            uint32_t pos = 0;
+            for (int j = 0; j < 6; j++) {
+                DvBlock &b = blk[m * 6 + j];
+                if (!b.complete && pos < mbn)
+                    consume_ac(b, mbpool, pos, mbn, coef + (m * 6 + j) * 64, qno, L.vlc, bad_vlc);
+            }
+            if (pos < mbn) append_bits(segpool, segn, mbpool, pos, mbn - pos);
+        }
+        // consume_pool_for_macroblocks (decoder.rs:225-233)
+        uint32_t pos = 0;
+        for (int j = 0; j < 30; j++) {
+            DvBlock &b = blk[j];
+            if (!b.complete && pos < segn) {
+                uint32_t qno = F.in[(size_t)dif[j / 6] * 80 + 3] & 0x0f;
+                consume_ac(b, segpool, pos, segn, coef + j * 64, qno, L.vlc, bad_vlc);
+            }
+        }
+        if (bad_vlc) kind = kDvBadVlc;
+        else
+            for (int j = 0; j < 30; j++)
+                if (!blk[j].complete) {
+                    kind = kDvIncomplete;
+                    break;
+                }
+        uint8_t *modes = L.modes + F.blk_off + (uint64_t)local * 30;
+        for (int j = 0; j < 30; j++) modes[j] = blk[j].mode;
+    }
+    L.seg_err[g] = (uint8_t)kind;
+    if (kind != kDiagNone) {
+        atomicMin(&L.states[f].bad_segment, local);
+        atomicAdd(&L.states[f].failed, 1u);
+    }
+}
+
+__global__ void dv_resolve_kernel(DvLaunch L) {
+    uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= L.n_frames) return;
+    DvState *st = &L.states[f];
+    uint32_t bad = st->bad_segment;
+    if (bad != 0xffffffffu) {
+        uint16_t kind = L.seg_err[L.frames[f].seg_first + bad];
+        st->diag = make_diag(kind, 0, bad % 27, bad / 27);
+        if (!L.frames[f].conceal) L.item_ok[L.frames[f].item] = 0;
+    }
+}
+
+// decoder.rs:395-422 macroblock_coordinates (in 8-sample units)
+__device__ __forceinline__ void mb_coords(bool pal, uint32_t seqs, uint32_t sequence, uint32_t slot, uint32_t m,
+                                          uint32_t *mbx, uint32_t *mby) {
+    const uint32_t OFF[5] = {2, 6, 8, 0, 4};
+    const uint32_t SHUF3[5] = {18, 9, 27, 0, 36};
+    const uint32_t LSTART[5] = {9, 4, 13, 0, 18};
+    if (pal) {
+        // SERPENT1[slot] = 0,1,2,2,1,0 repeating
+        uint32_t s6 = slot % 6;
+        uint32_t serp1 = s6 < 3 ? s6 : 5 - s6;
+        uint32_t x = SHUF3[m] + slot / 3;
+        uint32_t y = serp1 + ((sequence + OFF[m]) % seqs) * 3;
+        *mbx = x * 2;
+        *mby = y * 2;
+    } else {
+        uint32_t row = (sequence + OFF[m]) % seqs;
+        uint32_t k = slot + ((m == 1 || m == 2) ? 3 : 0);
+        uint32_t x = LSTART[m] + k / 6;
+        // SERPENT2[k] = 0..5,5..0 repeating
+        uint32_t k12 = k % 12;
+        uint32_t serp2 = k12 < 6 ? k12 : 11 - k12;
+        uint32_t y = serp2 + row * 6;
+        if (x > 21) y = y * 2 - row * 6;
+        *mbx = x * 4;
+        *mby = y;
+    }
+}
+
+constexpr int kIdctThreads = 256;  // 4 blocks x 64 samples
+
+__global__ void __launch_bounds__(kIdctThreads) dv_idct_kernel(DvLaunch L) {
+    __shared__ int32_t s_c[4][64];
+    __shared__ double s_h[4][64];
+    int lb = threadIdx.x >> 6, px = threadIdx.x & 63;
+    uint64_t gb = (uint64_t)blockIdx.x * 4 + lb;
+    bool valid = gb < L.n_blocks;
+    uint32_t f = 0, local_blk = 0;
+    const DvFrame *F = nullptr;
+    bool failed = false, mode = false;
+    if (valid) {
+        // frame from block index: blocks of frame f are [blk_off, blk_off + sequences*27*30)
+        uint32_t lo = 0, hi = L.n_frames;
+        while (hi - lo > 1) {
+            uint32_t mid = (lo + hi) >> 1;
+            if (L.frames[mid].blk_off <= gb) lo = mid;
+            else hi = mid;
+        }
+        f = lo;
+        F = &L.frames[f];
+        local_blk = (uint32_t)(gb - F->blk_off);
+        valid = L.item_ok[F->item] != 0;
+        if (valid) {
+            failed = L.seg_err[F->seg_first + local_blk / 30] != 0;
+            mode = L.modes[gb] != 0;
+            s_c[lb][px] = failed ? 0 : (int32_t)L.coef[gb * 64 + px];
+        }
+    }
+    __syncthreads();
+    int y = px >> 3, x = px & 7;
+    const double kFrac = 0.7071067811865476;  // FRAC_1_SQRT_2
+    double value = 0.0;
+    if (valid && !failed && mode) {
+        // inverse_248 (decoder.rs:555-602): butterfly, horizontal pass per row, field pass
+        int row = y;
+        int pair = row >> 1;
+        double sum = 0.0;
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            double first = (double)s_c[lb][pair * 16 + u];
+            double second = (double)s_c[lb][pair * 16 + 8 + u];
+            double b = (row & 1) ? __dsub_rn(first, second) : __dadd_rn(first, second);
+            if (b != 0.0) {
+                double cu = u == 0 ? kFrac : 1.0;
+                sum = __dadd_rn(sum, __dmul_rn(__dmul_rn(cu, b), c_cos16[(2 * x + 1) * u]));
+            }
+        }
+        s_h[lb][row * 8 + x] = sum / 2.0;
+    }
+    __syncthreads();
+    if (!valid) return;
+    if (!failed) {
+        if (mode) {
+            int field = y & 1, yy = y >> 1;  // output row y = 2*yy + field
+            double sum = 0.0;
+#pragma unroll
+            for (int v = 0; v < 4; v++) {
+                double h = s_h[lb][(v * 2 + field) * 8 + x];
+                if (h != 0.0) {
+                    double cv = v == 0 ? kFrac : 1.0;
+                    sum = __dadd_rn(sum, __dmul_rn(__dmul_rn(cv, h), c_cos16[2 * (2 * yy + 1) * v]));
+                }
+            }
+            value = sum / 2.0;
+        } else {
+            // inverse_88 (decoder.rs:520-548): direct 64-term sum in (v, u) order
+            const double kk00 = __dmul_rn(kFrac, kFrac);
+            double sum = 0.0;
+            for (int v = 0; v < 8; v++) {
+                for (int u = 0; u < 8; u++) {
+                    int32_t c = s_c[lb][v * 8 + u];
+                    if (c == 0) continue;
+                    double k = (u == 0 && v == 0) ? kk00 : (u == 0 || v == 0) ? kFrac : 1.0;
+                    double t = __dmul_rn(k, (double)c);
+                    t = __dmul_rn(t, c_cos16[(2 * x + 1) * u]);
+                    t = __dmul_rn(t, c_cos16[(2 * y + 1) * v]);
+                    sum = __dadd_rn(sum, t);
+                }
+            }
+            value = sum / 4.0;
+        }
+    }
+    uint8_t sample;
+    if (failed) {
+        sample = 0;  // set below per plane (limited-range black)
+    } else {
+        double r = fmin(fmax(round(value), 0.0), 255.0);
+        sample = (uint8_t)r;
+    }
+    // placement (decoder.rs:432-505)
+    uint32_t seg = local_blk / 30, j = local_blk % 30;
+    uint32_t sequence = seg / 27, slot = seg % 27, m = j / 6, bi = j % 6;
+    uint32_t mbx, mby;
+    mb_coords(F->pal != 0, F->sequences, sequence, slot, m, &mbx, &mby);
+    uint32_t X = mbx * 8, Y = mby * 8;
+    uint32_t W = F->width, H = F->height, cw = F->cw, ch = F->ch;
+    uint8_t *yp = F->planes, *cbp = F->planes + (size_t)W * H, *crp = cbp + (size_t)cw * ch;
+    uint32_t bx, by;
+    uint8_t *plane;
+    uint32_t pw;
+    bool chroma = bi >= 4;
+    if (F->pal || mbx >= 88) {
+        if (!chroma) {
+            bx = X + (bi & 1) * 8;
+            by = Y + (bi >> 1) * 8;
+            plane = yp;
+            pw = W;
+        } else {
+            plane = bi == 4 ? crp : cbp;
+            pw = cw;
+            if (F->pal) {
+                bx = X / 2;
+                by = Y / 2;
+            } else {  // put_split_chroma: columns 0-3 to rows y.., 4-7 to rows y+8..
+                bx = X / 4 - (x >= 4 ? 4 : 0);
+                by = Y + (x >= 4 ? 8 : 0);
+            }
+        }
+    } else {
+        if (!chroma) {
+            bx = X + bi * 8;
+            by = Y;
+            plane = yp;
+            pw = W;
+        } else {
+            plane = bi == 4 ? crp : cbp;
+            pw = cw;
+            bx = X / 4;
+            by = Y;
+        }
+    }
+    if (failed) sample = chroma ? 128 : 16;
+    plane[(size_t)(by + y) * pw + bx + x] = sample;
+}
+
+}  // namespace
+
+void launch_dv_decode(const DvLaunch &L, cudaStream_t s) {
+    if (L.n_dif) dif_check_kernel<<<(L.n_dif + 255) / 256, 256, 0, s>>>(L);
+    if (L.n_segments) segment_kernel<<<(L.n_segments + kSegThreads - 1) / kSegThreads, kSegThreads, 0, s>>>(L);
+    if (L.n_frames) dv_resolve_kernel<<<(L.n_frames + 127) / 128, 128, 0, s>>>(L);
+}
+
+void launch_dv_idct(const DvLaunch &L, cudaStream_t s) {
+    if (L.n_blocks == 0) return;
+    uint64_t grid = (L.n_blocks + 3) / 4;
+    dv_idct_kernel<<<(unsigned)grid, kIdctThreads, 0, s>>>(L);
+}
+
+}  // namespace mmr

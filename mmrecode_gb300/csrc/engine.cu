@@ -1,0 +1,1248 @@
+// Batch decode engine (host side): planning, device arenas, launches, status.
+#include "engine.h"
+
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <array>
+#include <map>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "jpeg_syntax.h"
+#include "kernels.h"
+#include "plan.h"
+#include "tables.h"
+
+namespace mmr {
+
+namespace {
+
+const int kZigzag[64] = MMR_ZIGZAG_INIT;
+
+inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+struct CudaError : std::runtime_error {
+    explicit CudaError(const std::string &m) : std::runtime_error(m) {}
+};
+
+#define MMR_CUDA(call)                                                                                  \
+    do {                                                                                                \
+        cudaError_t e_ = (call);                                                                        \
+        if (e_ != cudaSuccess) throw CudaError(std::string(#call) + ": " + cudaGetErrorString(e_));     \
+    } while (0)
+
+// Grow-only device allocation.
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t cap = 0;
+    void ensure(size_t n) {
+        if (n <= cap) return;
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        size_t c = std::max(n, cap + cap / 2);
+        c = align_up(c, 4096);
+        MMR_CUDA(cudaMalloc(&ptr, c));
+        cap = c;
+    }
+    ~DevBuf() {
+        if (ptr) cudaFree(ptr);
+    }
+    template <typename T>
+    T *as() const {
+        return reinterpret_cast<T *>(ptr);
+    }
+};
+
+struct PinBuf {
+    void *ptr = nullptr;
+    size_t cap = 0;
+    void ensure(size_t n) {
+        if (n <= cap) return;
+        if (ptr) cudaFreeHost(ptr);
+        ptr = nullptr;
+        size_t c = align_up(std::max(n, cap + cap / 2), 4096);
+        MMR_CUDA(cudaHostAlloc(&ptr, c, cudaHostAllocDefault));
+        cap = c;
+    }
+    ~PinBuf() {
+        if (ptr) cudaFreeHost(ptr);
+    }
+};
+
+// Packs many small arrays into one host image uploaded with a single copy.
+struct Blob {
+    std::vector<uint8_t> bytes;
+    size_t add(const void *src, size_t n, size_t align = 16) {
+        size_t off = align_up(bytes.size(), align);
+        bytes.resize(off + n);
+        if (n) memcpy(bytes.data() + off, src, n);
+        return off;
+    }
+    template <typename T>
+    size_t add_vec(const std::vector<T> &v) {
+        return add(v.data(), v.size() * sizeof(T), 16);
+    }
+};
+
+// ------------------------------------------------------------ MJPEG plan ---
+
+struct JPlan {
+    JpegHeader hdr;
+    bool parsed = false;     // prefix parse reached the first SOS
+    bool tail_known = false; // the tail was parsed on the host already
+    Diag final_diag{};       // decided before the GPU (no GPU work needed)
+    bool final_now = false;
+    Diag prologue{};         // decode_jpeg prologue failure (resolved after the tail)
+    bool decode = false;
+    uint32_t W = 0, H = 0, ncomp = 0, hmax = 1, vmax = 1, interleaved = 0;
+    uint32_t mcu_cols = 0, mcu_rows = 0, total_mcus = 0, ri = 0, n_intervals = 0;
+    std::vector<JComp> comps;
+    std::vector<JSched> sched;
+    uint16_t quant[4][64];
+    int lut_slot_key[8];     // index into the batch's unique LUT list, -1 if absent
+    uint32_t n_blocks = 0;
+    size_t planar_bytes = 0;
+    uint32_t fmt = 0;        // predicted from the header (color model may change in the tail)
+};
+
+// Huffman LUT source: counts + symbols bytes (as in the DHT payload).
+struct LutSource {
+    std::vector<uint8_t> key;  // 16 counts then symbols
+};
+
+// decode_jpeg prologue (decoder.rs:140-167, 223-255, 412-493) evaluated from the header.
+Diag jpeg_prologue(const uint8_t *in, const JpegHeader &h) {
+    if (!h.have_sof) return make_diag(kJNoSof);
+    if (h.scan_count != 1) return make_diag(kJScanCount, 0, h.scan_count);
+    if (h.height == 0) return make_diag(kJDnlHeight);
+    if (h.sos_ncomp != h.ncomp) return make_diag(kJPartialScan);
+    if (h.ss != 0 || h.se != 63 || h.ah != 0 || h.al != 0) return make_diag(kJNotBaseline);
+    const uint8_t *fc = in + h.sof_comp_off;
+    const uint8_t *sc = in + h.sos_comp_off;
+    for (uint32_t c = 0; c < h.ncomp; c++) {
+        uint32_t occ = 0;
+        for (uint32_t k = 0; k < h.sos_ncomp; k++) occ += sc[2 * k] == fc[3 * c];
+        if (occ != 1) return make_diag(kJScanSelect, 0, fc[3 * c]);
+    }
+    if (h.huff_err.kind != kDiagNone) return h.huff_err;
+    for (uint32_t c = 0; c < h.ncomp; c++) {
+        uint8_t tq = fc[3 * c + 2];
+        if (!h.q_present[tq]) return make_diag(kJMissingQuant, 0, fc[3 * c], tq);
+        if (h.q_sixteen[tq]) return make_diag(kJQuant16);
+    }
+    for (uint32_t k = 0; k < h.sos_ncomp; k++) {
+        bool found = false;
+        for (uint32_t c = 0; c < h.ncomp; c++)
+            if (fc[3 * c] == sc[2 * k]) {
+                found = true;
+                break;
+            }
+        if (!found) return make_diag(kJPanic);
+        uint8_t td = sc[2 * k + 1] >> 4, ta = sc[2 * k + 1] & 15;
+        if (!h.h_present[td]) return make_diag(kJMissingDc, 0, td);
+        if (!h.h_present[4 + ta]) return make_diag(kJMissingAc, 0, ta);
+    }
+    return make_diag(kDiagNone);
+}
+
+// into_video_frame's standard_pixel_format (decoder.rs:98-126) from geometry.
+uint32_t predict_format(int color_model, uint32_t ncomp, const uint32_t *pw, const uint32_t *ph, uint32_t W,
+                        uint32_t H, uint16_t *kind) {
+    *kind = kDiagNone;
+    if (color_model == 0 && ncomp == 1 && pw[0] == W && ph[0] == H) return kGray8;
+    if (color_model != 1 || ncomp != 3 || pw[0] != W || ph[0] != H || pw[1] != pw[2] || ph[1] != ph[2]) {
+        *kind = kJFormatComponents;
+        return 0;
+    }
+    if (pw[1] == W && ph[1] == H) return kYuv444;
+    if (pw[1] == (W + 1) / 2 && ph[1] == H) return kYuv422;
+    if (pw[1] == (W + 1) / 2 && ph[1] == (H + 1) / 2) return kYuv420;
+    *kind = kJFormatChroma;
+    return 0;
+}
+
+// infer_color_model (decoder.rs:169-194): 0 gray, 1 ycbcr, 2 rgb, 3 cmyk, 4 ycck, 5 unknown
+int color_model(const JpegHeader &h) {
+    if (h.ncomp == 1) return 0;
+    if (h.ncomp == 3 && h.adobe == 0) return 2;
+    if (h.ncomp == 3 && h.adobe == 1) return 1;
+    if (h.ncomp == 4 && h.adobe == 0) return 3;
+    if (h.ncomp == 4 && h.adobe == 2) return 4;
+    if (h.ncomp == 3 && h.adobe < 0 && h.jfif) return 1;
+    return 5;
+}
+
+void plan_geometry(const uint8_t *in, JPlan &p) {
+    const JpegHeader &h = p.hdr;
+    const uint8_t *fc = in + h.sof_comp_off;
+    p.W = h.width;
+    p.H = h.height;
+    p.ncomp = h.ncomp;
+    p.hmax = 1;
+    p.vmax = 1;
+    for (uint32_t c = 0; c < p.ncomp; c++) {
+        p.hmax = std::max<uint32_t>(p.hmax, fc[3 * c + 1] >> 4);
+        p.vmax = std::max<uint32_t>(p.vmax, fc[3 * c + 1] & 15);
+    }
+    p.interleaved = p.ncomp > 1;
+    uint32_t mcu_w = p.interleaved ? p.hmax * 8 : 8, mcu_h = p.interleaved ? p.vmax * 8 : 8;
+    p.mcu_cols = (p.W + mcu_w - 1) / mcu_w;
+    p.mcu_rows = (p.H + mcu_h - 1) / mcu_h;
+    p.total_mcus = p.mcu_cols * p.mcu_rows;
+    p.comps.resize(p.ncomp);
+    uint32_t blk = 0;
+    size_t out = 0;
+    for (uint32_t c = 0; c < p.ncomp; c++) {
+        JComp &C = p.comps[c];
+        memset(&C, 0, sizeof(C));
+        C.h = fc[3 * c + 1] >> 4;
+        C.v = fc[3 * c + 1] & 15;
+        C.q = fc[3 * c + 2];
+        C.plane_w = (uint32_t)(((uint64_t)p.W * C.h + p.hmax - 1) / p.hmax);
+        C.plane_h = (uint32_t)(((uint64_t)p.H * C.v + p.vmax - 1) / p.vmax);
+        C.bw = p.interleaved ? p.mcu_cols * C.h : p.mcu_cols;
+        C.bh = p.interleaved ? p.mcu_rows * C.v : p.mcu_rows;
+        C.blk_base = blk;
+        C.out_off = (uint32_t)out;
+        blk += C.bw * C.bh;
+        out += (size_t)C.plane_w * C.plane_h;
+    }
+    p.n_blocks = blk;
+    p.planar_bytes = out;
+}
+
+void plan_jpeg(const uint8_t *in, size_t len, JPlan &p) {
+    jpeg_parse_prefix(in, len, &p.hdr);
+    JpegHeader &h = p.hdr;
+    if (h.err.kind != kDiagNone) {
+        p.final_diag = h.err;
+        p.final_now = true;
+        return;
+    }
+    if (!h.have_sos) {
+        // parsed to EOI without any scan
+        p.final_diag = h.have_sof ? make_diag(kJScanCount, 0, 0) : make_diag(kJNoSof);
+        p.final_now = true;
+        return;
+    }
+    p.parsed = true;
+    if (!h.have_sof) {
+        // The first SOF0 (if any) follows the first scan: find that scan's end on the
+        // host and parse the rest of the image before planning the decode.
+        size_t term;
+        Diag e;
+        if (!jpeg_find_first_scan_end(in, len, &h, &term, &e)) {
+            p.final_diag = e;
+            p.final_now = true;
+            return;
+        }
+        jpeg_parse_tail(in, len, term, &h);
+        p.tail_known = true;
+        if (h.err.kind != kDiagNone) {
+            p.final_diag = h.err;
+            p.final_now = true;
+            return;
+        }
+        if (!h.have_sof) {
+            p.final_diag = make_diag(kJNoSof);
+            p.final_now = true;
+            return;
+        }
+    }
+    p.prologue = jpeg_prologue(in, h);
+    if (p.prologue.kind == kJScanCount) p.prologue = make_diag(kDiagNone);  // rechecked after the tail
+    plan_geometry(in, p);
+    uint32_t pw[3] = {0, 0, 0}, ph[3] = {0, 0, 0};
+    for (uint32_t c = 0; c < std::min<uint32_t>(p.ncomp, 3); c++) {
+        pw[c] = p.comps[c].plane_w;
+        ph[c] = p.comps[c].plane_h;
+    }
+    uint16_t fk;
+    p.fmt = predict_format(color_model(h), p.ncomp, pw, ph, p.W, p.H, &fk);
+    if (p.prologue.kind != kDiagNone) return;
+    p.decode = true;
+    uint32_t ri = h.dri ? h.dri : p.total_mcus;
+    p.ri = ri;
+    p.n_intervals = (p.total_mcus + ri - 1) / ri;
+    const uint8_t *fc = in + h.sof_comp_off;
+    const uint8_t *sc = in + h.sos_comp_off;
+    for (uint32_t k = 0; k < h.sos_ncomp; k++) {
+        uint32_t comp = 0;
+        for (uint32_t c = 0; c < p.ncomp; c++)
+            if (fc[3 * c] == sc[2 * k]) {
+                comp = c;
+                break;
+            }
+        uint32_t rows = p.interleaved ? p.comps[comp].v : 1, cols = p.interleaved ? p.comps[comp].h : 1;
+        for (uint32_t by = 0; by < rows; by++)
+            for (uint32_t bx = 0; bx < cols; bx++) {
+                JSched e;
+                memset(&e, 0, sizeof(e));
+                e.comp = (uint16_t)comp;
+                e.bx = (uint8_t)bx;
+                e.by = (uint8_t)by;
+                e.dc = sc[2 * k + 1] >> 4;
+                e.ac = sc[2 * k + 1] & 15;
+                p.sched.push_back(e);
+            }
+    }
+    for (int q = 0; q < 4; q++)
+        for (int k = 0; k < 64; k++) p.quant[q][k] = 0;
+    for (int q = 0; q < 4; q++)
+        if (h.q_present[q] && !h.q_sixteen[q])
+            for (int k = 0; k < 64; k++) p.quant[q][kZigzag[k]] = in[h.q_off[q] + k];
+}
+
+void build_lut(const uint8_t *key, size_t key_len, uint32_t sym_off, HuffLut *lut) {
+    memset(lut, 0, sizeof(*lut));
+    for (int l = 0; l < 18; l++) lut->maxcode[l] = -1;
+    const uint8_t *counts = key;
+    const uint8_t *symbols = key + 16;
+    uint32_t code = 0, k = 0;
+    for (int l = 1; l <= 16; l++) {
+        uint32_t n = counts[l - 1];
+        if (n) {
+            lut->valptr[l] = (int32_t)k - (int32_t)code;
+            lut->maxcode[l] = (int32_t)(code + n - 1);
+        }
+        for (uint32_t i = 0; i < n; i++) {
+            if (l <= 9) {
+                uint32_t first = code << (9 - l), cnt = 1u << (9 - l);
+                for (uint32_t j = 0; j < cnt; j++) lut->fast[first + j] = (uint16_t)((l << 8) | symbols[k]);
+            }
+            code++;
+            k++;
+        }
+        code <<= 1;
+    }
+    lut->sym_off = sym_off;
+    lut->nsym = (uint32_t)(key_len - 16);
+}
+
+// Raw position of the entropy reader after it has consumed n tokens (entropy.rs:143-165).
+size_t raw_after_tokens(const uint8_t *in, size_t len, size_t ds, uint64_t n) {
+    size_t p = ds;
+    uint64_t count = 0;
+    while (count < n && p < len) {
+        if (in[p] != 0xff) {
+            p++;
+            count++;
+            continue;
+        }
+        size_t q = p + 1;
+        while (q < len && in[q] == 0xff) q++;
+        if (q >= len) return len;
+        if (in[q] == 0x00) count++;
+        p = q + 1;
+    }
+    return p;
+}
+
+// -------------------------------------------------------------- DV plan ---
+
+struct DvPlan {
+    bool ok = false;
+    Diag diag{};
+    uint32_t pal = 0, sequences = 0, W = 0, H = 0, cw = 0, ch = 0;
+    size_t planar_bytes = 0;
+};
+
+// profile.rs:87-127 detect_profile
+DvPlan plan_dv(const uint8_t *in, size_t len) {
+    DvPlan p;
+    if (len < 4) {
+        p.diag = make_diag(kDvShortHeader, 0, (uint32_t)len);
+        return p;
+    }
+    if ((in[0] >> 5) != 0) {
+        p.diag = make_diag(kDvNotHeader);
+        return p;
+    }
+    p.pal = (in[3] & 0x80) != 0;
+    size_t size = p.pal ? 144000 : 120000;
+    if (len != size) {
+        p.diag = make_diag(kDvLength, 0, (uint32_t)size, (uint32_t)std::min<size_t>(len, 0xffffffffu));
+        return p;
+    }
+    p.ok = true;
+    p.sequences = p.pal ? 12 : 10;
+    p.W = 720;
+    p.H = p.pal ? 576 : 480;
+    p.cw = p.pal ? 360 : 180;
+    p.ch = p.pal ? 288 : 480;
+    p.planar_bytes = (size_t)p.W * p.H + 2 * (size_t)p.cw * p.ch;
+    return p;
+}
+
+// Two-level DV VLC table (see kernels.h for the entry layout), built from the
+// canonical codes of decoder.rs:319-354.
+std::vector<uint32_t> build_dv_vlc() {
+    struct E {
+        uint32_t code, len, run;
+        int32_t level;
+    };
+    std::vector<E> entries;
+    uint8_t len_of[409];
+    int n = 0;
+    for (auto &r : kDvVlcLenRuns)
+        for (int k = 0; k < r[1]; k++) len_of[n++] = (uint8_t)r[0];
+    uint32_t canonical = 0;
+    for (int i = 0; i < 409; i++) {
+        uint32_t len = len_of[i];
+        uint32_t code = canonical >> (32 - len);
+        canonical += 1u << (32 - len);
+        uint32_t run = i < 153 ? kDvVlcRunHead[i] : 0;
+        int32_t level = i < 153 ? kDvVlcLevelHead[i] : i - 153;
+        if (level == 0) entries.push_back({code, len, run, 0});
+        else {
+            entries.push_back({code << 1, len + 1, run, level});
+            entries.push_back({(code << 1) | 1, len + 1, run, -level});
+        }
+    }
+    const int l1 = kDvVlcL1Bits, l2 = 16 - kDvVlcL1Bits;
+    std::vector<uint32_t> t(1u << l1, 0);
+    for (auto &e : entries) {
+        uint32_t packed = e.len | (e.run << 5) | ((uint32_t)(e.level + 256) << 12);
+        if ((int)e.len <= l1) {
+            uint32_t first = e.code << (l1 - e.len), cnt = 1u << (l1 - e.len);
+            for (uint32_t j = 0; j < cnt; j++) t[first + j] = packed;
+        } else {
+            uint32_t prefix = e.code >> (e.len - l1);
+            if (!(t[prefix] & 0x80000000u)) {
+                uint32_t off = (uint32_t)t.size();
+                t.resize(t.size() + (1u << l2), 0);
+                t[prefix] = 0x80000000u | off;
+            }
+            uint32_t off = t[prefix] & 0xffffu;
+            uint32_t rest = e.code & ((1u << (e.len - l1)) - 1);
+            uint32_t first = rest << (16 - e.len), cnt = 1u << (16 - e.len);
+            for (uint32_t j = 0; j < cnt; j++) t[off + first + j] = packed;
+        }
+    }
+    return t;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------- messages ---
+
+std::string render_message(const Diag &d, const uint8_t *in, size_t len, uint32_t ds, uint32_t term) {
+    char b[256];
+    auto at = [&](const char *msg) {
+        snprintf(b, sizeof b, "JPEG at byte 0x%08x: %s", d.offset, msg);
+        return std::string(b);
+    };
+    auto entropy_at = [&](size_t off, const char *msg) {
+        snprintf(b, sizeof b, "JPEG entropy at byte 0x%08zx: %s", off, msg);
+        return std::string(b);
+    };
+    static const char *rst_names[8] = {"RST0", "RST1", "RST2", "RST3", "RST4", "RST5", "RST6", "RST7"};
+    auto marker_name = [&](uint32_t c) -> const char * {
+        if (c == 0x01) return "TEM";
+        if (c == 0xc0) return "SOF0";
+        if (c == 0xc4) return "DHT";
+        if (c >= 0xd0 && c <= 0xd7) return rst_names[c - 0xd0];
+        if (c == 0xd8) return "SOI";
+        if (c == 0xd9) return "EOI";
+        if (c == 0xda) return "SOS";
+        if (c == 0xdb) return "DQT";
+        if (c == 0xdc) return "DNL";
+        if (c == 0xdd) return "DRI";
+        if (c >= 0xe0 && c <= 0xef) return "APP";
+        if (c == 0xfe) return "COM";
+        return "UNKNOWN";
+    };
+    switch (d.kind) {
+    case kDiagNone: return "";
+    case kJExpectFF: return at("expected JPEG marker prefix 0xff");
+    case kJTruncMarker: return at("truncated marker");
+    case kJStuffedOutside: return at("stuffed 0xff byte outside entropy-coded data");
+    case kJExpectSoi: return at("expected SOI as the first marker");
+    case kJTruncLength: return at("truncated segment length");
+    case kJBadLength: return at("segment length must include its two length bytes");
+    case kJTruncPayload: {
+        std::string m = std::string("truncated ") + marker_name(d.aux) + " payload";
+        return at(m.c_str());
+    }
+    case kJSofShort: return at("SOF0 payload is too short");
+    case kJSofNoComp: return at("SOF0 must declare at least one component");
+    case kJSofSize: {
+        char m[96];
+        snprintf(m, sizeof m, "SOF0 declares %u components but has %u bytes", d.aux, d.aux2);
+        return at(m);
+    }
+    case kJSofPrecision: return at("baseline SOF0 sample precision must be 8 bits");
+    case kJSofWidth: return at("SOF0 width must be non-zero");
+    case kJSofSampling: return at("sampling factors must be between 1 and 4");
+    case kJSofTq: return at("quantization table selector must be 0 through 3");
+    case kJDqtPrecision: return at("DQT precision must be 0 or 1");
+    case kJDqtId: return at("DQT table identifier must be 0 through 3");
+    case kJDqtTrunc: return at("truncated DQT values");
+    case kJDqtEmpty: return at("DQT must contain at least one table");
+    case kJDhtClass: return at("DHT class must be 0 or 1");
+    case kJDhtId: return at("DHT table identifier must be 0 through 3");
+    case kJDhtTruncCounts: return at("truncated DHT code counts");
+    case kJDhtTruncSymbols: return at("truncated DHT symbols");
+    case kJDhtEmpty: return at("DHT must contain at least one table");
+    case kJDriSize: return at("DRI payload must contain exactly two bytes");
+    case kJSosEmpty: return at("SOS payload is empty");
+    case kJSosNoComp: return at("SOS must select at least one component");
+    case kJSosSize: {
+        char m[96];
+        snprintf(m, sizeof m, "SOS declares %u components but has %u bytes", d.aux, d.aux2);
+        return at(m);
+    }
+    case kJSosSelector: return at("Huffman table selectors must be 0 through 3");
+    case kJJfifShort: return at("JFIF APP0 payload is too short");
+    case kJJfifThumb: return at("JFIF thumbnail dimensions do not match payload size");
+    case kJScanTruncMarker: return at("truncated marker in entropy-coded data");
+    case kJScanNoTerminator: return at("entropy-coded scan has no terminating marker");
+    case kJNoSof: return "JPEG has no baseline SOF0 frame header";
+    case kJScanCount:
+        snprintf(b, sizeof b, "baseline decoder currently requires exactly one scan, found %u", d.aux);
+        return b;
+    case kJDnlHeight: return "JPEG height supplied by a DNL marker is not supported yet";
+    case kJPartialScan: return "non-interleaved or partial-component JPEG scans are not supported yet";
+    case kJNotBaseline: return "scan parameters are not baseline sequential";
+    case kJScanSelect:
+        snprintf(b, sizeof b, "JPEG scan must select frame component %u exactly once", d.aux);
+        return b;
+    case kJHuffInconsistent:
+        snprintf(b, sizeof b, "JPEG Huffman table %u has inconsistent symbol counts", d.aux);
+        return b;
+    case kJHuffOversub:
+        snprintf(b, sizeof b, "JPEG Huffman table %u is oversubscribed at length %u", d.aux, d.aux2);
+        return b;
+    case kJMissingQuant:
+        snprintf(b, sizeof b, "JPEG component %u references missing quantization table %u", d.aux, d.aux2);
+        return b;
+    case kJQuant16: return "16-bit quantization tables are not allowed in baseline JPEG";
+    case kJMissingDc:
+        snprintf(b, sizeof b, "JPEG scan references missing DC Huffman table %u", d.aux);
+        return b;
+    case kJMissingAc:
+        snprintf(b, sizeof b, "JPEG scan references missing AC Huffman table %u", d.aux);
+        return b;
+    case kJPanic: return "panic contained at MMRecode C API boundary";
+    case kJEndOfData: return entropy_at(term, "unexpected end of entropy-coded data");
+    case kJTruncEntropyMarker: return entropy_at(term, "truncated entropy marker");
+    case kJMarkerInData: {
+        size_t p = raw_after_tokens(in, len, ds, d.offset);
+        size_t q = p + 1;
+        while (q < len && in[q] == 0xff) q++;
+        char m[96];
+        snprintf(m, sizeof m, "unexpected marker 0xff%02x inside coded block", d.aux);
+        return entropy_at(q + 1, m);
+    }
+    case kJNoHuffCode: return entropy_at(raw_after_tokens(in, len, ds, d.offset), "no Huffman code matches the next 16 bits");
+    case kJDcCategory: return entropy_at(raw_after_tokens(in, len, ds, d.offset), "baseline DC coefficient category exceeds 11");
+    case kJAcZeroSize: return entropy_at(raw_after_tokens(in, len, ds, d.offset), "invalid zero-size AC Huffman symbol");
+    case kJZrlOverrun: return entropy_at(raw_after_tokens(in, len, ds, d.offset), "AC zero run exceeds the end of the block");
+    case kJAcCategory: return entropy_at(raw_after_tokens(in, len, ds, d.offset), "baseline AC coefficient category exceeds 10");
+    case kJAcRun: return entropy_at(raw_after_tokens(in, len, ds, d.offset), "AC coefficient run exceeds the end of the block");
+    case kJDcPredOverflow: return entropy_at(raw_after_tokens(in, len, ds, d.offset), "DC prediction overflow");
+    case kJDcDeqOverflow: return entropy_at(raw_after_tokens(in, len, ds, d.offset), "dequantized DC coefficient overflow");
+    case kJExtendTooLong: return entropy_at(raw_after_tokens(in, len, ds, d.offset), "coefficient magnitude contains more than 15 bits");
+    case kJExpectRst: return entropy_at(raw_after_tokens(in, len, ds, d.offset), "expected restart marker at MCU boundary");
+    case kJTruncRst: return entropy_at(raw_after_tokens(in, len, ds, d.offset), "truncated restart marker");
+    case kJRstMismatch:
+        snprintf(b, sizeof b, "JPEG at byte 0x%08zx: expected RST%u, found marker 0x%02x",
+                 raw_after_tokens(in, len, ds, d.offset), d.aux, d.aux2);
+        return b;
+    case kJFormatComponents: return "JPEG components do not map directly to a shared planar pixel format";
+    case kJFormatChroma: return "JPEG chroma sampling is not 4:2:0, 4:2:2, or 4:4:4";
+    case kDvShortHeader:
+        snprintf(b, sizeof b, "DV profile detection needs 4 header bytes, found %u", d.aux);
+        return b;
+    case kDvNotHeader: return "first DIF block is not a header";
+    case kDvLength:
+        snprintf(b, sizeof b, "DV header identifies a %u-byte frame, found %u bytes", d.aux, d.aux2);
+        return b;
+    case kDvDamagedId:
+        snprintf(b, sizeof b, "DV video segment %u in sequence %u has a damaged DIF identifier", d.aux, d.aux2);
+        return b;
+    case kDvIncomplete:
+        snprintf(b, sizeof b, "DV video segment %u in sequence %u has incomplete coefficients", d.aux, d.aux2);
+        return b;
+    case kDvBadVlc: return "invalid DV variable-length coefficient code";
+    case kOutputCapacity: return "output buffer is smaller than the decoded frame";
+    case kDeviceError: return "CUDA device failure during decode";
+    case kUnknownCodec: return "unknown codec or missing packet data";
+    default: return "decode failed";
+    }
+}
+
+// ---------------------------------------------------------------- probe ---
+
+Probe probe_packet(uint32_t codec, const uint8_t *data, size_t len) {
+    Probe pr;
+    if (codec == kCodecDv) {
+        DvPlan p = plan_dv(data, len);
+        if (!p.ok) {
+            pr.status = p.diag.status;
+            pr.diag = p.diag;
+            return pr;
+        }
+        pr.format = p.pal ? kYuv420 : kYuv411;
+        pr.range = kRangeLimited;
+        pr.width = p.W;
+        pr.height = p.H;
+        pr.plane_count = 3;
+        pr.plane_width[0] = p.W;
+        pr.plane_height[0] = p.H;
+        for (int i = 1; i < 3; i++) {
+            pr.plane_width[i] = p.cw;
+            pr.plane_height[i] = p.ch;
+        }
+        pr.planar_bytes = p.planar_bytes;
+        pr.rgb_bytes = (size_t)p.W * p.H * 3;
+        return pr;
+    }
+    if (codec != kCodecMjpeg) {
+        pr.diag = make_diag(kUnknownCodec);
+        pr.status = pr.diag.status;
+        return pr;
+    }
+    JPlan p;
+    plan_jpeg(data, len, p);
+    if (p.final_now) {
+        pr.diag = p.final_diag;
+        pr.status = pr.diag.status;
+        return pr;
+    }
+    if (p.prologue.kind != kDiagNone) {
+        pr.diag = p.prologue;
+        pr.status = pr.diag.status;
+    }
+    pr.format = p.fmt;
+    pr.range = kRangeFull;
+    pr.width = p.W;
+    pr.height = p.H;
+    pr.plane_count = p.ncomp;
+    for (uint32_t c = 0; c < std::min<uint32_t>(p.ncomp, 3); c++) {
+        pr.plane_width[c] = p.comps[c].plane_w;
+        pr.plane_height[c] = p.comps[c].plane_h;
+    }
+    pr.planar_bytes = p.planar_bytes;
+    pr.rgb_bytes = (size_t)p.W * p.H * 3;
+    return pr;
+}
+
+// --------------------------------------------------------------- engine ---
+
+struct Engine::Impl {
+    DevBuf d_in, d_tok, d_blob, d_tile_tok, d_tile_rst, d_rsts, d_results, d_coef, d_dc, d_planes, d_out, d_dvcoef,
+        d_modes, d_flags, d_segerr, d_vlc;
+    PinBuf h_blob, h_back;
+    std::vector<uint32_t> vlc;
+    // stage boundaries: start, uploads, scan, entropy, idct, dv, rgb, end
+    cudaEvent_t ev[8] = {};
+};
+
+Engine::Engine(int device) : device_(device), impl_(new Impl) {
+    MMR_CUDA(cudaSetDevice(device));
+    MMR_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    for (auto &e : impl_->ev) MMR_CUDA(cudaEventCreate(&e));
+    impl_->vlc = build_dv_vlc();
+    impl_->d_vlc.ensure(impl_->vlc.size() * 4);
+    MMR_CUDA(cudaMemcpy(impl_->d_vlc.ptr, impl_->vlc.data(), impl_->vlc.size() * 4, cudaMemcpyHostToDevice));
+}
+
+Engine::~Engine() {
+    cudaSetDevice(device_);
+    if (stream_) cudaStreamSynchronize(stream_);
+    for (auto &e : impl_->ev)
+        if (e) cudaEventDestroy(e);
+    delete impl_;
+    if (stream_) cudaStreamDestroy(stream_);
+}
+
+namespace {
+
+void set_result(Item &it, const Diag &d, const uint8_t *in, size_t len, uint32_t ds, uint32_t term) {
+    it.diag = d;
+    it.status = d.status;
+    it.message = d.kind == kDiagNone ? std::string() : render_message(d, in, len, ds, term);
+}
+
+}  // namespace
+
+int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
+    Impl &I = *impl_;
+    launches_ = 0;
+    for (size_t i = 0; i < n; i++) {
+        items[i].status = kOk;
+        items[i].diag = make_diag(kDiagNone);
+        items[i].message.clear();
+        items[i].concealed.clear();
+        items[i].out_bytes = 0;
+    }
+    try {
+        MMR_CUDA(cudaSetDevice(device_));
+        // ---------------------------------------------------- host planning
+        std::vector<JPlan> jplans;
+        std::vector<size_t> jitem;   // batch item of each MJPEG plan
+        std::vector<DvPlan> dplans;
+        std::vector<size_t> ditem;
+        for (size_t i = 0; i < n; i++) {
+            Item &it = items[i];
+            if (it.len && !it.data) {
+                set_result(it, make_diag(kUnknownCodec), nullptr, 0, 0, 0);
+                continue;
+            }
+            if (it.codec == kCodecMjpeg) {
+                jplans.emplace_back();
+                jitem.push_back(i);
+                plan_jpeg(it.data, it.len, jplans.back());
+            } else if (it.codec == kCodecDv) {
+                DvPlan p = plan_dv(it.data, it.len);
+                if (!p.ok) {
+                    set_result(it, p.diag, it.data, it.len, 0, 0);
+                    continue;
+                }
+                dplans.push_back(p);
+                ditem.push_back(i);
+            } else {
+                set_result(it, make_diag(kUnknownCodec), nullptr, 0, 0, 0);
+            }
+        }
+
+        // ------------------------------------------------------ MJPEG layout
+        Blob blob;
+        std::vector<JFrame> jframes;
+        std::vector<JState> jstates;
+        std::vector<uint32_t> tile_first(1, 0);
+        std::vector<JSched> sched;
+        std::vector<JComp> comps;
+        std::vector<HuffLut> luts;
+        std::vector<uint8_t> symbols;
+        std::vector<uint16_t> quant;
+        std::vector<uint2> items_small, items_big;
+        std::vector<JBlockRange> ranges;
+        std::vector<RgbJob> rgbjobs;
+        std::vector<uint64_t> rgbfirst(1, 0);
+        std::map<std::vector<uint8_t>, uint32_t> lut_index;
+        std::vector<uint32_t> item_ok(n, 1);
+        size_t in_bytes = 0, tok_bytes = 0, planes_bytes = 0, out_bytes = 0;
+        uint32_t rst_total = 0;
+        uint64_t blocks = 0;
+        std::vector<size_t> in_off(n, 0), out_off(n, 0), planes_off(n, SIZE_MAX);
+        std::vector<std::array<size_t, 6>> plane_geom(n);  // (offset, bytes) of up to 3 planes
+        // per JPEG plan: JFrame index (or -1)
+        std::vector<int> jframe_of(jplans.size(), -1);
+
+        auto place_input = [&](size_t i) {
+            if (!items[i].dev_data) {
+                in_off[i] = in_bytes;
+                in_bytes = align_up(in_bytes + items[i].len, 256);
+            }
+        };
+        auto out_need = [&](size_t i, size_t planar, size_t w, size_t h) -> size_t {
+            return items[i].output == kOutRgb24 ? w * h * 3 : planar;
+        };
+
+        for (size_t k = 0; k < jplans.size(); k++) {
+            JPlan &p = jplans[k];
+            size_t i = jitem[k];
+            Item &it = items[i];
+            if (p.final_now) {
+                set_result(it, p.final_diag, it.data, it.len, 0, 0);
+                continue;
+            }
+            // output sizing (only when the frame can succeed)
+            bool can_output = p.decode && p.fmt != 0;
+            if (can_output) {
+                size_t need = out_need(i, p.planar_bytes, p.W, p.H);
+                if (need > it.out_capacity || (!it.out && !it.plane_out[0] && need)) {
+                    set_result(it, make_diag(kOutputCapacity), nullptr, 0, 0, 0);
+                    continue;
+                }
+                it.out_bytes = need;
+                if (!it.out_on_device) {
+                    out_off[i] = out_bytes;
+                    out_bytes = align_up(out_bytes + need, 256);
+                }
+                for (uint32_t c = 0; c < std::min<uint32_t>(p.ncomp, 3); c++) {
+                    plane_geom[i][2 * c] = p.comps[c].out_off;
+                    plane_geom[i][2 * c + 1] = (size_t)p.comps[c].plane_w * p.comps[c].plane_h;
+                }
+            }
+            place_input(i);
+            JFrame F;
+            memset(&F, 0, sizeof(F));
+            F.in_len = (uint32_t)it.len;
+            F.data_start = p.hdr.data_offset;
+            F.item = (uint32_t)i;
+            F.decode = p.decode ? 1 : 0;
+            size_t tok_off = tok_bytes;
+            tok_bytes = align_up(tok_bytes + it.len, 256);
+            F.tok = reinterpret_cast<uint8_t *>(tok_off);  // relocated after allocation
+            uint32_t base16 = F.data_start & ~15u;
+            uint32_t nt = it.len > base16 ? (uint32_t)((it.len - base16 + kScanTile - 1) / kScanTile) : 0;
+            if (F.data_start >= it.len) nt = 0;
+            F.tile_first = tile_first.back();
+            tile_first.push_back(tile_first.back() + nt);
+            if (p.decode) {
+                F.width = p.W;
+                F.height = p.H;
+                F.ncomp = p.ncomp;
+                F.interleaved = p.interleaved;
+                F.mcu_cols = p.mcu_cols;
+                F.mcu_rows = p.mcu_rows;
+                F.total_mcus = p.total_mcus;
+                F.ri = p.ri;
+                F.n_intervals = p.n_intervals;
+                F.sched_off = (uint32_t)sched.size();
+                F.sched_len = (uint32_t)p.sched.size();
+                sched.insert(sched.end(), p.sched.begin(), p.sched.end());
+                F.comp_off = (uint32_t)comps.size();
+                comps.insert(comps.end(), p.comps.begin(), p.comps.end());
+                F.quant_off = (uint32_t)quant.size();
+                for (int q = 0; q < 4; q++) quant.insert(quant.end(), p.quant[q], p.quant[q] + 64);
+                for (int s = 0; s < 8; s++) {
+                    F.lut[s] = 0xffffffffu;
+                    if (!p.hdr.h_present[s]) continue;
+                    const uint8_t *src = it.data + p.hdr.h_off[s];
+                    std::vector<uint8_t> key(src, src + 16 + p.hdr.h_nsym[s]);
+                    auto f = lut_index.find(key);
+                    if (f == lut_index.end()) {
+                        HuffLut L;
+                        build_lut(key.data(), key.size(), (uint32_t)symbols.size(), &L);
+                        symbols.insert(symbols.end(), key.begin() + 16, key.end());
+                        f = lut_index.emplace(key, (uint32_t)luts.size()).first;
+                        luts.push_back(L);
+                    }
+                    F.lut[s] = f->second;
+                }
+                F.rst_off = rst_total;
+                rst_total += p.n_intervals;
+                F.blk_off = blocks;
+                F.n_blocks = p.n_blocks;
+                for (uint32_t c = 0; c < p.ncomp; c++) {
+                    JBlockRange r;
+                    r.first = blocks + p.comps[c].blk_base;
+                    r.frame = (uint32_t)jframes.size();
+                    r.comp = c;
+                    if (p.comps[c].bw * p.comps[c].bh) ranges.push_back(r);
+                }
+                blocks += p.n_blocks;
+                // planes: straight into a device output, else scratch
+                bool direct = can_output && it.output == kOutPlanar;
+                if (!direct) {
+                    planes_off[i] = planes_bytes;
+                    planes_bytes = align_up(planes_bytes + p.planar_bytes, 256);
+                }
+                F.item_base = 0;  // set below
+                auto &lst = p.ncomp <= 4 ? items_small : items_big;
+                for (uint32_t v = 0; v < p.n_intervals; v++) lst.push_back(make_uint2((uint32_t)jframes.size(), v));
+                if (can_output && it.output == kOutRgb24) {
+                    RgbJob J;
+                    memset(&J, 0, sizeof(J));
+                    J.w = p.W;
+                    J.h = p.H;
+                    J.lw = p.comps[0].plane_w;
+                    J.lh = p.comps[0].plane_h;
+                    J.gray = p.fmt == kGray8;
+                    if (!J.gray) {
+                        J.cbw = p.comps[1].plane_w;
+                        J.cbh = p.comps[1].plane_h;
+                        J.crw = p.comps[2].plane_w;
+                        J.crh = p.comps[2].plane_h;
+                        J.cb_off = p.comps[1].out_off;
+                        J.cr_off = p.comps[2].out_off;
+                    }
+                    J.limited = 0;
+                    J.item = (uint32_t)i;
+                    rgbjobs.push_back(J);
+                    rgbfirst.push_back(rgbfirst.back() + (uint64_t)p.W * p.H);
+                }
+            }
+            jframe_of[k] = (int)jframes.size();
+            jframes.push_back(F);
+            JState S;
+            memset(&S, 0, sizeof(S));
+            S.term = ~0ull;
+            S.bad_interval = 0xffffffffu;
+            jstates.push_back(S);
+        }
+        // item bases (small list first, then big)
+        {
+            std::vector<uint32_t> first_small(jframes.size(), 0xffffffffu), first_big(jframes.size(), 0xffffffffu);
+            for (size_t q = 0; q < items_small.size(); q++)
+                if (first_small[items_small[q].x] == 0xffffffffu) first_small[items_small[q].x] = (uint32_t)q;
+            for (size_t q = 0; q < items_big.size(); q++)
+                if (first_big[items_big[q].x] == 0xffffffffu)
+                    first_big[items_big[q].x] = (uint32_t)(items_small.size() + q);
+            for (size_t f = 0; f < jframes.size(); f++)
+                jframes[f].item_base = first_small[f] != 0xffffffffu ? first_small[f] : first_big[f];
+        }
+
+        // ------------------------------------------------------- DV layout
+        std::vector<DvFrame> dframes;
+        std::vector<DvState> dstates;
+        std::vector<uint32_t> seg_first(1, 0), dif_first(1, 0);
+        uint64_t dv_blocks = 0;
+        for (size_t k = 0; k < dplans.size(); k++) {
+            DvPlan &p = dplans[k];
+            size_t i = ditem[k];
+            Item &it = items[i];
+            size_t need = out_need(i, p.planar_bytes, p.W, p.H);
+            if (need > it.out_capacity || (!it.out && !it.plane_out[0] && need)) {
+                set_result(it, make_diag(kOutputCapacity), nullptr, 0, 0, 0);
+                continue;
+            }
+            it.out_bytes = need;
+            if (!it.out_on_device) {
+                out_off[i] = out_bytes;
+                out_bytes = align_up(out_bytes + need, 256);
+            }
+            plane_geom[i] = {0, (size_t)p.W * p.H, (size_t)p.W * p.H, (size_t)p.cw * p.ch,
+                             (size_t)p.W * p.H + (size_t)p.cw * p.ch, (size_t)p.cw * p.ch};
+            place_input(i);
+            DvFrame F;
+            memset(&F, 0, sizeof(F));
+            F.pal = p.pal;
+            F.sequences = p.sequences;
+            F.width = p.W;
+            F.height = p.H;
+            F.cw = p.cw;
+            F.ch = p.ch;
+            F.conceal = (it.flags & kFlagConceal) ? 1 : 0;
+            F.item = (uint32_t)i;
+            F.blk_off = dv_blocks;
+            F.seg_first = seg_first.back();
+            F.dif_first = dif_first.back();
+            seg_first.push_back(seg_first.back() + p.sequences * 27);
+            dif_first.push_back(dif_first.back() + p.sequences * 150);
+            dv_blocks += (uint64_t)p.sequences * 27 * 30;
+            bool direct = it.output == kOutPlanar;
+            if (!direct) {
+                planes_off[i] = planes_bytes;
+                planes_bytes = align_up(planes_bytes + p.planar_bytes, 256);
+                RgbJob J;
+                memset(&J, 0, sizeof(J));
+                J.w = p.W;
+                J.h = p.H;
+                J.lw = p.W;
+                J.lh = p.H;
+                J.cbw = J.crw = p.cw;
+                J.cbh = J.crh = p.ch;
+                J.cb_off = p.W * p.H;
+                J.cr_off = p.W * p.H + p.cw * p.ch;
+                J.limited = 1;
+                J.item = (uint32_t)i;
+                rgbjobs.push_back(J);
+                rgbfirst.push_back(rgbfirst.back() + (uint64_t)p.W * p.H);
+            }
+            dframes.push_back(F);
+            DvState S;
+            memset(&S, 0, sizeof(S));
+            S.bad_segment = 0xffffffffu;
+            dstates.push_back(S);
+        }
+
+        // ------------------------------------------------- device arenas
+        I.d_in.ensure(std::max<size_t>(in_bytes, 256));
+        I.d_tok.ensure(std::max<size_t>(tok_bytes, 256));
+        I.d_tile_tok.ensure(std::max<size_t>(tile_first.back() * 4, 256));
+        I.d_tile_rst.ensure(std::max<size_t>(tile_first.back() * 4, 256));
+        I.d_rsts.ensure(std::max<size_t>(rst_total * sizeof(RstEntry), 256));
+        size_t n_items = items_small.size() + items_big.size();
+        I.d_results.ensure(std::max<size_t>(n_items * sizeof(Diag), 256));
+        I.d_coef.ensure(std::max<size_t>(blocks * 128, 256));
+        I.d_dc.ensure(std::max<size_t>(blocks * 4, 256));
+        I.d_planes.ensure(std::max<size_t>(planes_bytes, 256));
+        I.d_out.ensure(std::max<size_t>(out_bytes, 256));
+        I.d_dvcoef.ensure(std::max<size_t>(dv_blocks * 128, 256));
+        I.d_modes.ensure(std::max<size_t>(dv_blocks, 256));
+        I.d_flags.ensure(std::max<size_t>(dif_first.back(), 256));
+        I.d_segerr.ensure(std::max<size_t>(seg_first.back(), 256));
+
+        uint8_t *d_in = I.d_in.as<uint8_t>();
+        auto in_ptr = [&](size_t i) -> const uint8_t * { return items[i].dev_data ? items[i].dev_data : d_in + in_off[i]; };
+        auto out_ptr = [&](size_t i) -> uint8_t * {
+            return items[i].out_on_device ? items[i].out : I.d_out.as<uint8_t>() + out_off[i];
+        };
+        auto planes_ptr = [&](size_t i) -> uint8_t * {
+            return planes_off[i] != SIZE_MAX ? I.d_planes.as<uint8_t>() + planes_off[i] : out_ptr(i);
+        };
+        for (auto &F : jframes) {
+            size_t i = F.item;
+            F.in = in_ptr(i);
+            F.tok = I.d_tok.as<uint8_t>() + reinterpret_cast<size_t>(F.tok);
+            F.planes = F.decode ? planes_ptr(i) : nullptr;
+        }
+        for (auto &F : dframes) {
+            F.in = in_ptr(F.item);
+            F.planes = planes_ptr(F.item);
+        }
+        for (auto &J : rgbjobs) {
+            J.planes = planes_ptr(J.item);
+            J.out = out_ptr(J.item);
+        }
+
+        // ------------------------------------------------------ plan blob
+        size_t o_jframes = blob.add_vec(jframes), o_jstates = blob.add_vec(jstates),
+               o_tile_first = blob.add_vec(tile_first), o_sched = blob.add_vec(sched), o_comps = blob.add_vec(comps),
+               o_luts = blob.add_vec(luts), o_symbols = blob.add_vec(symbols), o_quant = blob.add_vec(quant);
+        std::vector<uint2> all_items(items_small);
+        all_items.insert(all_items.end(), items_big.begin(), items_big.end());
+        size_t o_items = blob.add_vec(all_items), o_ranges = blob.add_vec(ranges), o_itemok = blob.add_vec(item_ok),
+               o_dframes = blob.add_vec(dframes), o_dstates = blob.add_vec(dstates), o_segfirst = blob.add_vec(seg_first),
+               o_diffirst = blob.add_vec(dif_first), o_rgbjobs = blob.add_vec(rgbjobs),
+               o_rgbfirst = blob.add_vec(rgbfirst);
+        size_t blob_size = std::max<size_t>(blob.bytes.size(), 256);
+        I.d_blob.ensure(blob_size);
+        I.h_blob.ensure(blob_size);
+        memcpy(I.h_blob.ptr, blob.bytes.data(), blob.bytes.size());
+        uint8_t *db = I.d_blob.as<uint8_t>();
+
+        // ------------------------------------------------------- launches
+        cudaStream_t s = stream_;
+        MMR_CUDA(cudaEventRecord(I.ev[0], s));
+        MMR_CUDA(cudaMemcpyAsync(db, I.h_blob.ptr, blob.bytes.size(), cudaMemcpyHostToDevice, s));
+        for (size_t i = 0; i < n; i++) {
+            bool planned = items[i].status == kOk && (items[i].codec == kCodecMjpeg || items[i].codec == kCodecDv);
+            if (planned && !items[i].dev_data && items[i].len)
+                MMR_CUDA(cudaMemcpyAsync(d_in + in_off[i], items[i].data, items[i].len, cudaMemcpyHostToDevice, s));
+        }
+        if (dv_blocks) MMR_CUDA(cudaMemsetAsync(I.d_dvcoef.ptr, 0, dv_blocks * 128, s));
+        MMR_CUDA(cudaEventRecord(I.ev[1], s));
+
+        JpegLaunch JL;
+        memset(&JL, 0, sizeof(JL));
+        JL.frames = reinterpret_cast<const JFrame *>(db + o_jframes);
+        JL.states = reinterpret_cast<JState *>(db + o_jstates);
+        JL.n_frames = (uint32_t)jframes.size();
+        JL.tile_first = reinterpret_cast<const uint32_t *>(db + o_tile_first);
+        JL.n_tiles = tile_first.back();
+        JL.tile_tok = I.d_tile_tok.as<uint32_t>();
+        JL.tile_rst = I.d_tile_rst.as<uint32_t>();
+        JL.rsts = I.d_rsts.as<RstEntry>();
+        JL.sched = reinterpret_cast<const JSched *>(db + o_sched);
+        JL.comps = reinterpret_cast<const JComp *>(db + o_comps);
+        JL.luts = reinterpret_cast<const HuffLut *>(db + o_luts);
+        JL.symbols = db + o_symbols;
+        JL.quant = reinterpret_cast<const uint16_t *>(db + o_quant);
+        JL.items = reinterpret_cast<const uint2 *>(db + o_items);
+        JL.n_items_small = (uint32_t)items_small.size();
+        JL.n_items = (uint32_t)n_items;
+        JL.results = I.d_results.as<Diag>();
+        JL.coef = I.d_coef.as<int16_t>();
+        JL.dc = I.d_dc.as<int32_t>();
+        JL.ranges = reinterpret_cast<const JBlockRange *>(db + o_ranges);
+        JL.n_ranges = (uint32_t)ranges.size();
+        JL.n_blocks = blocks;
+        JL.item_ok = reinterpret_cast<uint32_t *>(db + o_itemok);
+        if (!jframes.empty()) {
+            launch_jpeg_scan(JL, s);
+            MMR_CUDA(cudaEventRecord(I.ev[2], s));
+            launch_jpeg_entropy(JL, s);
+            MMR_CUDA(cudaEventRecord(I.ev[3], s));
+            launch_jpeg_idct(JL, s);
+            launches_ += (JL.n_tiles ? 3 : 0) + (JL.n_items_small ? 1 : 0) + (n_items > JL.n_items_small ? 1 : 0) + 1 +
+                         (blocks ? 1 : 0);
+        } else {
+            MMR_CUDA(cudaEventRecord(I.ev[2], s));
+            MMR_CUDA(cudaEventRecord(I.ev[3], s));
+        }
+        MMR_CUDA(cudaEventRecord(I.ev[4], s));
+        DvLaunch DL;
+        memset(&DL, 0, sizeof(DL));
+        DL.frames = reinterpret_cast<const DvFrame *>(db + o_dframes);
+        DL.states = reinterpret_cast<DvState *>(db + o_dstates);
+        DL.n_frames = (uint32_t)dframes.size();
+        DL.seg_first = reinterpret_cast<const uint32_t *>(db + o_segfirst);
+        DL.n_segments = seg_first.back();
+        DL.dif_first = reinterpret_cast<const uint32_t *>(db + o_diffirst);
+        DL.n_dif = dif_first.back();
+        DL.flags = I.d_flags.as<uint8_t>();
+        DL.seg_err = I.d_segerr.as<uint8_t>();
+        DL.coef = I.d_dvcoef.as<int16_t>();
+        DL.modes = I.d_modes.as<uint8_t>();
+        DL.vlc = I.d_vlc.as<uint32_t>();
+        DL.n_blocks = dv_blocks;
+        DL.item_ok = JL.item_ok;
+        if (!dframes.empty()) {
+            launch_dv_decode(DL, s);
+            launch_dv_idct(DL, s);
+            launches_ += 4;
+        }
+        MMR_CUDA(cudaEventRecord(I.ev[5], s));
+        RgbLaunch RL;
+        RL.jobs = reinterpret_cast<const RgbJob *>(db + o_rgbjobs);
+        RL.first = reinterpret_cast<const uint64_t *>(db + o_rgbfirst);
+        RL.n_jobs = (uint32_t)rgbjobs.size();
+        RL.n_pixels = rgbfirst.back();
+        RL.item_ok = JL.item_ok;
+        if (RL.n_pixels) {
+            launch_rgb(RL, s);
+            launches_ += 1;
+        }
+        MMR_CUDA(cudaEventRecord(I.ev[6], s));
+        MMR_CUDA(cudaGetLastError());
+
+        // ------------------------------------------------------- read-back
+        size_t back_j = jstates.size() * sizeof(JState), back_d = dstates.size() * sizeof(DvState);
+        size_t back_ok = n * 4, back_seg = seg_first.back();
+        size_t o_b1 = 0, o_b2 = align_up(back_j, 16), o_b3 = align_up(o_b2 + back_d, 16),
+               o_b4 = align_up(o_b3 + back_ok, 16);
+        I.h_back.ensure(std::max<size_t>(o_b4 + back_seg, 256));
+        uint8_t *hb = reinterpret_cast<uint8_t *>(I.h_back.ptr);
+        if (back_j) MMR_CUDA(cudaMemcpyAsync(hb + o_b1, db + o_jstates, back_j, cudaMemcpyDeviceToHost, s));
+        if (back_d) MMR_CUDA(cudaMemcpyAsync(hb + o_b2, db + o_dstates, back_d, cudaMemcpyDeviceToHost, s));
+        if (back_ok) MMR_CUDA(cudaMemcpyAsync(hb + o_b3, db + o_itemok, back_ok, cudaMemcpyDeviceToHost, s));
+        if (back_seg) MMR_CUDA(cudaMemcpyAsync(hb + o_b4, I.d_segerr.ptr, back_seg, cudaMemcpyDeviceToHost, s));
+        for (size_t i = 0; i < n; i++) {
+            Item &it = items[i];
+            if (it.status != kOk || it.out_on_device || !it.out_bytes) continue;
+            const uint8_t *src = I.d_out.as<uint8_t>() + out_off[i];
+            if (it.plane_out[0] && it.output == kOutPlanar) {
+                for (int c = 0; c < 3; c++)
+                    if (it.plane_out[c] && plane_geom[i][2 * c + 1])
+                        MMR_CUDA(cudaMemcpyAsync(it.plane_out[c], src + plane_geom[i][2 * c], plane_geom[i][2 * c + 1],
+                                                 cudaMemcpyDeviceToHost, s));
+            } else {
+                MMR_CUDA(cudaMemcpyAsync(it.out, src, it.out_bytes, cudaMemcpyDeviceToHost, s));
+            }
+        }
+        MMR_CUDA(cudaEventRecord(I.ev[7], s));
+        MMR_CUDA(cudaStreamSynchronize(s));
+        if (times) {
+            float *dst[8] = {nullptr, &times->upload_ms, &times->scan_ms, &times->entropy_ms, &times->idct_ms,
+                             &times->dv_ms, &times->rgb_ms, &times->download_ms};
+            for (int k = 1; k < 8; k++) MMR_CUDA(cudaEventElapsedTime(dst[k], I.ev[k - 1], I.ev[k]));
+            MMR_CUDA(cudaEventElapsedTime(&times->device_ms, I.ev[0], I.ev[7]));
+            times->jpeg_blocks = blocks;
+            times->dv_blocks = dv_blocks;
+            times->rgb_pixels = rgbfirst.back();
+            times->input_bytes = 0;
+            times->output_bytes = 0;
+            for (size_t i = 0; i < n; i++) {
+                times->input_bytes += items[i].len;
+                times->output_bytes += items[i].out_bytes;
+            }
+        }
+        const JState *hj = reinterpret_cast<const JState *>(hb + o_b1);
+        const DvState *hd = reinterpret_cast<const DvState *>(hb + o_b2);
+        const uint8_t *hseg = hb + o_b4;
+
+        // ------------------------------------------------ status resolution
+        for (size_t k = 0; k < jplans.size(); k++) {
+            int fidx = jframe_of[k];
+            if (fidx < 0) continue;
+            JPlan &p = jplans[k];
+            Item &it = items[jitem[k]];
+            const JState &S = hj[fidx];
+            const uint8_t *in = it.data;
+            uint32_t ds = p.hdr.data_offset;
+            // scan end -> rest of parse_jpeg (parser.rs:373-414 then the marker loop)
+            uint32_t term = 0;
+            if (!p.tail_known) {
+                if (S.term == ~0ull) {
+                    set_result(it, make_diag(kJScanNoTerminator, (uint32_t)it.len), in, it.len, ds, 0);
+                    continue;
+                }
+                term = (uint32_t)(S.term >> 9);
+                if ((S.term >> 8) & 1) {
+                    // truncated FF run: the reference stops at the end of the input
+                    set_result(it, make_diag(kJScanTruncMarker, (uint32_t)it.len), in, it.len, ds, 0);
+                    continue;
+                }
+                jpeg_parse_tail(in, it.len, term, &p.hdr);
+                if (p.hdr.err.kind != kDiagNone) {
+                    set_result(it, p.hdr.err, in, it.len, ds, term);
+                    continue;
+                }
+            } else {
+                term = (uint32_t)(S.term >> 9);
+            }
+            if (p.hdr.scan_count != 1) {
+                set_result(it, make_diag(kJScanCount, 0, p.hdr.scan_count), in, it.len, ds, term);
+                continue;
+            }
+            if (p.prologue.kind != kDiagNone) {
+                set_result(it, p.prologue, in, it.len, ds, term);
+                continue;
+            }
+            if (S.bad_interval != 0xffffffffu) {
+                set_result(it, S.diag, in, it.len, ds, term);
+                continue;
+            }
+            // into_video_frame
+            uint32_t pw[3] = {0, 0, 0}, ph[3] = {0, 0, 0};
+            for (uint32_t c = 0; c < std::min<uint32_t>(p.ncomp, 3); c++) {
+                pw[c] = p.comps[c].plane_w;
+                ph[c] = p.comps[c].plane_h;
+            }
+            uint16_t fk;
+            uint32_t fmt = predict_format(color_model(p.hdr), p.ncomp, pw, ph, p.W, p.H, &fk);
+            if (fk != kDiagNone) {
+                set_result(it, make_diag(fk), in, it.len, ds, term);
+                continue;
+            }
+            if (fmt != p.fmt) {
+                // colour model changed by a tail APP segment after the output was sized
+                set_result(it, make_diag(kJFormatComponents), in, it.len, ds, term);
+                continue;
+            }
+            it.format = fmt;
+            it.range = kRangeFull;
+            it.width = p.W;
+            it.height = p.H;
+            it.plane_count = p.ncomp;
+            for (uint32_t c = 0; c < p.ncomp; c++) {
+                it.plane_offset[c] = p.comps[c].out_off;
+                it.plane_width[c] = p.comps[c].plane_w;
+                it.plane_height[c] = p.comps[c].plane_h;
+            }
+        }
+        for (size_t k = 0, f = 0; k < dplans.size(); k++) {
+            Item &it = items[ditem[k]];
+            if (it.status != kOk) continue;
+            const DvState &S = hd[f];
+            const DvFrame &F = dframes[f];
+            f++;
+            DvPlan &p = dplans[k];
+            if (S.bad_segment != 0xffffffffu) {
+                if (!F.conceal) {
+                    set_result(it, S.diag, nullptr, 0, 0, 0);
+                    continue;
+                }
+                for (uint32_t sgi = 0; sgi < p.sequences * 27; sgi++)
+                    if (hseg[F.seg_first + sgi]) it.concealed.push_back({sgi / 27, sgi % 27});
+            }
+            it.format = p.pal ? kYuv420 : kYuv411;
+            it.range = kRangeLimited;
+            it.width = p.W;
+            it.height = p.H;
+            it.plane_count = 3;
+            it.plane_offset[0] = 0;
+            it.plane_offset[1] = (size_t)p.W * p.H;
+            it.plane_offset[2] = (size_t)p.W * p.H + (size_t)p.cw * p.ch;
+            it.plane_width[0] = p.W;
+            it.plane_height[0] = p.H;
+            for (int c = 1; c < 3; c++) {
+                it.plane_width[c] = p.cw;
+                it.plane_height[c] = p.ch;
+            }
+        }
+        for (size_t i = 0; i < n; i++)
+            if (items[i].status != kOk) items[i].out_bytes = 0;
+        return kOk;
+    } catch (const CudaError &e) {
+        cudaGetLastError();
+        for (size_t i = 0; i < n; i++) {
+            items[i].diag = make_diag(kDeviceError);
+            items[i].status = kInternal;
+            items[i].message = std::string("CUDA device failure: ") + e.what();
+            items[i].out_bytes = 0;
+        }
+        return kInternal;
+    }
+}
+
+}  // namespace mmr

@@ -1,0 +1,100 @@
+// Batch decode engine: plans a batch of MJPEG / DV25 packets on the host,
+// runs the decode kernels on one CUDA stream and resolves per-item status in
+// the reference decoder's error order.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "common.h"
+
+namespace mmr {
+
+enum Codec : uint32_t { kCodecMjpeg = 1, kCodecDv = 2 };
+enum ItemFlags : uint32_t { kFlagConceal = 1 };
+
+struct Item {
+    // input: `data` must be host-readable (headers are planned on the host);
+    // `dev_data`, when set, is a device copy of the same bytes and is used instead
+    // of uploading `data`.
+    const uint8_t *data = nullptr;
+    const uint8_t *dev_data = nullptr;
+    size_t len = 0;
+    uint32_t codec = kCodecMjpeg;
+    uint32_t output = kOutPlanar;
+    uint32_t flags = 0;
+    uint8_t *out = nullptr;  // destination (host memory, or device memory when out_on_device)
+    size_t out_capacity = 0;
+    bool out_on_device = false;
+    // planar host output written plane by plane (each pointer holds that plane's
+    // width*height bytes); used instead of `out` when plane_out[0] is set
+    uint8_t *plane_out[3] = {nullptr, nullptr, nullptr};
+    // results
+    int32_t status = kOk;
+    Diag diag{};
+    std::string message;
+    uint32_t format = 0, range = 0;
+    size_t width = 0, height = 0, plane_count = 0;
+    size_t plane_offset[3] = {0, 0, 0}, plane_width[3] = {0, 0, 0}, plane_height[3] = {0, 0, 0};
+    size_t out_bytes = 0;
+    std::vector<std::pair<uint32_t, uint32_t>> concealed;  // (sequence, slot)
+};
+
+// Header-only geometry of one packet (no decode).
+struct Probe {
+    int32_t status = kOk;
+    Diag diag{};
+    uint32_t format = 0, range = 0;
+    size_t width = 0, height = 0, plane_count = 0;
+    size_t plane_width[3] = {0, 0, 0}, plane_height[3] = {0, 0, 0};
+    size_t planar_bytes = 0, rgb_bytes = 0;
+};
+
+Probe probe_packet(uint32_t codec, const uint8_t *data, size_t len);
+
+// Renders a diagnostic as the reference's message. `data` is the packet, used
+// to turn token counts into byte offsets for entropy-stage errors.
+std::string render_message(const Diag &d, const uint8_t *data, size_t len, uint32_t data_start, uint32_t term);
+
+// CUDA-event times on the engine stream for the last decode() call.
+struct EngineTimes {
+    float device_ms = 0;    // first upload .. last read-back
+    float upload_ms = 0;    // plan + packet uploads
+    float scan_ms = 0;      // MJPEG marker scan
+    float entropy_ms = 0;   // MJPEG Huffman decode + resolve
+    float idct_ms = 0;      // MJPEG dequantisation + IDCT
+    float dv_ms = 0;        // DV segment decode + transform
+    float rgb_ms = 0;       // colour conversion
+    float download_ms = 0;  // read-back
+    uint64_t input_bytes = 0, output_bytes = 0, jpeg_blocks = 0, dv_blocks = 0, rgb_pixels = 0;
+};
+
+class Engine {
+public:
+    explicit Engine(int device);
+    ~Engine();
+    Engine(const Engine &) = delete;
+    Engine &operator=(const Engine &) = delete;
+
+    // Decodes `n` items; blocks until done. Returns kOk, or kInternal when the
+    // device failed (then every item carries kDeviceError).
+    int32_t decode(Item *items, size_t n, EngineTimes *times = nullptr);
+
+    int device() const { return device_; }
+    cudaStream_t stream() const { return stream_; }
+    // Number of this engine's kernel launches in the last decode() call.
+    uint32_t last_launches() const { return launches_; }
+
+    struct Impl;
+
+private:
+    int device_;
+    cudaStream_t stream_ = nullptr;
+    uint32_t launches_ = 0;
+    Impl *impl_;
+};
+
+}  // namespace mmr

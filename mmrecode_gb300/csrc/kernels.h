@@ -1,0 +1,78 @@
+// Kernel launchers (host-callable) for the MJPEG and DV25 decode stages.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "plan.h"
+
+namespace mmr {
+
+constexpr int kScanTile = 4096;  // bytes of entropy-coded data per marker-scan CTA
+
+struct JpegLaunch {
+    const JFrame *frames;        // device
+    JState *states;              // device
+    uint32_t n_frames;
+    const uint32_t *tile_first;  // n_frames + 1 prefix of marker-scan tiles
+    uint32_t n_tiles;
+    uint32_t *tile_tok;          // per tile: token count, then its exclusive prefix
+    uint32_t *tile_rst;
+    RstEntry *rsts;
+    const JSched *sched;
+    const JComp *comps;
+    const HuffLut *luts;
+    const uint8_t *symbols;
+    const uint16_t *quant;       // natural order
+    const uint2 *items;          // (frame, interval); frames with <= 4 components first
+    uint32_t n_items_small;
+    uint32_t n_items;
+    Diag *results;               // per item
+    int16_t *coef;               // 64 levels per block
+    int32_t *dc;                 // dequantised DC per block
+    const JBlockRange *ranges;
+    uint32_t n_ranges;
+    uint64_t n_blocks;
+    uint32_t *item_ok;           // per batch item: 1 while decoding has not failed
+};
+
+void launch_jpeg_scan(const JpegLaunch &L, cudaStream_t s);
+void launch_jpeg_entropy(const JpegLaunch &L, cudaStream_t s);
+void launch_jpeg_idct(const JpegLaunch &L, cudaStream_t s);
+
+struct DvLaunch {
+    const DvFrame *frames;
+    DvState *states;
+    uint32_t n_frames;
+    const uint32_t *seg_first;   // n_frames + 1 prefix of segments
+    uint32_t n_segments;
+    const uint32_t *dif_first;   // n_frames + 1 prefix of DIF blocks
+    uint32_t n_dif;
+    uint8_t *flags;              // per DIF block: 1 if its identifier is damaged
+    uint8_t *seg_err;            // per segment: DiagKind (0 = ok)
+    int16_t *coef;               // 64 per block, natural order
+    uint8_t *modes;              // per block: 1 = 2-4-8
+    const uint32_t *vlc;         // two-level VLC table
+    uint64_t n_blocks;
+    uint32_t *item_ok;
+};
+
+void launch_dv_decode(const DvLaunch &L, cudaStream_t s);
+void launch_dv_idct(const DvLaunch &L, cudaStream_t s);
+
+struct RgbLaunch {
+    const RgbJob *jobs;
+    const uint64_t *first;  // n_jobs + 1 prefix of pixels
+    uint32_t n_jobs;
+    uint64_t n_pixels;
+    const uint32_t *item_ok;
+};
+
+void launch_rgb(const RgbLaunch &L, cudaStream_t s);
+
+// DV VLC lookup: level-1 indexed by the next 10 bits; long codes index a
+// 64-entry level-2 block with the following 6 bits. Entry layout:
+//   bit 31 set: level-2 block at bits 0..15 (entry index)
+//   otherwise: len (bits 0..4), run (bits 5..11), level + 256 (bits 12..20); len 0 = no code
+constexpr int kDvVlcL1Bits = 10;
+
+}  // namespace mmr

@@ -1,0 +1,122 @@
+// Device-visible plan records for one decode batch (host builds, kernels read).
+#pragma once
+
+#include "common.h"
+
+namespace mmr {
+
+// ---------------------------------------------------------------- MJPEG ----
+
+// Canonical-Huffman lookup for one DHT table (crates/codecs/mjpeg/src/entropy.rs:18-70).
+// fast[] resolves every code of length <= 9 from the next 9 bits; longer codes use
+// maxcode/valptr (JPEG Annex F.2.2.3), which for canonical codes finds the same
+// code as the reference's length-by-length search.
+struct HuffLut {
+    uint16_t fast[512];    // (length << 8) | symbol; 0 when the code is longer than 9 bits or absent
+    int32_t maxcode[18];   // largest code of each length 1..16, -1 if none
+    int32_t valptr[18];    // symbol index of a length's first code, minus that code
+    uint32_t sym_off;      // first symbol in the symbol pool
+    uint32_t nsym;
+};
+
+// One frame component (SOF0 order).
+struct JComp {
+    uint32_t plane_w, plane_h;  // visible samples (decoder.rs:440-445)
+    uint32_t bw, bh;            // block grid covered by the MCUs
+    uint32_t blk_base;          // frame-relative index of block (0,0)
+    uint32_t out_off;           // offset of this plane in the frame's planar buffer
+    uint8_t h, v, q, pad;       // sampling factors and quantisation slot
+    uint32_t pad2;
+};
+
+// One block of an MCU, in the scan's component order (decoder.rs:374-400).
+struct JSched {
+    uint16_t comp;   // frame component index
+    uint8_t bx, by;  // block position inside the MCU
+    uint8_t dc, ac;  // Huffman table slots
+    uint8_t pad[2];
+};
+
+struct JFrame {
+    const uint8_t *in;      // packet (device)
+    uint8_t *tok;           // unstuffed entropy-coded bytes (device), capacity in_len
+    uint8_t *planes;        // planar samples (device): the output itself, or scratch for RGB output
+    uint32_t in_len;
+    uint32_t data_start;    // first entropy-coded byte
+    uint32_t width, height;
+    uint32_t ncomp, interleaved;
+    uint32_t mcu_cols, mcu_rows, total_mcus;
+    uint32_t ri;            // MCUs per restart interval (total_mcus when there is no DRI)
+    uint32_t n_intervals;
+    uint32_t item_base;     // first (frame, interval) work item
+    uint32_t sched_off, sched_len;
+    uint32_t comp_off;
+    uint32_t lut[8];        // HuffLut index of DC 0..3 then AC 0..3; UINT32_MAX when undefined
+    uint32_t quant_off;     // 4 tables x 64 entries, natural order
+    uint32_t rst_off;       // restart table (capacity n_intervals)
+    uint32_t tile_first;    // first marker-scan tile
+    uint32_t decode;        // 0: the header already failed; only the marker scan runs
+    uint64_t blk_off;       // first block in the coefficient arena
+    uint32_t n_blocks;
+    uint32_t item;          // caller's batch item
+};
+
+// Written by the kernels, copied back to the host.
+struct JState {
+    unsigned long long term;  // (offset << 9) | (truncated << 8) | code of the first terminator; ~0 if none
+    uint32_t n_tokens;
+    uint32_t n_rst;
+    uint32_t bad_interval;    // first interval that failed (UINT32_MAX if none)
+    uint32_t pad;
+    Diag diag;                // that interval's diagnostic (offset = tokens consumed)
+};
+
+struct RstEntry {
+    uint32_t tok;     // tokens before the marker
+    uint32_t number;  // n of RSTn
+};
+
+// One (frame, component) run of coefficient blocks, for the transform kernel.
+struct JBlockRange {
+    uint64_t first;  // first global block
+    uint32_t frame;
+    uint32_t comp;   // frame component index
+};
+
+// ---------------------------------------------------------------- DV25 -----
+
+struct DvFrame {
+    const uint8_t *in;   // 120000 / 144000 bytes (device)
+    uint8_t *planes;     // planar samples (device): the output itself, or scratch for RGB output
+    uint32_t pal;        // 0: 525/60, 1: 625/50
+    uint32_t sequences;  // 10 or 12
+    uint32_t width, height, cw, ch;
+    uint32_t conceal;
+    uint32_t item;
+    uint64_t blk_off;    // first block in the DV coefficient arena (sequences*27*30 blocks)
+    uint32_t seg_first;  // first segment in the segment arrays
+    uint32_t dif_first;  // first DIF block in the issue-flag array
+};
+
+struct DvState {
+    uint32_t bad_segment;  // first failing segment (sequence*27+slot), UINT32_MAX if none
+    uint32_t failed;       // number of failing segments
+    Diag diag;
+};
+
+// ---------------------------------------------------------------- colour ---
+
+// One frame to convert to interleaved RGB24 (crates/cli/src/terminal_preview.rs:7159-7236, 1:1).
+struct RgbJob {
+    const uint8_t *planes;
+    uint8_t *out;
+    uint32_t w, h;
+    uint32_t lw, lh, cbw, cbh, crw, crh;
+    uint32_t cb_off, cr_off;  // offsets of Cb / Cr in planes (Y at 0)
+    uint32_t limited;         // ColorRange::Limited
+    uint32_t gray;
+    uint32_t item;
+    uint32_t pad;
+};
+
+}  // namespace mmr
