@@ -237,7 +237,9 @@ __global__ void __launch_bounds__(kScanThreads) scan_emit_kernel(JpegLaunch L) {
             rst_idx++;
         }
     }
-    if (threadIdx.x == 0 && term < tr.base + (uint32_t)kScanTile) {
+    // The last tile that starts before the terminator publishes the totals (the
+    // terminator may sit exactly on the next tile's first byte).
+    if (threadIdx.x == 0 && term <= tr.base + (uint32_t)kScanTile) {
         L.states[tr.frame].n_tokens = L.tile_tok[t] + ttok;
         L.states[tr.frame].n_rst = L.tile_rst[t] + trst;
     }

@@ -240,7 +240,8 @@ def test_crafted_cases_in_one_batch(ctx):
 
 def test_idct_ties_and_clamps_through_streams(ctx):
     # DC-only blocks over a range of dequantised DC values, including the x.5 ties (dc = 4 mod 8)
-    blocks = [(d, [], True) for d in [4, -4, 0, 1, 8, 12, -1024, 1020, 1023, -1023, 2047]]
+    # consecutive differences stay within DC category 11 (|diff| <= 2047)
+    blocks = [(d, [], True) for d in [4, -4, 0, 1, 8, 12, -1024, 0, 1020, 1023, 0, -1023, 0, 2047, 2043, 20]]
     diffs, prev = [], 0
     for d, a, e in blocks:
         diffs.append((d - prev, a, e))
@@ -251,6 +252,27 @@ def test_idct_ties_and_clamps_through_streams(ctx):
     acs = [(0, ((-1) ** k) * (500 + k)) for k in range(40)]
     data = jpeg(8, 8, [(1, 1, 1, 0)], quant={0: [255] * 64}, entropy=stuff(encode_blocks([(3, acs, True)]).raw_bytes()))
     check_single(m.CODEC_MJPEG, data, "dense saturating")
+
+
+def _pad_entropy(packet: bytes, pad: int) -> bytes:
+    """Inserts `pad` zero bytes after the last MCU's data (ignored by the decoder) before EOI."""
+    return packet[:-2] + bytes(pad) + packet[-2:]
+
+
+def test_terminator_on_scan_tile_boundaries(ctx):
+    # The marker scan works on 4096-byte tiles starting at the 16-byte boundary below the
+    # first entropy byte; a terminator on a tile's first byte (or one byte either side)
+    # must still yield the right token and restart-marker totals.
+    packets = []
+    for base in synth.mjpeg_stream(113, 2, 160, 120, "420", 85, 0) + synth.mjpeg_stream(114, 1, 160, 128, "422", 85, 10):
+        st, _, info = oracle.jpeg_parse(base)
+        ds = info["data_offset"]
+        term = ds + info["data_length"]
+        need = (4096 - (term - (ds & ~15)) % 4096) % 4096
+        for delta in (-1, 0, 1, 4096):
+            if need + delta >= 0:
+                packets.append(_pad_entropy(base, need + delta))
+    check_batch(ctx, m.CODEC_MJPEG, packets, "tile boundary")
 
 
 # ------------------------------------------------------------------ seeded corruption
