@@ -125,6 +125,31 @@ MMR_API mmr_status mmr_mjpeg_encode_ex(const mmr_video_frame_view *frame, const 
 /* mmr_dv_encode (crates/codecs/dv/src/encoder.rs:67-103) with a DCT-mode policy. */
 MMR_API mmr_status mmr_dv_encode_ex(const mmr_video_frame_view *frame, uint32_t mode_policy, mmr_buffer *out_buffer);
 
+/*
+ * DV25 decode that allocates nothing. No counterpart in the reference library.
+ *
+ * For callers that must not allocate memory while decoding: a real-time capture
+ * or playback thread that cannot take cudaMalloc's implicit device
+ * synchronisation, an application whose GPU memory is budgeted up front, or a
+ * host runtime that forbids allocations outside its own arena. The packet
+ * (120000 or 144000 bytes) and the output buffer (planar Y | Cb | Cr, at least
+ * info->planar_bytes after the call; 622080 bytes covers both systems) are the
+ * caller's host memory; all device work uses one fixed 2.25 MiB array inside
+ * the library, which every GPU that loads the library keeps until the process
+ * exits. Packets longer than 144000 bytes are rejected with
+ * MMR_STATUS_INVALID_ARGUMENT. Results equal mmr_dv_decode's for the same
+ * packet. On success the call performs no allocation at all; a failing call
+ * stores its diagnostic for mmr_last_error_message like every other entry point.
+ *
+ * The first call on a device sets that device up (it looks up the array's
+ * device address and writes a lookup table into it), so make that first call
+ * before any stream capture. All calls share the array: calls that overlap on
+ * the GPU (several threads decoding on the same device) race, so serialise them.
+ * info->struct_size must be sizeof(mmr_gpu_frame_info); the call fills *info.
+ */
+MMR_API mmr_status mmr_dv_decode_static(const uint8_t *data, size_t len, uint8_t *out, size_t out_capacity,
+                                        mmr_gpu_frame_info *info);
+
 #ifdef __cplusplus
 }
 #endif

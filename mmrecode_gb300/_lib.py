@@ -107,6 +107,8 @@ SIGNATURES = {
     "mmr_mjpeg_encode_ex": ([ctypes.POINTER(VideoFrameView), ctypes.POINTER(JpegEncodeOptions), ctypes.POINTER(Buffer)],
                             ctypes.c_int32),
     "mmr_dv_encode_ex": ([ctypes.POINTER(VideoFrameView), ctypes.c_uint32, ctypes.POINTER(Buffer)], ctypes.c_int32),
+    "mmr_dv_decode_static": ([ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
+                              ctypes.POINTER(FrameInfo)], ctypes.c_int32),
 }
 
 _lib = None

@@ -14,6 +14,7 @@
 #include "../../include/mmrecode_gpu.h"
 #include "encode.h"
 #include "engine.h"
+#include "last_error.h"
 
 using mmr::Engine;
 using mmr::Item;
@@ -234,6 +235,15 @@ mmr_status outside_scope(const char *what) {
 }
 
 }  // namespace
+
+namespace mmr {
+
+void set_last_error(int32_t status, const char *message) {
+    if (status == MMR_STATUS_OK) g_last_error.clear();
+    else g_last_error.assign(message);
+}
+
+}  // namespace mmr
 
 struct mmr_gpu_context {
     Engine *engine;

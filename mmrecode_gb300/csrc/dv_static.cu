@@ -1,0 +1,259 @@
+// DV25 decode that allocates nothing (mmr_dv_decode_static in mmrecode_gpu.h).
+//
+// Meant for callers that must not allocate memory while decoding: a real-time
+// capture or playback thread that cannot afford cudaMalloc's implicit device
+// synchronisation, a host application whose memory is budgeted up front, or
+// an embedding runtime that forbids allocations outside its own arena. Every
+// device byte this path uses lives in one file-scope array, g_dv_scratch,
+// sized for one DV25 frame of either system (kDvStaticScratchBytes, 2.25 MiB);
+// every GPU that loads the library holds that array until the process exits.
+// The caller passes the packet and the output buffer in host memory.
+//
+// The first call on a device sets that device up (looks up the array's device
+// address with cudaGetSymbolAddress and writes the VLC lookup table into it),
+// so that first call should come before any stream capture. All calls share
+// the array and it keeps the last call's contents: each call clears what must
+// start at zero, and calls that overlap on the GPU (from several threads on the
+// same device) race on it -- serialise them.
+#include <cuda_runtime.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <mutex>
+#include <string>
+
+#include "../../include/mmrecode_gpu.h"
+#include "engine.h"
+#include "last_error.h"
+#include "kernels.h"
+#include "plan.h"
+#include "tables.h"
+
+namespace mmr {
+namespace {
+
+constexpr size_t kDvStaticScratchBytes = 2304u * 1024u;  // 2.25 MiB
+constexpr size_t kDvMaxInput = 144000;                   // one 625/50 frame
+constexpr size_t kDvMaxPlanar = 720 * 576 + 2 * 360 * 288;
+constexpr uint32_t kDvMaxSegments = 12 * 27;
+constexpr uint32_t kDvMaxDif = 12 * 150;
+constexpr size_t kVlcMaxEntries = 1024 + 64 * 64;
+
+static __device__ __align__(256) uint8_t g_dv_scratch[kDvStaticScratchBytes];
+
+constexpr size_t a256(size_t v) { return (v + 255) / 256 * 256; }
+// Layout of g_dv_scratch (byte offsets).
+constexpr size_t kOffIn = 0;
+constexpr size_t kOffOut = kOffIn + a256(kDvMaxInput);
+constexpr size_t kOffFlags = kOffOut + a256(kDvMaxPlanar);
+constexpr size_t kOffSegErr = kOffFlags + a256(kDvMaxDif);
+constexpr size_t kOffModes = kOffSegErr + a256(kDvMaxSegments);
+constexpr size_t kOffCoef = kOffModes + a256(kDvMaxSegments * 30);
+constexpr size_t kOffVlc = kOffCoef + a256((size_t)kDvMaxSegments * 30 * 128);
+constexpr size_t kOffMeta = kOffVlc + a256(kVlcMaxEntries * 4);
+constexpr size_t kMetaBytes = 1024;
+static_assert(kOffMeta + kMetaBytes <= kDvStaticScratchBytes, "DV static scratch layout exceeds the array");
+
+struct Meta {  // per-call plan and state (lives at kOffMeta)
+    DvFrame frame;
+    DvState state;
+    uint32_t item_ok;
+    uint32_t seg_first[2];
+    uint32_t dif_first[2];
+};
+static_assert(sizeof(Meta) <= kMetaBytes, "DV static metadata exceeds its region");
+
+// Two-level VLC table with the layout kernels.h documents, from the canonical
+// codes of crates/codecs/dv/src/decoder.rs:319-354; filled into a static host
+// array (no heap use) and copied into the scratch at set-up.
+uint32_t g_vlc_host[kVlcMaxEntries];
+
+size_t fill_vlc_table() {
+    struct E {
+        uint32_t code, len, run;
+        int32_t level;
+    };
+    static E entries[746];
+    size_t ne = 0;
+    uint8_t len_of[409];
+    int n = 0;
+    for (auto &r : kDvVlcLenRuns)
+        for (int k = 0; k < r[1]; k++) len_of[n++] = (uint8_t)r[0];
+    uint32_t canonical = 0;
+    for (int i = 0; i < 409; i++) {
+        uint32_t len = len_of[i];
+        uint32_t code = canonical >> (32 - len);
+        canonical += 1u << (32 - len);
+        uint32_t run = i < 153 ? kDvVlcRunHead[i] : 0;
+        int32_t level = i < 153 ? kDvVlcLevelHead[i] : i - 153;
+        if (level == 0) entries[ne++] = {code, len, run, 0};
+        else {
+            entries[ne++] = {code << 1, len + 1, run, level};
+            entries[ne++] = {(code << 1) | 1, len + 1, run, -level};
+        }
+    }
+    const uint32_t l1 = kDvVlcL1Bits, l2 = 16 - kDvVlcL1Bits;
+    size_t size = (size_t)1 << l1;
+    memset(g_vlc_host, 0, sizeof(g_vlc_host));
+    for (size_t k = 0; k < ne; k++) {
+        const E &e = entries[k];
+        uint32_t packed = e.len | (e.run << 5) | ((uint32_t)(e.level + 256) << 12);
+        if (e.len <= l1) {
+            for (uint32_t j = 0; j < (1u << (l1 - e.len)); j++) g_vlc_host[(e.code << (l1 - e.len)) + j] = packed;
+        } else {
+            uint32_t prefix = e.code >> (e.len - l1);
+            if (!(g_vlc_host[prefix] & 0x80000000u)) {
+                if (size + ((size_t)1 << l2) > kVlcMaxEntries) return 0;
+                g_vlc_host[prefix] = 0x80000000u | (uint32_t)size;
+                size += (size_t)1 << l2;
+            }
+            uint32_t off = g_vlc_host[prefix] & 0xffffu, rest = e.code & ((1u << (e.len - l1)) - 1);
+            for (uint32_t j = 0; j < (1u << (16 - e.len)); j++) g_vlc_host[off + (rest << (16 - e.len)) + j] = packed;
+        }
+    }
+    return size;
+}
+
+std::mutex g_setup_mutex;
+uint8_t *g_scratch_ptr[64] = {};  // device address of g_dv_scratch, per device
+
+// Once per device, with that device current.
+cudaError_t setup(int device, uint8_t **ptr) {
+    std::lock_guard<std::mutex> lock(g_setup_mutex);
+    if (device < 0 || device >= 64) return cudaErrorInvalidDevice;
+    if (g_scratch_ptr[device]) {
+        *ptr = g_scratch_ptr[device];
+        return cudaSuccess;
+    }
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_dv_scratch);
+    if (e != cudaSuccess) return e;
+    size_t entries = fill_vlc_table();
+    if (entries == 0) return cudaErrorInvalidValue;
+    e = cudaMemcpy((uint8_t *)p + kOffVlc, g_vlc_host, entries * 4, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return e;
+    g_scratch_ptr[device] = (uint8_t *)p;
+    *ptr = (uint8_t *)p;
+    return cudaSuccess;
+}
+
+mmr_status fail(mmr_gpu_frame_info *info, mmr_status st, const char *m) {
+    set_last_error(st, m);
+    if (info) info->status = st;
+    return st;
+}
+
+}  // namespace
+}  // namespace mmr
+
+using namespace mmr;
+
+extern "C" MMR_API mmr_status mmr_dv_decode_static(const uint8_t *data, size_t len, uint8_t *out, size_t out_capacity,
+                                                   mmr_gpu_frame_info *info) {
+    char msg[200];
+    if (!info || info->struct_size != sizeof(mmr_gpu_frame_info))
+        return fail(nullptr, MMR_STATUS_INVALID_ARGUMENT, "invalid argument: info is null or its struct_size is wrong");
+    size_t keep = info->struct_size;
+    memset(info, 0, sizeof(*info));
+    info->struct_size = keep;
+    if (len > 0 && !data)
+        return fail(info, MMR_STATUS_INVALID_ARGUMENT, "invalid argument: data is null while length is nonzero");
+    if (len > kDvMaxInput) {
+        snprintf(msg, sizeof msg, "invalid argument: packet of %zu bytes exceeds the %zu-byte frame the static scratch holds",
+                 len, kDvMaxInput);
+        return fail(info, MMR_STATUS_INVALID_ARGUMENT, msg);
+    }
+    // detect_profile (crates/codecs/dv/src/profile.rs:87-127)
+    Probe pr = probe_packet(kCodecDv, data, len);
+    if (pr.status != kOk) {
+        snprintf(msg, sizeof msg, "invalid data: %s", render_message(pr.diag, data, len, 0, 0).c_str());
+        return fail(info, pr.status, msg);
+    }
+    if (!out || out_capacity < pr.planar_bytes) {
+        snprintf(msg, sizeof msg, "invalid argument: output buffer needs %zu bytes", pr.planar_bytes);
+        return fail(info, MMR_STATUS_INVALID_ARGUMENT, msg);
+    }
+    int device = 0;
+    uint8_t *s = nullptr;
+    cudaError_t e = cudaGetDevice(&device);
+    if (e == cudaSuccess) e = setup(device, &s);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        snprintf(msg, sizeof msg, "CUDA device unavailable: %s", cudaGetErrorString(e));
+        return fail(info, MMR_STATUS_INTERNAL_ERROR, msg);
+    }
+    bool pal = pr.format == kYuv420;
+    uint32_t seqs = pal ? 12 : 10;
+    Meta meta;
+    memset(&meta, 0, sizeof(meta));
+    DvFrame &F = meta.frame;
+    F.in = s + kOffIn;
+    F.planes = s + kOffOut;
+    F.pal = pal;
+    F.sequences = seqs;
+    F.width = 720;
+    F.height = pal ? 576 : 480;
+    F.cw = pal ? 360 : 180;
+    F.ch = pal ? 288 : 480;
+    F.conceal = 0;
+    F.item = 0;
+    meta.state.bad_segment = 0xffffffffu;
+    meta.item_ok = 1;
+    meta.seg_first[1] = seqs * 27;
+    meta.dif_first[1] = seqs * 150;
+    Meta *dm = reinterpret_cast<Meta *>(s + kOffMeta);
+    DvLaunch L;
+    memset(&L, 0, sizeof(L));
+    L.frames = &dm->frame;
+    L.states = &dm->state;
+    L.n_frames = 1;
+    L.seg_first = dm->seg_first;
+    L.n_segments = seqs * 27;
+    L.dif_first = dm->dif_first;
+    L.n_dif = seqs * 150;
+    L.flags = s + kOffFlags;
+    L.seg_err = s + kOffSegErr;
+    L.coef = reinterpret_cast<int16_t *>(s + kOffCoef);
+    L.modes = s + kOffModes;
+    L.vlc = reinterpret_cast<const uint32_t *>(s + kOffVlc);
+    L.n_blocks = (uint64_t)seqs * 27 * 30;
+    L.item_ok = &dm->item_ok;
+    cudaStream_t st = 0;
+    e = cudaMemcpyAsync(s + kOffIn, data, len, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dm, &meta, sizeof(meta), cudaMemcpyHostToDevice, st);
+    // the segment decoder writes only non-zero coefficients
+    if (e == cudaSuccess) e = cudaMemsetAsync(s + kOffCoef, 0, L.n_blocks * 128, st);
+    if (e == cudaSuccess) {
+        launch_dv_decode(L, st);
+        launch_dv_idct(L, st);
+        e = cudaGetLastError();
+    }
+    Meta back;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&back, dm, sizeof(back), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, s + kOffOut, pr.planar_bytes, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        snprintf(msg, sizeof msg, "CUDA device failure: %s", cudaGetErrorString(e));
+        return fail(info, MMR_STATUS_INTERNAL_ERROR, msg);
+    }
+    if (back.state.bad_segment != 0xffffffffu) {
+        Diag d = back.state.diag;
+        snprintf(msg, sizeof msg, "invalid data: %s", render_message(d, nullptr, 0, 0, 0).c_str());
+        return fail(info, d.status, msg);
+    }
+    info->status = MMR_STATUS_OK;
+    info->format = pr.format;
+    info->range = pr.range;
+    info->width = pr.width;
+    info->height = pr.height;
+    info->plane_count = 3;
+    for (int c = 0; c < 3; c++) {
+        info->plane_width[c] = pr.plane_width[c];
+        info->plane_height[c] = pr.plane_height[c];
+    }
+    info->planar_bytes = pr.planar_bytes;
+    info->rgb_bytes = pr.rgb_bytes;
+    set_last_error(MMR_STATUS_OK, "");
+    return MMR_STATUS_OK;
+}
