@@ -322,6 +322,7 @@ def main():
     peak, peak_kind = _peaks()
     transform_bytes = blocks * 128 + n * rgb_bytes
     entropy_bytes = in_bytes + blocks * 128
+    exact_frac = stages[-1]["idct_exact_samples"] / max(1, blocks * 64)
     stage_times = {"scan": scan_ms, "entropy": entropy_ms, "idct": idct_ms, "rgb": rgb_ms,
                    "upload": avg("upload_ms"), "download": avg("download_ms")}
     if idct_ms + rgb_ms >= entropy_ms:
@@ -377,6 +378,7 @@ def main():
             "batched_over_plain": value / plain_fps,
             "latency_ms": {"batched_p50": ms_per_step, "batched_p99": ms_per_step},
             "stage_ms": stage_times,
+            "idct_exact_sample_fraction": exact_frac,
             "roofline": roofline,
             "cpu_baseline": cpu,
             "bit_exact_sample": bit_exact,

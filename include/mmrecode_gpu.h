@@ -102,6 +102,7 @@ typedef struct mmr_gpu_batch_stats {
     size_t struct_size;
     double total_ms, upload_ms, scan_ms, entropy_ms, idct_ms, dv_ms, rgb_ms, download_ms;
     uint64_t input_bytes, output_bytes, jpeg_blocks, dv_blocks, rgb_pixels;
+    uint64_t idct_exact_samples; /* samples the fp32 IDCT left to the exact binary64 pass */
     uint32_t launches;
 } mmr_gpu_batch_stats;
 

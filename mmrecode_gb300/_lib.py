@@ -68,7 +68,8 @@ class GpuItem(ctypes.Structure):
 class BatchStats(ctypes.Structure):
     _fields_ = [("struct_size", ctypes.c_size_t)] + [(n, ctypes.c_double) for n in (
         "total_ms", "upload_ms", "scan_ms", "entropy_ms", "idct_ms", "dv_ms", "rgb_ms", "download_ms")] + [
-        (n, ctypes.c_uint64) for n in ("input_bytes", "output_bytes", "jpeg_blocks", "dv_blocks", "rgb_pixels")] + [
+        (n, ctypes.c_uint64) for n in ("input_bytes", "output_bytes", "jpeg_blocks", "dv_blocks", "rgb_pixels",
+                                      "idct_exact_samples")] + [
         ("launches", ctypes.c_uint32)]
 
 

@@ -477,6 +477,7 @@ MMR_API mmr_status mmr_gpu_last_batch_stats(const mmr_gpu_context *context, mmr_
     stats->jpeg_blocks = t.jpeg_blocks;
     stats->dv_blocks = t.dv_blocks;
     stats->rgb_pixels = t.rgb_pixels;
+    stats->idct_exact_samples = t.idct_exact_samples;
     stats->launches = context->last_launches;
     return finish(MMR_STATUS_OK, "");
 }

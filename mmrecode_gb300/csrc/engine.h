@@ -70,6 +70,7 @@ struct EngineTimes {
     float rgb_ms = 0;       // colour conversion
     float download_ms = 0;  // read-back
     uint64_t input_bytes = 0, output_bytes = 0, jpeg_blocks = 0, dv_blocks = 0, rgb_pixels = 0;
+    uint64_t idct_exact_samples = 0;  // MJPEG samples recomputed in exact binary64 order
 };
 
 class Engine {

@@ -498,11 +498,68 @@ __global__ void resolve_kernel(JpegLaunch L) {
 }
 
 // ---------------------------------------------------------------- IDCT ----
+//
+// transform.rs:86-109 computes, in binary64 and in this order,
+//   t[v][x] = sum_u M[x][u] * c[v][u]            (from 0.0, u = 0..7)
+//   s[y][x] = sum_v M[y][v] * t[v][x]            (from 0.0, v = 0..7)
+//   sample  = clamp(round_half_away(s + 128.0), 0, 255)
+// GB300 issues binary64 at a small fraction of its fp32 rate, so every sample
+// is first computed in fp32 and kept only when it provably rounds like the
+// binary64 value:
+//   S  = sum_v sum_u M[y][v] M[x][u] c[v][u]   (exact real value, double M)
+//   B  = sum_v sum_u |M[y][v]| |M[x][u]| |c[v][u]|  <=  Mmax^2 * C1,
+//        C1 = sum |c|, Mmax = max |M| = 0.49039264 (Mmax^2 < 0.2405)
+//   fp32 path (M and c rounded to fp32, FMA accumulation, u = 2^-24):
+//        |s32 - S| <= (2u + 8u) + (u + 8u) ... = 19u * B + O(u^2) B   (pass 1 error
+//        10u A with A = sum_u |M||c|, propagated through pass 2, plus pass 2's
+//        own 8u; standard recursive-summation bounds, Higham ch. 3)
+//   binary64 reference: |s64 - S| <= 16 * 2^-53 * B, and its +128.0 rounds
+//        by at most 2^-53 |s + 128|.
+// With delta = 2^-21 * C1 + 2^-40 |s32| + 2^-30 (2^-21 * C1 >= 19u * 0.2405 C1
+// with 1.7x margin), if no half-integer lies within delta of s32 + 128 both
+// values round to the same integer; samples certain to clamp are kept too.
+// Every other sample is queued and recomputed in the exact reference order by
+// fixup_kernel (or in place when the queue is full). Zero coefficients are
+// skipped in the exact path: a zero term adds +-0.0, which leaves any sum that
+// is not -0.0 unchanged, and these sums are never -0.0.
+
+__constant__ float c_idct32[64] = MMR_IDCT_MATRIX_INIT;
+
+__device__ __forceinline__ uint8_t exact_sample(const int32_t *c, int stride, int y, int x) {
+    double t[8];
+#pragma unroll
+    for (int v = 0; v < 8; v++) {
+        double acc = 0.0;
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            int32_t cv = c[v * stride + u];
+            if (cv) acc = __dadd_rn(acc, __dmul_rn(c_idct[x * 8 + u], (double)cv));
+        }
+        t[v] = acc;
+    }
+    double acc = 0.0;
+#pragma unroll
+    for (int v = 0; v < 8; v++)
+        if (t[v] != 0.0) acc = __dadd_rn(acc, __dmul_rn(c_idct[y * 8 + v], t[v]));
+    double px = round(__dadd_rn(acc, 128.0));
+    return (uint8_t)fmin(fmax(px, 0.0), 255.0);
+}
 
 constexpr int kIdctBlocks = 32;  // blocks per CTA, 8 threads (one column each) per block
 
+__device__ __forceinline__ uint32_t find_range(const JpegLaunch &L, uint64_t g) {
+    uint32_t lo = 0, hi = L.n_ranges;
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (L.ranges[mid].first <= g) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
 __global__ void __launch_bounds__(kIdctBlocks * 8) idct_kernel(JpegLaunch L) {
     __shared__ int32_t s_c[kIdctBlocks][65];
+    __shared__ float s_f[kIdctBlocks][65];
     int lb = threadIdx.x >> 3, x = threadIdx.x & 7;
     uint64_t g = (uint64_t)blockIdx.x * kIdctBlocks + lb;
     bool valid = g < L.n_blocks;
@@ -510,57 +567,99 @@ __global__ void __launch_bounds__(kIdctBlocks * 8) idct_kernel(JpegLaunch L) {
     const JFrame *F = nullptr;
     const JComp *C = nullptr;
     if (valid) {
-        uint32_t lo = 0, hi = L.n_ranges;
-        while (hi - lo > 1) {
-            uint32_t mid = (lo + hi) >> 1;
-            if (L.ranges[mid].first <= g) lo = mid;
-            else hi = mid;
-        }
-        r = lo;
+        r = find_range(L, g);
         F = &L.frames[L.ranges[r].frame];
         C = &L.comps[F->comp_off + L.ranges[r].comp];
         valid = L.item_ok[F->item] != 0;
     }
+    uint64_t l1 = 0;  // sum |c| over this thread's row
     if (valid) {
         const uint16_t *Q = L.quant + F->quant_off + C->q * 64;
         int4 v = reinterpret_cast<const int4 *>(L.coef + g * 64)[x];
         const int16_t *lv = reinterpret_cast<const int16_t *>(&v);
 #pragma unroll
-        for (int j = 0; j < 8; j++) s_c[lb][x * 8 + j] = (int32_t)lv[j] * (int32_t)Q[x * 8 + j];
-        if (x == 0) s_c[lb][0] = L.dc[g];
+        for (int j = 0; j < 8; j++) {
+            int32_t c = (j == 0 && x == 0) ? L.dc[g] : (int32_t)lv[j] * (int32_t)Q[x * 8 + j];
+            s_c[lb][x * 8 + j] = c;
+            s_f[lb][x * 8 + j] = (float)c;
+            l1 += (uint64_t)(c < 0 ? -(int64_t)c : (int64_t)c);
+        }
     }
+    // C1 over the block's 8 threads (lanes 8k..8k+7 of the warp)
+#pragma unroll
+    for (int o = 1; o < 8; o <<= 1) l1 += __shfl_xor_sync(0xffffffffu, l1, o);
     __syncthreads();
     if (!valid) return;
-    // temporary[v*8+x] = sum_u M[x][u] * c[v*8+u], accumulated from 0.0 in u order
-    double mrow[8];
+    float mrow[8];
 #pragma unroll
-    for (int u = 0; u < 8; u++) mrow[u] = c_idct[x * 8 + u];
-    double t[8];
+    for (int u = 0; u < 8; u++) mrow[u] = c_idct32[x * 8 + u];
+    float t[8];
 #pragma unroll
     for (int v = 0; v < 8; v++) {
-        double acc = 0.0;
+        float acc = 0.0f;
 #pragma unroll
-        for (int u = 0; u < 8; u++) {
-            int32_t cv = s_c[lb][v * 8 + u];
-            // a zero coefficient contributes +-0.0, which never changes a sum that is not -0.0
-            if (cv) acc = __dadd_rn(acc, __dmul_rn(mrow[u], (double)cv));
-        }
+        for (int u = 0; u < 8; u++) acc = fmaf(mrow[u], s_f[lb][v * 8 + u], acc);
         t[v] = acc;
     }
+    const float delta_base = (float)l1 * 0x1p-21f + 0x1p-30f;
     uint64_t local = g - L.ranges[r].first;
     uint32_t gx = (uint32_t)(local % C->bw), gy = (uint32_t)(local / C->bw);
     uint32_t col = gx * 8 + x;
     uint8_t *plane = F->planes + C->out_off;
 #pragma unroll
     for (int y = 0; y < 8; y++) {
-        double acc = 0.0;
+        float acc = 0.0f;
 #pragma unroll
-        for (int v = 0; v < 8; v++)
-            if (t[v] != 0.0) acc = __dadd_rn(acc, __dmul_rn(c_idct[y * 8 + v], t[v]));
-        double px = round(__dadd_rn(acc, 128.0));
-        px = fmin(fmax(px, 0.0), 255.0);
+        for (int v = 0; v < 8; v++) acc = fmaf(c_idct32[y * 8 + v], t[v], acc);
         uint32_t row = gy * 8 + y;
-        if (row < C->plane_h && col < C->plane_w) plane[(uint64_t)row * C->plane_w + col] = (uint8_t)px;
+        if (row >= C->plane_h || col >= C->plane_w) continue;
+        float delta = delta_base + fabsf(acc) * 0x1p-40f;
+        int out;
+        bool certain = true;
+        if (acc + delta < 0.5f - 128.0f) out = 0;
+        else if (acc - delta > 254.5f - 128.0f) out = 255;
+        else {
+            float fl = floorf(acc);
+            float fr = acc - fl;  // exact for |acc| < 2^23
+            certain = fabsf(fr - 0.5f) > delta && delta < 0.25f;
+            int rr = (int)fl + (fr > 0.5f ? 1 : 0) + 128;
+            out = rr < 0 ? 0 : rr > 255 ? 255 : rr;
+        }
+        uint64_t dst = (uint64_t)row * C->plane_w + col;
+        if (certain) {
+            plane[dst] = (uint8_t)out;
+            continue;
+        }
+        uint32_t slot = atomicAdd(L.fix_count, 1u);
+        if (slot < L.fix_capacity) L.fix[slot] = (g << 6) | (uint64_t)(y * 8 + x);
+        else plane[dst] = exact_sample(&s_c[lb][0], 8, y, x);  // queue full: exact in place
+    }
+}
+
+// Exact reference-order recomputation of the queued samples.
+__global__ void __launch_bounds__(256) idct_fixup_kernel(JpegLaunch L) {
+    uint32_t n = min(*L.fix_count, L.fix_capacity);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        unsigned long long e = L.fix[i];
+        uint64_t g = e >> 6;
+        int y = (int)(e >> 3) & 7, x = (int)e & 7;
+        uint32_t r = find_range(L, g);
+        const JFrame *F = &L.frames[L.ranges[r].frame];
+        const JComp *C = &L.comps[F->comp_off + L.ranges[r].comp];
+        const uint16_t *Q = L.quant + F->quant_off + C->q * 64;
+        int32_t c[64];
+        const int4 *src = reinterpret_cast<const int4 *>(L.coef + g * 64);
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            int4 v = src[k];
+            const int16_t *lv = reinterpret_cast<const int16_t *>(&v);
+#pragma unroll
+            for (int j = 0; j < 8; j++) c[k * 8 + j] = (int32_t)lv[j] * (int32_t)Q[k * 8 + j];
+        }
+        c[0] = L.dc[g];
+        uint64_t local = g - L.ranges[r].first;
+        uint32_t gx = (uint32_t)(local % C->bw), gy = (uint32_t)(local / C->bw);
+        F->planes[C->out_off + (uint64_t)(gy * 8 + y) * C->plane_w + gx * 8 + x] = exact_sample(c, 8, y, x);
     }
 }
 
@@ -588,6 +687,7 @@ void launch_jpeg_idct(const JpegLaunch &L, cudaStream_t s) {
     if (L.n_blocks == 0) return;
     uint64_t grid = (L.n_blocks + kIdctBlocks - 1) / kIdctBlocks;
     idct_kernel<<<(unsigned)grid, kIdctBlocks * 8, 0, s>>>(L);
+    idct_fixup_kernel<<<L.fixup_grid, 256, 0, s>>>(L);
 }
 
 }  // namespace mmr

@@ -33,6 +33,10 @@ struct JpegLaunch {
     uint32_t n_ranges;
     uint64_t n_blocks;
     uint32_t *item_ok;           // per batch item: 1 while decoding has not failed
+    unsigned long long *fix;     // samples the fp32 IDCT could not decide: (block << 6) | (y*8+x)
+    uint32_t *fix_count;         // zero-initialised per batch
+    uint32_t fix_capacity;
+    uint32_t fixup_grid;         // CTAs of the grid-stride fixup pass
 };
 
 void launch_jpeg_scan(const JpegLaunch &L, cudaStream_t s);
