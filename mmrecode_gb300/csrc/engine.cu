@@ -296,7 +296,7 @@ void plan_jpeg(const uint8_t *in, size_t len, JPlan &p) {
             for (int k = 0; k < 64; k++) p.quant[q][kZigzag[k]] = in[h.q_off[q] + k];
 }
 
-void build_lut(const uint8_t *key, size_t key_len, uint32_t sym_off, HuffLut *lut) {
+void build_lut(const uint8_t *key, size_t key_len, uint32_t sym_off, bool ac, HuffLut *lut) {
     memset(lut, 0, sizeof(*lut));
     for (int l = 0; l < 18; l++) lut->maxcode[l] = -1;
     const uint8_t *counts = key;
@@ -311,7 +311,21 @@ void build_lut(const uint8_t *key, size_t key_len, uint32_t sym_off, HuffLut *lu
         for (uint32_t i = 0; i < n; i++) {
             if (l <= 9) {
                 uint32_t first = code << (9 - l), cnt = 1u << (9 - l);
-                for (uint32_t j = 0; j < cnt; j++) lut->fast[first + j] = (uint16_t)((l << 8) | symbols[k]);
+                uint8_t sym = symbols[k];
+                uint32_t run = ac ? sym >> 4 : 0, size = ac ? sym & 15 : sym;
+                bool fast_ok = ac ? (size >= 1 && size <= 10) : (size >= 1 && size <= 11);
+                for (uint32_t j = 0; j < cnt; j++) {
+                    // the first code symbol of each 9-bit pattern wins (codes are prefix-free)
+                    if (lut->fast[first + j]) continue;
+                    lut->fast[first + j] = (uint16_t)((l << 8) | sym);
+                    if (fast_ok && l + size <= 9) {
+                        uint32_t bits = (first + j) & ((1u << (9 - l)) - 1);  // the bits after the code
+                        int32_t v = (int32_t)(bits >> (9 - l - size));
+                        if (v < (1 << (size - 1))) v += 1 - (1 << size);  // receive_extend
+                        lut->fastv[first + j] =
+                            (int32_t)((uint32_t)v << 16) | (int32_t)((size << 12) | (run << 8) | (l + size));
+                    }
+                }
             }
             code++;
             k++;
@@ -635,14 +649,14 @@ Probe probe_packet(uint32_t codec, const uint8_t *data, size_t len) {
 
 struct Engine::Impl {
     DevBuf d_in, d_tok, d_blob, d_tile_tok, d_tile_rst, d_rsts, d_results, d_coef, d_dc, d_planes, d_out, d_dvcoef,
-        d_modes, d_flags, d_segerr, d_vlc, d_fix;
+        d_modes, d_flags, d_segerr, d_vlc, d_fix, d_slot_item, d_ivs, d_sync, d_spec, d_prefix, d_events, d_ivkey;
     PinBuf h_blob, h_back;
     std::vector<uint32_t> vlc;
     // stage boundaries: start, uploads, scan, entropy, idct, dv, rgb, end
     cudaEvent_t ev[8] = {};
 };
 
-Engine::Engine(int device) : device_(device), impl_(new Impl) {
+Engine::Engine(int device) : device_(device), slice_bits_(kSliceBitsDefault), impl_(new Impl) {
     MMR_CUDA(cudaSetDevice(device));
     MMR_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
     for (auto &e : impl_->ev) MMR_CUDA(cudaEventCreate(&e));
@@ -729,6 +743,8 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
         size_t in_bytes = 0, tok_bytes = 0, planes_bytes = 0, out_bytes = 0;
         uint32_t rst_total = 0;
         uint64_t blocks = 0;
+        uint64_t n_slots = 0;
+        const uint32_t slice_bits = slice_bits_;
         std::vector<size_t> in_off(n, 0), out_off(n, 0), planes_off(n, SIZE_MAX);
         std::vector<std::array<size_t, 6>> plane_geom(n);  // (offset, bytes) of up to 3 planes
         // per JPEG plan: JFrame index (or -1)
@@ -807,11 +823,12 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
                     if (!p.hdr.h_present[s]) continue;
                     const uint8_t *src = it.data + p.hdr.h_off[s];
                     std::vector<uint8_t> key(src, src + 16 + p.hdr.h_nsym[s]);
+                    key.push_back(s >= 4);  // DC and AC lookups differ for the same code table
                     auto f = lut_index.find(key);
                     if (f == lut_index.end()) {
                         HuffLut L;
-                        build_lut(key.data(), key.size(), (uint32_t)symbols.size(), &L);
-                        symbols.insert(symbols.end(), key.begin() + 16, key.end());
+                        build_lut(key.data(), key.size() - 1, (uint32_t)symbols.size(), s >= 4, &L);
+                        symbols.insert(symbols.end(), key.begin() + 16, key.end() - 1);
                         f = lut_index.emplace(key, (uint32_t)luts.size()).first;
                         luts.push_back(L);
                     }
@@ -819,6 +836,11 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
                 }
                 F.rst_off = rst_total;
                 rst_total += p.n_intervals;
+                if (p.ncomp <= 4) {
+                    F.slot_first = (uint32_t)n_slots;
+                    F.slot_count = (uint32_t)((8 * (uint64_t)it.len + slice_bits - 1) / slice_bits + p.n_intervals);
+                    n_slots += F.slot_count;
+                }
                 F.blk_off = blocks;
                 F.n_blocks = p.n_blocks;
                 for (uint32_t c = 0; c < p.ncomp; c++) {
@@ -946,7 +968,8 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
 
         // ------------------------------------------------- device arenas
         I.d_in.ensure(std::max<size_t>(in_bytes, 256));
-        I.d_tok.ensure(std::max<size_t>(tok_bytes, 256));
+        // +64: the entropy decoder's 32-bit word reader may read a few bytes past a frame's tokens
+        I.d_tok.ensure(std::max<size_t>(tok_bytes + 64, 256));
         I.d_tile_tok.ensure(std::max<size_t>(tile_first.back() * 4, 256));
         I.d_tile_rst.ensure(std::max<size_t>(tile_first.back() * 4, 256));
         I.d_rsts.ensure(std::max<size_t>(rst_total * sizeof(RstEntry), 256));
@@ -964,6 +987,14 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
         // queue fills, the kernel recomputes in place instead
         uint32_t fix_capacity = (uint32_t)std::min<uint64_t>(blocks / 2 + 65536, 0x7fffffffu);
         I.d_fix.ensure((size_t)fix_capacity * 8);
+        if (n_slots > 0xffffffffull) throw std::runtime_error("batch too large for the chunked entropy decoder");
+        I.d_slot_item.ensure(std::max<size_t>(n_slots * 4, 256));
+        I.d_sync.ensure(std::max<size_t>(n_slots * sizeof(SliceSync), 256));
+        I.d_spec.ensure(std::max<size_t>(n_slots * sizeof(SliceSpec), 256));
+        I.d_prefix.ensure(std::max<size_t>(n_slots * sizeof(SlicePrefix), 256));
+        I.d_events.ensure(std::max<size_t>(n_slots * sizeof(SliceEvent), 256));
+        I.d_ivs.ensure(std::max<size_t>(items_small.size() * sizeof(IvInfo), 256));
+        I.d_ivkey.ensure(std::max<size_t>(items_small.size() * 8, 256));
 
         uint8_t *d_in = I.d_in.as<uint8_t>();
         auto in_ptr = [&](size_t i) -> const uint8_t * { return items[i].dev_data ? items[i].dev_data : d_in + in_off[i]; };
@@ -1000,6 +1031,8 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
                o_rgbfirst = blob.add_vec(rgbfirst);
         uint32_t zero_counter = 0;
         size_t o_fixcount = blob.add(&zero_counter, 4);
+        uint32_t zero_dirty[kSyncPasses] = {};
+        size_t o_dirty = blob.add(zero_dirty, sizeof(zero_dirty));
         size_t blob_size = std::max<size_t>(blob.bytes.size(), 256);
         I.d_blob.ensure(blob_size);
         I.h_blob.ensure(blob_size);
@@ -1031,6 +1064,7 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
         JL.sched = reinterpret_cast<const JSched *>(db + o_sched);
         JL.comps = reinterpret_cast<const JComp *>(db + o_comps);
         JL.luts = reinterpret_cast<const HuffLut *>(db + o_luts);
+        JL.n_luts = (uint32_t)luts.size();
         JL.symbols = db + o_symbols;
         JL.quant = reinterpret_cast<const uint16_t *>(db + o_quant);
         JL.items = reinterpret_cast<const uint2 *>(db + o_items);
@@ -1047,14 +1081,25 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
         JL.fix_count = reinterpret_cast<uint32_t *>(db + o_fixcount);
         JL.fix_capacity = fix_capacity;
         JL.fixup_grid = 4 * 152;
+        JL.slice_bits = slice_bits;
+        JL.n_slots = (uint32_t)n_slots;
+        JL.slot_item = I.d_slot_item.as<uint32_t>();
+        JL.ivs = I.d_ivs.as<IvInfo>();
+        JL.sync = I.d_sync.as<SliceSync>();
+        JL.spec = I.d_spec.as<SliceSpec>();
+        JL.prefix = I.d_prefix.as<SlicePrefix>();
+        JL.events = I.d_events.as<SliceEvent>();
+        JL.iv_key = I.d_ivkey.as<unsigned long long>();
+        JL.sync_dirty = reinterpret_cast<uint32_t *>(db + o_dirty);
         if (!jframes.empty()) {
             launch_jpeg_scan(JL, s);
             MMR_CUDA(cudaEventRecord(I.ev[2], s));
+            launch_jpeg_slices(JL, s);
             launch_jpeg_entropy(JL, s);
             MMR_CUDA(cudaEventRecord(I.ev[3], s));
             launch_jpeg_idct(JL, s);
-            launches_ += (JL.n_tiles ? 3 : 0) + (JL.n_items_small ? 1 : 0) + (n_items > JL.n_items_small ? 1 : 0) + 1 +
-                         (blocks ? 2 : 0);
+            launches_ += (JL.n_tiles ? 3 : 0) + (JL.n_slots ? jpeg_slice_launches(JL) : 0) +
+                         (n_items > JL.n_items_small ? 1 : 0) + 1 + (blocks ? 2 : 0);
         } else {
             MMR_CUDA(cudaEventRecord(I.ev[2], s));
             MMR_CUDA(cudaEventRecord(I.ev[3], s));

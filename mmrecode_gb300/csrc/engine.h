@@ -88,6 +88,13 @@ public:
     cudaStream_t stream() const { return stream_; }
     // Number of this engine's kernel launches in the last decode() call.
     uint32_t last_launches() const { return launches_; }
+    // Bits per slice of the chunked entropy decoder (a multiple of 32, >= 128).
+    uint32_t slice_bits() const { return slice_bits_; }
+    bool set_slice_bits(uint32_t bits) {
+        if (bits < 128 || bits % 32 || bits > (1u << 20)) return false;
+        slice_bits_ = bits;
+        return true;
+    }
 
     struct Impl;
 
@@ -95,6 +102,7 @@ private:
     int device_;
     cudaStream_t stream_ = nullptr;
     uint32_t launches_ = 0;
+    uint32_t slice_bits_;
     Impl *impl_;
 };
 

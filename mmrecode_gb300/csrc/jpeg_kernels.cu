@@ -246,226 +246,261 @@ __global__ void __launch_bounds__(kScanThreads) scan_emit_kernel(JpegLaunch L) {
 }
 
 // ------------------------------------------------------------ entropy -----
+//
+// One restart interval per thread, written as a flat loop that decodes one
+// Huffman symbol per iteration (DC or AC, chosen by the coefficient index k),
+// so the threads of a warp stay in step whatever their block boundaries.
+// Bits come from the unstuffed token stream as big-endian 32-bit words; the
+// reader may hold bits past the interval's barrier, so every use of bits is
+// checked against the count before the barrier (`limit`), which is exactly
+// where the reference reader would meet the next marker or the end of data.
+// Codes whose code and magnitude bits fit in 9 bits decode with one lookup
+// (HuffLut::fastv); others follow the reference's order of checks.
 
-struct BitStream {
-    const uint8_t *tok;
-    uint32_t pos;   // next token to load
-    uint32_t end;   // barrier: first token this interval may not read
-    uint64_t buf;   // next bits, MSB first
-    int nbits;      // valid bits in buf
-    uint32_t used;  // bits consumed in this interval
+constexpr int kLutCache = 6;  // deduplicated Huffman lookups held in shared memory
+
+__device__ __forceinline__ uint32_t bswap32(uint32_t x) { return __byte_perm(x, 0, 0x0123); }
+
+struct Reader {
+    const uint32_t *words;
+    uint32_t wpos;   // next word to load
+    uint64_t buf;    // next bits, MSB first
+    int nbits;       // bits held in buf (>= 32 after refill)
+    uint32_t used;   // bits consumed since the interval start
+    uint32_t limit;  // bits before the barrier
 };
 
-__device__ __forceinline__ void fill(BitStream &s) {
-    while (s.nbits <= 56 && s.pos < s.end) {
-        s.buf |= (uint64_t)s.tok[s.pos] << (56 - s.nbits);
-        s.pos++;
-        s.nbits += 8;
+__device__ __forceinline__ void reader_init(Reader &r, const uint8_t *tok, uint32_t start, uint32_t end) {
+    r.words = reinterpret_cast<const uint32_t *>(tok);
+    uint32_t w0 = start >> 2, skip = (start & 3) * 8;
+    r.buf = (uint64_t)bswap32(__ldg(r.words + w0)) << (32 + skip);
+    r.nbits = 32 - (int)skip;
+    r.wpos = w0 + 1;
+    r.used = 0;
+    r.limit = (end - start) * 8;
+}
+
+__device__ __forceinline__ void refill(Reader &r) {
+    if (r.nbits <= 32) {
+        r.buf |= (uint64_t)bswap32(__ldg(r.words + r.wpos)) << (32 - r.nbits);
+        r.wpos++;
+        r.nbits += 32;
     }
 }
 
-__device__ __forceinline__ void consume(BitStream &s, int n) {
-    s.buf <<= n;
-    s.nbits -= n;
-    s.used += n;
+__device__ __forceinline__ void take(Reader &r, int n) {
+    r.buf <<= n;
+    r.nbits -= n;
+    r.used += n;
 }
 
-// Next Huffman symbol (entropy.rs:57-70). Returns the code length, 0 if no code
-// of length <= 16 matches the (zero-padded) next bits.
-__device__ __forceinline__ int huff_peek(const HuffLut *__restrict__ lut, const uint8_t *__restrict__ symbols,
-                                         const BitStream &s, uint32_t *sym) {
-    uint32_t e = lut->fast[s.buf >> 55];
+// Symbol for the next bits (entropy.rs:57-70): code length, 0 when no code of
+// length <= 16 matches.
+__device__ __forceinline__ int slow_symbol(const HuffLut *T, const uint8_t *__restrict__ symbols, uint64_t buf,
+                                           uint32_t *sym) {
+    uint32_t e = T->fast[buf >> 55];
     if (e) {
         *sym = e & 0xff;
         return (int)(e >> 8);
     }
-    uint32_t code16 = (uint32_t)(s.buf >> 48);
+    uint32_t code16 = (uint32_t)(buf >> 48);
 #pragma unroll 1
     for (int l = 10; l <= 16; l++) {
         int32_t c = (int32_t)(code16 >> (16 - l));
-        if (c <= lut->maxcode[l]) {
-            *sym = symbols[lut->sym_off + lut->valptr[l] + c];
+        if (c <= T->maxcode[l]) {
+            *sym = symbols[T->sym_off + T->valptr[l] + c];
             return l;
         }
     }
     return 0;
 }
 
-struct EntropyError {
-    uint16_t kind;
-    uint32_t bitpos;  // reader position in bits from the interval start
-    uint32_t aux, aux2;
-};
-
 template <int MAXC>
-__device__ void decode_interval(const JpegLaunch &L, uint32_t item, int16_t *stage) {
+__device__ void decode_interval(const JpegLaunch &L, uint32_t item, int16_t *stage, const HuffLut *s_lut,
+                                const uint8_t *s_zz) {
     uint2 it = L.items[item];
-    uint32_t f = it.x, iv = it.y;
-    const JFrame &F = L.frames[f];
-    JState *st = &L.states[f];
-    Diag out = make_diag(kDiagNone);
+    const uint32_t f = it.x, iv = it.y;
+    const JFrame *Fp = L.frames + f;
+    JState *st = L.states + f;
     unsigned long long termv = st->term;
-    if (!F.decode || termv == ~0ull || ((termv >> 8) & 1)) return;
-    uint32_t n_rst = min(st->n_rst, F.n_intervals);
-    uint32_t n_tok = st->n_tokens;
-    const RstEntry *rst = L.rsts + F.rst_off;
+    if (!Fp->decode || termv == ~0ull || ((termv >> 8) & 1)) return;
+    const uint32_t n_int = Fp->n_intervals, ri = Fp->ri, total_mcus = Fp->total_mcus, mcu_cols = Fp->mcu_cols;
+    const uint32_t sched_len = Fp->sched_len, interleaved = Fp->interleaved;
+    const JSched *sched = L.sched + Fp->sched_off;
+    const JComp *comps = L.comps + Fp->comp_off;
+    const uint16_t *quant = L.quant + Fp->quant_off;
+    const uint64_t blk_off = Fp->blk_off;
+    uint32_t lut_idx[8];
+#pragma unroll
+    for (int s = 0; s < 8; s++) lut_idx[s] = Fp->lut[s];
+    const uint32_t n_rst = min(st->n_rst, n_int), n_tok = st->n_tokens;
+    const RstEntry *rst = L.rsts + Fp->rst_off;
     uint32_t start;
     if (iv == 0) start = 0;
     else if (iv - 1 < n_rst) start = rst[iv - 1].tok;
     else return;  // no RST precedes this interval: an earlier interval fails its restart check
-    bool barrier_rst = iv < n_rst;
-    uint32_t barrier = barrier_rst ? rst[iv].tok : n_tok;
+    const bool barrier_rst = iv < n_rst;
+    const uint32_t barrier = barrier_rst ? rst[iv].tok : n_tok;
 
-    BitStream s;
-    s.tok = F.tok;
-    s.pos = start;
-    s.end = barrier;
-    s.buf = 0;
-    s.nbits = 0;
-    s.used = 0;
+    Reader r;
+    reader_init(r, Fp->tok, start, barrier);
     int32_t pred[MAXC];
+#pragma unroll
     for (int c = 0; c < MAXC; c++) pred[c] = 0;
-
-    EntropyError err;
-    err.kind = kDiagNone;
-    uint32_t mcu0 = iv * F.ri;
-    uint32_t mcu1 = min(mcu0 + F.ri, F.total_mcus);
-    const JSched *sched = L.sched + F.sched_off;
-    const JComp *comps = L.comps + F.comp_off;
     int4 *stage4 = reinterpret_cast<int4 *>(stage);
 
-    for (uint32_t mcu = mcu0; mcu < mcu1 && err.kind == kDiagNone; mcu++) {
-        uint32_t mx = mcu % F.mcu_cols, my = mcu / F.mcu_cols;
-        for (uint32_t si = 0; si < F.sched_len; si++) {
-            JSched e = sched[si];
-            const JComp &C = comps[e.comp];
-            const HuffLut *dct = L.luts + F.lut[e.dc];
-            const HuffLut *act = L.luts + F.lut[4 + e.ac];
-            const uint16_t *Q = L.quant + F.quant_off + C.q * 64;
-#pragma unroll
-            for (int k = 0; k < 8; k++) stage4[k] = make_int4(0, 0, 0, 0);
-            // DC (decoder.rs:501-515)
-            fill(s);
+    uint32_t mcu = iv * ri;
+    const uint32_t mcu1 = min(mcu + ri, total_mcus);
+    if (mcu >= mcu1 || sched_len == 0) return;
+    uint32_t si = 0, comp = 0;
+    const HuffLut *dcl = nullptr, *acl = nullptr;
+    int32_t q0 = 0, dq = 0;
+    uint64_t blk = 0;
+    auto setup_block = [&]() {
+        JSched e = sched[si];
+        comp = e.comp;
+        const JComp &C = comps[comp];
+        uint32_t mx = mcu % mcu_cols, my = mcu / mcu_cols;
+        uint32_t gx = interleaved ? mx * C.h + e.bx : mx, gy = interleaved ? my * C.v + e.by : my;
+        blk = blk_off + C.blk_base + (uint64_t)gy * C.bw + gx;
+        q0 = quant[C.q * 64];
+        uint32_t di = lut_idx[e.dc], ai = lut_idx[4 + e.ac];
+        dcl = di < kLutCache ? s_lut + di : L.luts + di;
+        acl = ai < kLutCache ? s_lut + ai : L.luts + ai;
+    };
+    setup_block();
+    int k = 0;
+    uint16_t kind = kDiagNone;
+    uint32_t errpos = 0;
+    const uint16_t barrier_kind = barrier_rst ? kJMarkerInData : kJEndOfData;
+    for (;;) {
+        refill(r);
+        const HuffLut *T = k == 0 ? dcl : acl;
+        const uint32_t avail = r.limit - r.used;
+        const int32_t fv = T->fastv[r.buf >> 55];
+        int run, size, codelen, val = 0;
+        bool have_val;
+        if (fv != 0 && (uint32_t)(fv & 0xff) <= avail) {
+            run = (fv >> 8) & 15;
+            size = (fv >> 12) & 15;
+            codelen = (fv & 0xff) - size;
+            val = fv >> 16;
+            have_val = true;
+        } else {
             uint32_t sym;
-            int len = huff_peek(dct, L.symbols, s, &sym);
-            if (len == 0 || len > s.nbits) {
-                err.kind = (len == 0 && s.nbits >= 16) ? kJNoHuffCode : (barrier_rst ? kJMarkerInData : kJEndOfData);
-                err.bitpos = s.used + 16;
+            codelen = slow_symbol(T, L.symbols, r.buf, &sym);
+            if (codelen == 0 || (uint32_t)codelen > avail) {
+                kind = (codelen == 0 && avail >= 16) ? (uint16_t)kJNoHuffCode : barrier_kind;
+                errpos = r.used + 16;
                 break;
             }
-            consume(s, len);
-            if (sym > 11) {
-                err.kind = kJDcCategory;
-                err.bitpos = s.used;
-                break;
-            }
-            int32_t diff = 0;
-            if (sym) {
-                if (s.nbits < (int)sym) {
-                    err.kind = barrier_rst ? kJMarkerInData : kJEndOfData;
+            have_val = false;
+            if (k == 0) {  // decoder.rs:503-506
+                run = 0;
+                size = (int)sym;
+                if (size > 11) {
+                    take(r, codelen);
+                    kind = kJDcCategory;
+                    errpos = r.used;
                     break;
                 }
-                int32_t v = (int32_t)(s.buf >> (64 - sym));
-                consume(s, sym);
-                diff = v < (1 << (sym - 1)) ? v + 1 - (1 << sym) : v;
-            }
-            int64_t p = (int64_t)pred[e.comp] + diff;
-            if (p > INT32_MAX || p < INT32_MIN) {
-                err.kind = kJDcPredOverflow;
-                err.bitpos = s.used;
-                break;
-            }
-            pred[e.comp] = (int32_t)p;
-            int64_t dq = p * (int64_t)Q[0];
-            if (dq > INT32_MAX || dq < INT32_MIN) {
-                err.kind = kJDcDeqOverflow;
-                err.bitpos = s.used;
-                break;
-            }
-            // AC (decoder.rs:517-546)
-            int k = 1;
-            while (k < 64) {
-                fill(s);
-                len = huff_peek(act, L.symbols, s, &sym);
-                if (len == 0 || len > s.nbits) {
-                    err.kind = (len == 0 && s.nbits >= 16) ? kJNoHuffCode : (barrier_rst ? kJMarkerInData : kJEndOfData);
-                    err.bitpos = s.used + 16;
-                    break;
-                }
-                consume(s, len);
-                int run = sym >> 4, size = sym & 15;
+            } else {  // decoder.rs:519-537
+                run = (int)(sym >> 4);
+                size = (int)(sym & 15);
                 if (size == 0) {
-                    if (run == 0) break;
-                    if (run != 15) {
-                        err.kind = kJAcZeroSize;
-                        err.bitpos = s.used;
-                        break;
+                    take(r, codelen);
+                    if (run != 0) {
+                        if (run != 15) {
+                            kind = kJAcZeroSize;
+                            errpos = r.used;
+                            break;
+                        }
+                        k += 16;
+                        if (k > 64) {
+                            kind = kJZrlOverrun;
+                            errpos = r.used;
+                            break;
+                        }
+                        if (k < 64) continue;
                     }
-                    k += 16;
-                    if (k > 64) {
-                        err.kind = kJZrlOverrun;
-                        err.bitpos = s.used;
-                        break;
-                    }
-                    continue;
+                    k = 64;  // EOB, or a zero run ending exactly at index 64
                 }
                 if (size > 10) {
-                    err.kind = kJAcCategory;
-                    err.bitpos = s.used;
+                    take(r, codelen);
+                    kind = kJAcCategory;
+                    errpos = r.used;
                     break;
                 }
-                k += run;
-                if (k >= 64) {
-                    err.kind = kJAcRun;
-                    err.bitpos = s.used;
-                    break;
-                }
-                if (s.nbits < size) {
-                    err.kind = barrier_rst ? kJMarkerInData : kJEndOfData;
-                    break;
-                }
-                int32_t v = (int32_t)(s.buf >> (64 - size));
-                consume(s, size);
-                v = v < (1 << (size - 1)) ? v + 1 - (1 << size) : v;
-                stage[c_zigzag[k]] = (int16_t)v;
-                k++;
             }
-            if (err.kind != kDiagNone) break;
-            // block write (levels + dequantised DC)
-            uint32_t gx, gy;
-            if (F.interleaved) {
-                gx = mx * C.h + e.bx;
-                gy = my * C.v + e.by;
-            } else {
-                gx = mx;
-                gy = my;
-            }
-            uint64_t blk = F.blk_off + C.blk_base + (uint64_t)gy * C.bw + gx;
-            int4 *dst = reinterpret_cast<int4 *>(L.coef + blk * 64);
-#pragma unroll
-            for (int q = 0; q < 8; q++) dst[q] = stage4[q];
-            L.dc[blk] = (int32_t)dq;
         }
+        if (k < 64) {
+            if (k > 0 && k + run >= 64) {  // decoder.rs:538-541, before the magnitude bits
+                take(r, codelen);
+                kind = kJAcRun;
+                errpos = r.used;
+                break;
+            }
+            if ((uint32_t)(codelen + size) > avail) {  // magnitude bits run into the barrier
+                kind = barrier_kind;
+                break;
+            }
+            if (!have_val && size) {  // receive_extend (entropy.rs:168-182)
+                int32_t v = (int32_t)((r.buf << codelen) >> (64 - size));
+                val = v < (1 << (size - 1)) ? v + 1 - (1 << size) : v;
+            }
+            take(r, codelen + size);
+            if (k == 0) {  // decoder.rs:507-515
+                int64_t p = (int64_t)pred[comp] + val;
+                if (p > INT32_MAX || p < INT32_MIN) {
+                    kind = kJDcPredOverflow;
+                    errpos = r.used;
+                    break;
+                }
+                pred[comp] = (int32_t)p;
+                int64_t d = p * (int64_t)q0;
+                if (d > INT32_MAX || d < INT32_MIN) {
+                    kind = kJDcDeqOverflow;
+                    errpos = r.used;
+                    break;
+                }
+                dq = (int32_t)d;
+                k = 1;
+                continue;
+            }
+            k += run;
+            stage[s_zz[k]] = (int16_t)val;
+            if (++k < 64) continue;
+        }
+        // block complete: levels + dequantised DC out, staging cleared
+        int4 *dst = reinterpret_cast<int4 *>(L.coef + blk * 64);
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            dst[q] = stage4[q];
+            stage4[q] = make_int4(0, 0, 0, 0);
+        }
+        L.dc[blk] = dq;
+        if (++si == sched_len) {
+            si = 0;
+            if (++mcu == mcu1) break;
+        }
+        setup_block();
+        k = 0;
     }
 
-    if (err.kind != kDiagNone) {
-        uint32_t offset;
-        if (err.kind == kJMarkerInData) {
-            offset = barrier;
-            out = make_diag(kJMarkerInData, offset, 0xd0 + rst[iv].number);
-        } else if (err.kind == kJEndOfData) {
-            out = make_diag(kJEndOfData, n_tok);
-        } else {
-            offset = start + (err.bitpos + 7) / 8;
-            out = make_diag(err.kind, offset);
-        }
-    } else if (iv + 1 < F.n_intervals) {
+    Diag out = make_diag(kDiagNone);
+    if (kind != kDiagNone) {
+#pragma unroll
+        for (int q = 0; q < 8; q++) stage4[q] = make_int4(0, 0, 0, 0);
+        if (kind == kJMarkerInData) out = make_diag(kJMarkerInData, barrier, 0xd0 + rst[iv].number);
+        else if (kind == kJEndOfData) out = make_diag(kJEndOfData, n_tok);
+        else out = make_diag(kind, start + (errpos + 7) / 8);
+    } else if (iv + 1 < n_int) {
         // consume_restart before the next interval (entropy.rs:111-134)
-        uint32_t tend = start + (s.used + 7) / 8;
+        uint32_t tend = start + (r.used + 7) / 8;
         uint32_t expected = iv & 7;
         if (barrier_rst && rst[iv].tok == tend) {
             if (rst[iv].number != expected) out = make_diag(kJRstMismatch, tend, expected, 0xd0 + rst[iv].number);
-        } else if (tend < n_tok && F.tok[tend] == 0xff) {
+        } else if (tend < n_tok && Fp->tok[tend] == 0xff) {
             out = make_diag(kJRstMismatch, tend, expected, 0x00);
         } else {
             out = make_diag(kJExpectRst, tend);
@@ -477,10 +512,21 @@ __device__ void decode_interval(const JpegLaunch &L, uint32_t item, int16_t *sta
 
 template <int MAXC>
 __global__ void __launch_bounds__(kEntropyThreads) entropy_kernel(JpegLaunch L, uint32_t first, uint32_t count) {
+    __shared__ __align__(16) HuffLut s_lut[kLutCache];
     __shared__ __align__(16) int16_t s_stage[kEntropyThreads * kStageStride];
+    __shared__ uint8_t s_zz[64];
+    const uint32_t nl = min(L.n_luts, (uint32_t)kLutCache);
+    const int4 *src = reinterpret_cast<const int4 *>(L.luts);
+    int4 *dst = reinterpret_cast<int4 *>(s_lut);
+    for (uint32_t i = threadIdx.x; i < nl * (uint32_t)(sizeof(HuffLut) / 16); i += blockDim.x) dst[i] = src[i];
+    if (threadIdx.x < 64) s_zz[threadIdx.x] = (uint8_t)c_zigzag[threadIdx.x];
+    int4 *mine = reinterpret_cast<int4 *>(s_stage + threadIdx.x * kStageStride);
+#pragma unroll
+    for (int q = 0; q < 8; q++) mine[q] = make_int4(0, 0, 0, 0);
+    __syncthreads();
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= count) return;
-    decode_interval<MAXC>(L, first + i, s_stage + threadIdx.x * kStageStride);
+    decode_interval<MAXC>(L, first + i, s_stage + threadIdx.x * kStageStride, s_lut, s_zz);
 }
 
 __global__ void resolve_kernel(JpegLaunch L) {
@@ -673,9 +719,6 @@ void launch_jpeg_scan(const JpegLaunch &L, cudaStream_t s) {
 }
 
 void launch_jpeg_entropy(const JpegLaunch &L, cudaStream_t s) {
-    if (L.n_items_small)
-        entropy_kernel<4><<<(L.n_items_small + kEntropyThreads - 1) / kEntropyThreads, kEntropyThreads, 0, s>>>(
-            L, 0, L.n_items_small);
     uint32_t big = L.n_items - L.n_items_small;
     if (big)
         entropy_kernel<256><<<(big + kEntropyThreads - 1) / kEntropyThreads, kEntropyThreads, 0, s>>>(

@@ -1,0 +1,788 @@
+// Chunked, self-synchronising Huffman decode of baseline JPEG scans (sm_103a).
+//
+// The reference decodes a scan serially, one restart interval after another
+// (crates/codecs/mjpeg/src/decoder.rs:313-410, 495-548; entropy.rs:57-182). A
+// thread per interval leaves a GB300 nearly idle (135 intervals per 1080p frame,
+// one per scan without DRI), so every interval is cut into fixed-size bit slices
+// that decode in parallel. Huffman codes resynchronise: a decode started at a
+// wrong bit or in a wrong coefficient state soon meets the true decode at a
+// symbol boundary with the same state, and from there both are identical.
+//
+//   slice_plan     per frame: interval token ranges, slice counts, slot -> interval map
+//   slice_spec     every slice decoded from a guessed state (the first slice from the
+//                  true one) up to its end; keeps the state at 1/4, 1/2 and 3/4 of it
+//   slice_sync     (twice) each slice whose start no longer equals its predecessor's
+//                  exit state re-decodes from that state until it meets one of its own
+//                  checkpoints (then the rest is known) or its end
+//   slice_fix      per interval, only when the last sync pass still changed a state:
+//                  walks the slices in order until every start equals the previous
+//                  exit. Then slice 0 starts in the true state and each exit is the
+//                  true state at that point, so every start is the true one.
+//   slice_prefix   per interval: block index and DC predictors at each slice start
+//   slice_decode   the final decode from true states: quantised AC levels, dequantised
+//                  DC, and each slice's first event (an error, or the interval's last
+//                  block completed)
+//   slice_resolve  per interval: the earliest event in stream order becomes the
+//                  interval's result, or the restart-marker check (entropy.rs:111-134)
+//
+// A slice owns the blocks whose DC symbol starts between its start state and its
+// exit state; it decodes the block that straddles its end to completion, and skips
+// (decodes without output) the one straddling its start. Errors are reported only
+// by the owner of the block they occur in, so the earliest reported event is the
+// one the serial decoder stops at.
+#include <cuda_runtime.h>
+
+#include "kernels.h"
+#include "tables.h"
+
+namespace mmr {
+namespace {
+
+__constant__ uint8_t c_slice_zz[64] = MMR_ZIGZAG_INIT;
+
+constexpr unsigned long long kStErr = ~0ull;        // no state: the decode failed before this point
+constexpr unsigned long long kStGuess = ~0ull - 1;  // start not yet derived from the predecessor
+constexpr int kSliceThreads = 128;
+constexpr int kStride = 72;  // int16 per staged block (144 B: conflict-free 16 B rows)
+constexpr int kKeyBits = 26;
+constexpr uint16_t kBarrierErr = 0xffff;
+
+__device__ __forceinline__ unsigned long long pack_state(unsigned long long p, uint32_t si, uint32_t k) {
+    return (p << 16) | (si << 8) | k;
+}
+
+__device__ __forceinline__ uint32_t bswap32(uint32_t x) { return __byte_perm(x, 0, 0x0123); }
+
+// Big-endian bit reader over unstuffed tokens, 32-bit word loads. It may hold
+// bits past the interval's barrier; callers never use more than `avail` bits.
+struct Bits {
+    const uint32_t *words;
+    uint32_t wpos;
+    int nbits;
+    uint64_t buf;
+    uint32_t used;  // bits consumed, counted from the reader's base position
+};
+
+__device__ __forceinline__ void bits_init(Bits &r, const uint8_t *tok, unsigned long long bit, uint32_t used) {
+    r.words = reinterpret_cast<const uint32_t *>(tok);
+    const uint32_t w0 = (uint32_t)(bit >> 5), skip = (uint32_t)bit & 31;
+    r.buf = (uint64_t)bswap32(__ldg(r.words + w0)) << (32 + skip);
+    r.nbits = 32 - (int)skip;
+    r.wpos = w0 + 1;
+    r.used = used;
+}
+
+__device__ __forceinline__ void refill(Bits &r) {
+    if (r.nbits <= 32) {
+        r.buf |= (uint64_t)bswap32(__ldg(r.words + r.wpos)) << (32 - r.nbits);
+        r.wpos++;
+        r.nbits += 32;
+    }
+}
+
+__device__ __forceinline__ void take(Bits &r, int n) {
+    r.buf <<= n;
+    r.nbits -= n;
+    r.used += n;
+}
+
+// Code length of the next Huffman code (entropy.rs:57-70), 0 when none of length <= 16 matches.
+__device__ __forceinline__ int slow_symbol(const HuffLut *__restrict__ T, const uint8_t *__restrict__ symbols,
+                                           uint64_t buf, uint32_t *sym) {
+    const uint32_t e = __ldg(&T->fast[buf >> 55]);
+    if (e) {
+        *sym = e & 0xff;
+        return (int)(e >> 8);
+    }
+    const uint32_t code16 = (uint32_t)(buf >> 48);
+#pragma unroll 1
+    for (int l = 10; l <= 16; l++) {
+        const int32_t c = (int32_t)(code16 >> (16 - l));
+        if (c <= __ldg(&T->maxcode[l])) {
+            *sym = __ldg(&symbols[__ldg(&T->sym_off) + __ldg(&T->valptr[l]) + c]);
+            return l;
+        }
+    }
+    return 0;
+}
+
+enum : int { kSymError = 0, kSymDc, kSymAc, kSymRun, kSymEob };
+
+// Decodes one symbol for coefficient index k (0: DC), in the reference's order of
+// checks (decoder.rs:501-546). kSymDc: val = DC difference, k = 1. kSymAc: level
+// val at zigzag index `at`, k past it (64 completes the block). kSymRun: sixteen
+// zeros. kSymEob: block complete. kSymError: err (kBarrierErr when the symbol runs
+// into the barrier) and errbit, the reader position the reference reports.
+__device__ __forceinline__ int next_symbol(Bits &r, uint32_t avail, const HuffLut *__restrict__ T,
+                                           const uint8_t *__restrict__ symbols, int &k, int &at, int32_t &val,
+                                           uint16_t &err, uint32_t &errbit) {
+    refill(r);
+    const int32_t fv = __ldg(&T->fastv[r.buf >> 55]);
+    if (fv != 0) {
+        const int total = fv & 0xff, run = (fv >> 8) & 15;
+        if ((uint32_t)total <= avail && (k == 0 || k + run < 64)) {
+            val = fv >> 16;
+            take(r, total);
+            if (k == 0) {
+                k = 1;
+                return kSymDc;
+            }
+            at = k + run;
+            k = at + 1;
+            return kSymAc;
+        }
+    }
+    uint32_t sym;
+    const int l = slow_symbol(T, symbols, r.buf, &sym);
+    if (l == 0 || (uint32_t)l > avail) {
+        err = (l == 0 && avail >= 16) ? (uint16_t)kJNoHuffCode : kBarrierErr;
+        errbit = r.used + 16;
+        return kSymError;
+    }
+    int size, run;
+    if (k == 0) {
+        size = (int)sym;
+        run = 0;
+        if (size > 11) {
+            take(r, l);
+            err = kJDcCategory;
+            errbit = r.used;
+            return kSymError;
+        }
+    } else {
+        run = (int)(sym >> 4);
+        size = (int)(sym & 15);
+        if (size == 0) {
+            take(r, l);
+            if (run == 0) {
+                k = 64;
+                return kSymEob;
+            }
+            if (run != 15) {
+                err = kJAcZeroSize;
+                errbit = r.used;
+                return kSymError;
+            }
+            k += 16;
+            if (k > 64) {
+                err = kJZrlOverrun;
+                errbit = r.used;
+                return kSymError;
+            }
+            return k == 64 ? kSymEob : kSymRun;
+        }
+        if (size > 10) {
+            take(r, l);
+            err = kJAcCategory;
+            errbit = r.used;
+            return kSymError;
+        }
+        if (k + run >= 64) {
+            take(r, l);
+            err = kJAcRun;
+            errbit = r.used;
+            return kSymError;
+        }
+    }
+    if ((uint32_t)(l + size) > avail) {
+        err = kBarrierErr;
+        errbit = r.used;
+        return kSymError;
+    }
+    int32_t v = 0;
+    if (size) {  // receive_extend (entropy.rs:168-182)
+        v = (int32_t)((r.buf << l) >> (64 - size));
+        v = v < (1 << (size - 1)) ? v + 1 - (1 << size) : v;
+    }
+    take(r, l + size);
+    val = v;
+    if (k == 0) {
+        k = 1;
+        return kSymDc;
+    }
+    at = k + run;
+    k = at + 1;
+    return kSymAc;
+}
+
+// Tables of MCU block si.
+struct BlockTabs {
+    const HuffLut *dc;
+    const HuffLut *ac;
+    uint32_t comp;
+};
+
+__device__ __forceinline__ BlockTabs block_tabs(const JpegLaunch &L, const JFrame &F, uint32_t si) {
+    const JSched e = L.sched[F.sched_off + si];
+    BlockTabs t;
+    t.comp = e.comp;
+    t.dc = L.luts + F.lut[e.dc];
+    t.ac = L.luts + F.lut[4 + e.ac];
+    return t;
+}
+
+__device__ __forceinline__ void add_dc(int32_t (&dc)[4], uint32_t comp, int32_t v) {
+#pragma unroll
+    for (int c = 0; c < 4; c++)
+        if (comp == (uint32_t)c) dc[c] += v;
+}
+
+struct SliceRef {
+    uint32_t item, j;
+    IvInfo v;
+    const JFrame *F;
+    bool last;
+};
+
+__device__ __forceinline__ bool slice_ref(const JpegLaunch &L, uint32_t slot, SliceRef &s) {
+    if (slot >= L.n_slots) return false;
+    s.item = L.slot_item[slot];
+    if (s.item == 0xffffffffu) return false;
+    s.v = L.ivs[s.item];
+    s.j = slot - s.v.slot_first;
+    s.F = L.frames + L.items[s.item].x;
+    s.last = s.j + 1 == s.v.n_slices;
+    return true;
+}
+
+__device__ __forceinline__ uint32_t clamp_u32(unsigned long long x) {
+    return x > 0xffffffffull ? 0xffffffffu : (uint32_t)x;
+}
+
+// ------------------------------------------------------------------ plan ---
+
+__global__ void slice_plan_kernel(JpegLaunch L) {
+    const uint32_t f = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    const uint32_t lane = threadIdx.x & 31;
+    if (f >= L.n_frames) return;
+    const JFrame &F = L.frames[f];
+    if (!F.decode || F.ncomp > 4) return;
+    const JState &st = L.states[f];
+    const unsigned long long termv = st.term;
+    const bool scan_ok = termv != ~0ull && !((termv >> 8) & 1);
+    const uint32_t n_int = F.n_intervals;
+    const uint32_t n_rst = min(st.n_rst, n_int), n_tok = st.n_tokens;
+    const RstEntry *rst = L.rsts + F.rst_off;
+    const uint32_t S = L.slice_bits;
+    uint32_t used = 0;
+    for (uint32_t c = 0; c < n_int; c += 32) {
+        const uint32_t iv = c + lane;
+        uint32_t n_s = 0, start = 0, barrier = 0, flags = 0, blocks = 0;
+        if (iv < n_int) {
+            bool dec = scan_ok;
+            if (iv == 0) start = 0;
+            else if (iv - 1 < n_rst) start = rst[iv - 1].tok;
+            else dec = false;  // no RST precedes it: an earlier interval fails its restart check
+            if (dec) {
+                flags = iv < n_rst ? 1u : 0u;
+                barrier = flags ? rst[iv].tok : n_tok;
+                const unsigned long long lbits = (unsigned long long)(barrier - start) * 8;
+                n_s = (uint32_t)max(1ull, (lbits + S - 1) / S);
+                const uint32_t mcu0 = iv * F.ri, mcu1 = min(mcu0 + F.ri, F.total_mcus);
+                blocks = (mcu1 - mcu0) * F.sched_len;
+            }
+        }
+        uint32_t incl = n_s;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t o = __shfl_up_sync(0xffffffffu, incl, d);
+            if (lane >= (uint32_t)d) incl += o;
+        }
+        const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+        uint32_t first = used + incl - n_s;
+        if (used + total > F.slot_count) {  // cannot happen: slot_count bounds the token count
+            n_s = 0;
+            first = used;
+        }
+        if (iv < n_int) {
+            IvInfo v;
+            v.start = start;
+            v.barrier = barrier;
+            v.slot_first = F.slot_first + first;
+            v.n_slices = n_s;
+            v.blocks = blocks;
+            v.flags = flags;
+            L.ivs[F.item_base + iv] = v;
+            L.iv_key[F.item_base + iv] = ~0ull;
+        }
+        for (uint32_t t = 0; t < 32 && c + t < n_int; t++) {
+            const uint32_t nt = __shfl_sync(0xffffffffu, n_s, t), ft = __shfl_sync(0xffffffffu, first, t);
+            for (uint32_t x = lane; x < nt; x += 32) L.slot_item[F.slot_first + ft + x] = F.item_base + c + t;
+        }
+        if (used + total <= F.slot_count) used += total;
+    }
+    for (uint32_t x = used + lane; x < F.slot_count; x += 32) L.slot_item[F.slot_first + x] = 0xffffffffu;
+}
+
+// ------------------------------------------------------ speculative pass ---
+
+__global__ void __launch_bounds__(kSliceThreads) slice_spec_kernel(JpegLaunch L) {
+    const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+    SliceRef s;
+    if (!slice_ref(L, slot, s)) return;
+    const bool guess = s.j != 0;
+    SliceSync out;
+    out.start = guess ? kStGuess : pack_state(0, 0, 0);
+    out.exit = kStErr;
+    out.blocks = 0;
+    out.pad = 0;
+#pragma unroll
+    for (int c = 0; c < 4; c++) out.dc[c] = 0;
+    if (s.last) {  // nothing reads the last slice's exit or counts
+        L.sync[slot] = out;
+        return;
+    }
+    const JFrame &F = *s.F;
+    const uint32_t S = L.slice_bits;
+    const unsigned long long p0 = (unsigned long long)s.j * S;
+    const unsigned long long lbits = (unsigned long long)(s.v.barrier - s.v.start) * 8;
+    const uint32_t lim = clamp_u32(lbits - p0);  // bits before the barrier, from p0
+    const uint64_t tokbit = (uint64_t)s.v.start * 8;
+    Bits r;
+    bits_init(r, F.tok, tokbit + p0, 0);
+    int k = guess ? 1 : 0;
+    uint32_t si = 0;
+    BlockTabs tb = block_tabs(L, F, si);
+    uint32_t blocks = 0;
+    int32_t dc[4] = {0, 0, 0, 0};
+    SliceSpec *sp = L.spec + slot;
+    uint32_t q = 0, recorded = 0;
+    const uint32_t step = S / (kSliceCheckpoints + 1);
+    unsigned long long exit_state = kStErr;
+    for (;;) {
+        const uint32_t pr = r.used;
+        if (pr >= S) {
+            exit_state = pack_state(p0 + pr, si, k);
+            break;
+        }
+        if (guess) {
+            while (q < (uint32_t)kSliceCheckpoints && pr >= (q + 1) * step) {
+                SlicePoint cp;
+                cp.state = pack_state(p0 + pr, si, k);
+                cp.blocks = blocks;
+                cp.pad = 0;
+#pragma unroll
+                for (int c = 0; c < 4; c++) cp.dc[c] = dc[c];
+                sp->cp[q] = cp;
+                recorded |= 1u << q;
+                q++;
+            }
+        }
+        if (k == 0) blocks++;
+        int at;
+        int32_t val;
+        uint16_t err;
+        uint32_t eb;
+        const int sy = next_symbol(r, lim - pr, k == 0 ? tb.dc : tb.ac, L.symbols, k, at, val, err, eb);
+        if (sy == kSymDc) {
+            add_dc(dc, tb.comp, val);
+            continue;
+        }
+        if (sy == kSymRun || (sy == kSymAc && k < 64)) continue;
+        if (sy == kSymError) {
+            if (!guess || err == kBarrierErr) break;  // exit_state stays kStErr
+            // A decode from a guessed state met an invalid symbol: start again one bit
+            // later; what came before cannot lead to the exit, so its checkpoints go.
+            for (uint32_t x = 0; x < (uint32_t)kSliceCheckpoints; x++)
+                if (recorded & (1u << x)) sp->cp[x].state = kStErr;
+            recorded = 0;
+            blocks = 0;
+#pragma unroll
+            for (int c = 0; c < 4; c++) dc[c] = 0;
+            k = 1;
+            si = 0;
+            tb = block_tabs(L, F, si);
+            bits_init(r, F.tok, tokbit + p0 + pr + 1, pr + 1);
+            continue;
+        }
+        k = 0;  // block complete
+        si = si + 1 == F.sched_len ? 0 : si + 1;
+        tb = block_tabs(L, F, si);
+    }
+    if (guess) {
+        for (uint32_t x = 0; x < (uint32_t)kSliceCheckpoints; x++)
+            if (!(recorded & (1u << x))) sp->cp[x].state = kStErr;
+        SlicePoint e;
+        e.state = exit_state;
+        e.blocks = blocks;
+        e.pad = 0;
+#pragma unroll
+        for (int c = 0; c < 4; c++) e.dc[c] = dc[c];
+        sp->exit = e;
+    }
+    out.exit = exit_state;
+    out.blocks = blocks;
+#pragma unroll
+    for (int c = 0; c < 4; c++) out.dc[c] = dc[c];
+    L.sync[slot] = out;
+}
+
+// ------------------------------------------------------------ sync pass ---
+
+// Re-decodes slice `slot` (not the first, not the last) from state `from`, the
+// exit of its predecessor, until it meets one of the slice's speculative
+// checkpoints or passes the slice end. Returns whether the exit state changed.
+__device__ bool resync_slice(const JpegLaunch &L, uint32_t slot, const SliceRef &s, unsigned long long from) {
+    SliceSync out;
+    out.start = from;
+    out.pad = 0;
+    out.blocks = 0;
+#pragma unroll
+    for (int c = 0; c < 4; c++) out.dc[c] = 0;
+    const unsigned long long old_exit = L.sync[slot].exit;
+    if (from == kStErr) {
+        out.exit = kStErr;
+        L.sync[slot] = out;
+        return old_exit != kStErr;
+    }
+    const JFrame &F = *s.F;
+    const uint32_t S = L.slice_bits;
+    const unsigned long long p0 = from >> 16;
+    const unsigned long long nominal = (unsigned long long)s.j * S;
+    const uint32_t rel = (uint32_t)(p0 - nominal);  // < one symbol: from is the first boundary past nominal
+    const unsigned long long lbits = (unsigned long long)(s.v.barrier - s.v.start) * 8;
+    const uint32_t lim = clamp_u32(lbits - p0);
+    Bits r;
+    bits_init(r, F.tok, (uint64_t)s.v.start * 8 + p0, 0);
+    int k = (int)(from & 0xff);
+    uint32_t si = (uint32_t)(from >> 8) & 0xff;
+    BlockTabs tb = block_tabs(L, F, si);
+    uint32_t blocks = 0;
+    int32_t dc[4] = {0, 0, 0, 0};
+    const SliceSpec *sp = L.spec + slot;
+    const uint32_t step = S / (kSliceCheckpoints + 1);
+    uint32_t q = 0;
+    while (q < (uint32_t)kSliceCheckpoints && (q + 1) * step <= rel) q++;  // marks already behind
+    unsigned long long exit_state = kStErr;
+    for (;;) {
+        const uint32_t pr = r.used;
+        const uint32_t pn = pr + rel;  // position from the nominal slice start
+        if (pn >= S) {
+            exit_state = pack_state(p0 + pr, si, k);
+            break;
+        }
+        bool matched = false;
+        while (q < (uint32_t)kSliceCheckpoints && pn >= (q + 1) * step) {
+            const unsigned long long cs = sp->cp[q].state;
+            if (cs != kStErr && cs == pack_state(p0 + pr, si, k)) {
+                const SlicePoint cp = sp->cp[q], e = sp->exit;
+                exit_state = e.state;
+                blocks += e.blocks - cp.blocks;
+#pragma unroll
+                for (int c = 0; c < 4; c++) dc[c] += e.dc[c] - cp.dc[c];
+                matched = true;
+                break;
+            }
+            q++;
+        }
+        if (matched) break;
+        if (k == 0) blocks++;
+        int at;
+        int32_t val;
+        uint16_t err;
+        uint32_t eb;
+        const int sy = next_symbol(r, lim - pr, k == 0 ? tb.dc : tb.ac, L.symbols, k, at, val, err, eb);
+        if (sy == kSymDc) {
+            add_dc(dc, tb.comp, val);
+            continue;
+        }
+        if (sy == kSymRun || (sy == kSymAc && k < 64)) continue;
+        if (sy == kSymError) break;  // exit_state stays kStErr
+        k = 0;
+        si = si + 1 == F.sched_len ? 0 : si + 1;
+        tb = block_tabs(L, F, si);
+    }
+    out.exit = exit_state;
+    out.blocks = blocks;
+#pragma unroll
+    for (int c = 0; c < 4; c++) out.dc[c] = dc[c];
+    L.sync[slot] = out;
+    return exit_state != old_exit;
+}
+
+__global__ void __launch_bounds__(kSliceThreads) slice_sync_kernel(JpegLaunch L, uint32_t pass) {
+    const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+    SliceRef s;
+    if (!slice_ref(L, slot, s) || s.j == 0) return;
+    const unsigned long long prev = *(volatile const unsigned long long *)&L.sync[slot - 1].exit;
+    const unsigned long long cur = L.sync[slot].start;
+    if (prev == cur) return;
+    if (s.last) {
+        L.sync[slot].start = prev;
+        return;
+    }
+    if (resync_slice(L, slot, s, prev)) atomicAdd(&L.sync_dirty[pass], 1u);
+}
+
+// One warp per interval; runs only when the last sync pass still changed an exit state.
+__global__ void slice_fix_kernel(JpegLaunch L) {
+    if (*(volatile uint32_t *)&L.sync_dirty[kSyncPasses - 1] == 0) return;
+    const uint32_t item = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    const uint32_t lane = threadIdx.x & 31;
+    if (item >= L.n_items_small) return;
+    const IvInfo v = L.ivs[item];
+    for (uint32_t c = 1; c < v.n_slices; c += 32) {
+        for (;;) {
+            const uint32_t j = c + lane;
+            bool bad = false;
+            if (j < v.n_slices) {
+                const uint32_t slot = v.slot_first + j;
+                bad = *(volatile unsigned long long *)&L.sync[slot].start !=
+                      *(volatile unsigned long long *)&L.sync[slot - 1].exit;
+            }
+            const uint32_t m = __ballot_sync(0xffffffffu, bad);
+            if (!m) break;
+            const uint32_t first = __ffs(m) - 1;
+            if (lane == first) {
+                const uint32_t slot = v.slot_first + j;
+                SliceRef s;
+                slice_ref(L, slot, s);
+                const unsigned long long prev = *(volatile unsigned long long *)&L.sync[slot - 1].exit;
+                if (s.last) L.sync[slot].start = prev;
+                else resync_slice(L, slot, s, prev);
+                __threadfence_block();
+            }
+            __syncwarp();
+        }
+    }
+}
+
+// ---------------------------------------------------------------- prefix ---
+
+__global__ void slice_prefix_kernel(JpegLaunch L) {
+    const uint32_t item = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    const uint32_t lane = threadIdx.x & 31;
+    if (item >= L.n_items_small) return;
+    const IvInfo v = L.ivs[item];
+    uint32_t carry_b = 0;
+    long long carry_d[4] = {0, 0, 0, 0};
+    for (uint32_t c = 0; c < v.n_slices; c += 32) {
+        const uint32_t j = c + lane;
+        uint32_t b = 0;
+        long long d[4] = {0, 0, 0, 0};
+        if (j + 1 < v.n_slices) {  // the last slice's counts are never needed
+            const SliceSync &y = L.sync[v.slot_first + j];
+            b = y.blocks;
+#pragma unroll
+            for (int q = 0; q < 4; q++) d[q] = y.dc[q];
+        }
+        uint32_t ib = b;
+        long long id[4] = {d[0], d[1], d[2], d[3]};
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t tb = __shfl_up_sync(0xffffffffu, ib, o);
+            long long td[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) td[q] = __shfl_up_sync(0xffffffffu, id[q], o);
+            if (lane >= (uint32_t)o) {
+                ib += tb;
+#pragma unroll
+                for (int q = 0; q < 4; q++) id[q] += td[q];
+            }
+        }
+        if (j < v.n_slices) {
+            SlicePrefix P;
+            P.base = carry_b + ib - b;
+            P.pad = 0;
+#pragma unroll
+            for (int q = 0; q < 4; q++) P.dc[q] = carry_d[q] + id[q] - d[q];
+            L.prefix[v.slot_first + j] = P;
+        }
+        carry_b += __shfl_sync(0xffffffffu, ib, 31);
+#pragma unroll
+        for (int q = 0; q < 4; q++) carry_d[q] += __shfl_sync(0xffffffffu, id[q], 31);
+    }
+}
+
+// ---------------------------------------------------------------- decode ---
+
+__device__ __forceinline__ void report(const JpegLaunch &L, const SliceRef &s, uint32_t slot, unsigned long long pos,
+                                       const Diag &d, uint32_t complete) {
+    SliceEvent e;
+    e.diag = d;
+    e.complete = complete;
+    L.events[slot] = e;
+    atomicMin(&L.iv_key[s.item], (pos << kKeyBits) | s.j);
+}
+
+__global__ void __launch_bounds__(kSliceThreads) slice_decode_kernel(JpegLaunch L) {
+    __shared__ __align__(16) int16_t s_stage[kSliceThreads * kStride];
+    int16_t *stage = s_stage + threadIdx.x * kStride;
+    int4 *stage4 = reinterpret_cast<int4 *>(stage);
+#pragma unroll
+    for (int q = 0; q < 8; q++) stage4[q] = make_int4(0, 0, 0, 0);
+    const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+    SliceRef s;
+    if (!slice_ref(L, slot, s)) return;
+    const unsigned long long from = L.sync[slot].start;
+    if (from == kStErr || from == kStGuess) return;
+    const SlicePrefix P = L.prefix[slot];
+    const uint32_t B = s.v.blocks;
+    if (P.base >= B) return;
+    const uint32_t nown = s.last ? B - P.base : min(L.sync[slot].blocks, B - P.base);
+    if (nown == 0) return;
+    const JFrame &F = *s.F;
+    const uint32_t iv = L.items[s.item].y;
+    const unsigned long long p0 = from >> 16;
+    const unsigned long long lbits = (unsigned long long)(s.v.barrier - s.v.start) * 8;
+    const uint32_t lim = clamp_u32(lbits - p0);
+    const uint32_t sched_len = F.sched_len;
+    Bits r;
+    bits_init(r, F.tok, (uint64_t)s.v.start * 8 + p0, 0);
+    int k = (int)(from & 0xff);
+    uint32_t si = (uint32_t)(from >> 8) & 0xff;
+    int at;
+    int32_t val;
+    uint16_t err;
+    uint32_t eb;
+    if (k != 0) {  // the block straddling the start belongs to an earlier slice
+        const BlockTabs tb = block_tabs(L, F, si);
+        for (;;) {
+            const int sy = next_symbol(r, lim - r.used, tb.ac, L.symbols, k, at, val, err, eb);
+            if (sy == kSymError) return;
+            if (sy == kSymEob || (sy == kSymAc && k == 64)) break;
+        }
+        si = si + 1 == sched_len ? 0 : si + 1;
+        k = 0;
+    }
+    long long pred[4];
+#pragma unroll
+    for (int c = 0; c < 4; c++) pred[c] = P.dc[c];
+    const JComp *comps = L.comps + F.comp_off;
+    const uint16_t *quant = L.quant + F.quant_off;
+    const RstEntry *rst = L.rsts + F.rst_off;
+    const uint32_t mcu0 = iv * F.ri;
+    for (uint32_t owned = 0; owned < nown; owned++) {
+        const uint32_t b = P.base + owned;
+        const uint32_t mcu = mcu0 + b / sched_len;
+        const JSched e = L.sched[F.sched_off + si];
+        const JComp &C = comps[e.comp];
+        const HuffLut *dcl = L.luts + F.lut[e.dc];
+        const HuffLut *acl = L.luts + F.lut[4 + e.ac];
+        const uint32_t mx = mcu % F.mcu_cols, my = mcu / F.mcu_cols;
+        const uint32_t gx = F.interleaved ? mx * C.h + e.bx : mx, gy = F.interleaved ? my * C.v + e.by : my;
+        const uint64_t blk = F.blk_off + C.blk_base + (uint64_t)gy * C.bw + gx;
+        const int32_t q0 = quant[C.q * 64];
+        uint16_t kind = kDiagNone;
+        uint32_t errpos = 0;
+        unsigned long long symstart = p0 + r.used;
+        int32_t dq = 0;
+        // DC (decoder.rs:501-515)
+        int sy = next_symbol(r, lim - r.used, dcl, L.symbols, k, at, val, err, eb);
+        if (sy == kSymError) {
+            kind = err;
+            errpos = eb;
+        } else {
+            long long pc = 0;
+#pragma unroll
+            for (int c = 0; c < 4; c++)
+                if (e.comp == (uint32_t)c) pc = pred[c];
+            const long long pn = pc + val;
+            if (pn > INT32_MAX || pn < INT32_MIN) {
+                kind = kJDcPredOverflow;
+                errpos = r.used;
+            } else {
+#pragma unroll
+                for (int c = 0; c < 4; c++)
+                    if (e.comp == (uint32_t)c) pred[c] = pn;
+                const long long d = pn * (long long)q0;
+                if (d > INT32_MAX || d < INT32_MIN) {
+                    kind = kJDcDeqOverflow;
+                    errpos = r.used;
+                }
+                dq = (int32_t)d;
+            }
+        }
+        // AC (decoder.rs:517-546)
+        while (kind == kDiagNone && k < 64) {
+            symstart = p0 + r.used;
+            sy = next_symbol(r, lim - r.used, acl, L.symbols, k, at, val, err, eb);
+            if (sy == kSymAc) stage[c_slice_zz[at]] = (int16_t)val;
+            else if (sy == kSymError) {
+                kind = err;
+                errpos = eb;
+            }
+        }
+        if (kind != kDiagNone) {
+            Diag d;
+            if (kind == kBarrierErr) {
+                d = (s.v.flags & 1) ? make_diag(kJMarkerInData, s.v.barrier, 0xd0 + rst[iv].number)
+                                    : make_diag(kJEndOfData, L.states[L.items[s.item].x].n_tokens);
+            } else {
+                d = make_diag(kind, s.v.start + (uint32_t)((p0 + errpos + 7) / 8));
+            }
+            report(L, s, slot, symstart, d, 0);
+            return;
+        }
+        int4 *dst = reinterpret_cast<int4 *>(L.coef + blk * 64);
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            dst[q] = stage4[q];
+            stage4[q] = make_int4(0, 0, 0, 0);
+        }
+        L.dc[blk] = dq;
+        if (b + 1 == B) {
+            const unsigned long long endbit = p0 + r.used;
+            report(L, s, slot, endbit, make_diag(kDiagNone, s.v.start + (uint32_t)((endbit + 7) / 8)), 1);
+            return;
+        }
+        k = 0;
+        si = si + 1 == sched_len ? 0 : si + 1;
+    }
+}
+
+// --------------------------------------------------------------- resolve ---
+
+__global__ void slice_resolve_kernel(JpegLaunch L) {
+    const uint32_t item = blockIdx.x * blockDim.x + threadIdx.x;
+    if (item >= L.n_items_small) return;
+    const IvInfo v = L.ivs[item];
+    if (v.n_slices == 0) return;
+    const uint2 it = L.items[item];
+    const JFrame &F = L.frames[it.x];
+    JState *st = L.states + it.x;
+    const uint32_t iv = it.y;
+    const unsigned long long key = L.iv_key[item];
+    Diag out = make_diag(kDiagNone);
+    if (key == ~0ull) {
+        out = make_diag(kDeviceError);  // every decoded interval ends in an event
+    } else {
+        const SliceEvent e = L.events[v.slot_first + (uint32_t)(key & ((1u << kKeyBits) - 1))];
+        if (!e.complete) {
+            out = e.diag;
+        } else if (iv + 1 < F.n_intervals) {
+            // consume_restart before the next interval (entropy.rs:111-134)
+            const uint32_t tend = e.diag.offset, expected = iv & 7, n_tok = st->n_tokens;
+            const RstEntry *rst = L.rsts + F.rst_off;
+            if ((v.flags & 1) && rst[iv].tok == tend) {
+                if (rst[iv].number != expected) out = make_diag(kJRstMismatch, tend, expected, 0xd0 + rst[iv].number);
+            } else if (tend < n_tok && F.tok[tend] == 0xff) {
+                out = make_diag(kJRstMismatch, tend, expected, 0x00);
+            } else {
+                out = make_diag(kJExpectRst, tend);
+            }
+        }
+    }
+    L.results[item] = out;
+    if (out.kind != kDiagNone) atomicMin(&st->bad_interval, iv);
+}
+
+}  // namespace
+
+int jpeg_slice_launches(const JpegLaunch &L) { return L.n_items_small ? 6 + kSyncPasses : 0; }
+
+void launch_jpeg_slices(const JpegLaunch &L, cudaStream_t s) {
+    if (!L.n_items_small || !L.n_slots) return;
+    const uint32_t warps_per_cta = 4;
+    slice_plan_kernel<<<(L.n_frames + warps_per_cta - 1) / warps_per_cta, 32 * warps_per_cta, 0, s>>>(L);
+    const uint32_t grid = (L.n_slots + kSliceThreads - 1) / kSliceThreads;
+    slice_spec_kernel<<<grid, kSliceThreads, 0, s>>>(L);
+    for (uint32_t p = 0; p < (uint32_t)kSyncPasses; p++) slice_sync_kernel<<<grid, kSliceThreads, 0, s>>>(L, p);
+    const uint32_t ivgrid = (L.n_items_small + warps_per_cta - 1) / warps_per_cta;
+    slice_fix_kernel<<<ivgrid, 32 * warps_per_cta, 0, s>>>(L);
+    slice_prefix_kernel<<<ivgrid, 32 * warps_per_cta, 0, s>>>(L);
+    slice_decode_kernel<<<grid, kSliceThreads, 0, s>>>(L);
+    slice_resolve_kernel<<<(L.n_items_small + 127) / 128, 128, 0, s>>>(L);
+}
+
+}  // namespace mmr

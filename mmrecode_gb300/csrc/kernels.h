@@ -21,6 +21,7 @@ struct JpegLaunch {
     const JSched *sched;
     const JComp *comps;
     const HuffLut *luts;
+    uint32_t n_luts;
     const uint8_t *symbols;
     const uint16_t *quant;       // natural order
     const uint2 *items;          // (frame, interval); frames with <= 4 components first
@@ -37,10 +38,26 @@ struct JpegLaunch {
     uint32_t *fix_count;         // zero-initialised per batch
     uint32_t fix_capacity;
     uint32_t fixup_grid;         // CTAs of the grid-stride fixup pass
+    // chunked entropy decoder (frames with <= 4 components; items [0, n_items_small))
+    uint32_t slice_bits;         // multiple of 32
+    uint32_t n_slots;
+    uint32_t *slot_item;         // per slot: item, UINT32_MAX when unused
+    IvInfo *ivs;                 // per item
+    SliceSync *sync;             // per slot
+    SliceSpec *spec;             // per slot
+    SlicePrefix *prefix;         // per slot
+    SliceEvent *events;          // per slot
+    unsigned long long *iv_key;  // per item: (position << 26 | slice) of its first event
+    uint32_t *sync_dirty;        // per sync pass: slices whose exit state changed (zeroed per batch)
 };
 
+constexpr int kSyncPasses = 2;
+constexpr uint32_t kSliceBitsDefault = 2048;
+
 void launch_jpeg_scan(const JpegLaunch &L, cudaStream_t s);
-void launch_jpeg_entropy(const JpegLaunch &L, cudaStream_t s);
+void launch_jpeg_entropy(const JpegLaunch &L, cudaStream_t s);   // frames with > 4 components
+void launch_jpeg_slices(const JpegLaunch &L, cudaStream_t s);    // frames with <= 4 components
+int jpeg_slice_launches(const JpegLaunch &L);
 void launch_jpeg_idct(const JpegLaunch &L, cudaStream_t s);
 
 struct DvLaunch {

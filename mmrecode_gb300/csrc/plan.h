@@ -13,10 +13,15 @@ namespace mmr {
 // code as the reference's length-by-length search.
 struct HuffLut {
     uint16_t fast[512];    // (length << 8) | symbol; 0 when the code is longer than 9 bits or absent
+    // Code and magnitude bits together within the next 9 bits, for symbols that decode
+    // without error (DC size <= 11; AC size 1..10): value << 16 | size << 12 | run << 8 |
+    // total bits; 0 otherwise (EOB, ZRL, invalid symbols and long codes take the slow path).
+    int32_t fastv[512];
     int32_t maxcode[18];   // largest code of each length 1..16, -1 if none
     int32_t valptr[18];    // symbol index of a length's first code, minus that code
     uint32_t sym_off;      // first symbol in the symbol pool
     uint32_t nsym;
+    uint32_t pad[2];       // size multiple of 16 (copied to shared memory with 16-byte loads)
 };
 
 // One frame component (SOF0 order).
@@ -59,6 +64,61 @@ struct JFrame {
     uint64_t blk_off;       // first block in the coefficient arena
     uint32_t n_blocks;
     uint32_t item;          // caller's batch item
+    uint32_t slot_first;    // first slice slot of the chunked entropy decoder
+    uint32_t slot_count;    // slots reserved: ceil(8 * in_len / slice_bits) + n_intervals
+};
+
+// --------------------------------------------- chunked entropy decoding ----
+//
+// A decoder state is packed as (bit position << 16) | (MCU block index << 8) | k,
+// the bit position counted from the interval's first entropy-coded token and k
+// the zigzag index of the next coefficient (0: the DC symbol comes next).
+
+// One restart interval (the whole scan without DRI) of a frame with <= 4 components.
+struct IvInfo {
+    uint32_t start;       // first token
+    uint32_t barrier;     // tokens before the RST marker (or the end of the scan) that ends it
+    uint32_t slot_first;  // first slice slot
+    uint32_t n_slices;    // 0: not decoded (header failure, or no RST precedes it)
+    uint32_t blocks;      // coefficient blocks in the interval
+    uint32_t flags;       // bit 0: the barrier is an RST marker
+};
+
+// Per slice: the state its decode starts from and what that decode produced.
+struct SliceSync {
+    unsigned long long start;  // start state (guess marker before the first sync pass)
+    unsigned long long exit;   // state at the first symbol boundary at or past the slice end
+    uint32_t blocks;           // blocks whose DC symbol starts in [start, exit)
+    int32_t dc[4];             // sum of their DC differences, per scan component
+    uint32_t pad;
+};
+
+// A point of the speculative decode: its state and the counts accumulated before it.
+struct SlicePoint {
+    unsigned long long state;
+    uint32_t blocks;
+    int32_t dc[4];
+    uint32_t pad;
+};
+
+constexpr int kSliceCheckpoints = 3;  // at 1/4, 1/2 and 3/4 of the slice
+
+struct SliceSpec {
+    SlicePoint exit;                      // end of the speculative decode
+    SlicePoint cp[kSliceCheckpoints];     // state at the first symbol boundary past each mark
+};
+
+// Block index and DC predictors at a slice's start (interval-relative).
+struct SlicePrefix {
+    uint32_t base;
+    uint32_t pad;
+    long long dc[4];
+};
+
+// The first event of a slice's final decode: an error, or the interval's last block done.
+struct SliceEvent {
+    Diag diag;          // error; for completion, offset = tokens consumed by the interval
+    uint32_t complete;
 };
 
 // Written by the kernels, copied back to the host.
