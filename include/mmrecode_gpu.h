@@ -97,6 +97,14 @@ MMR_API double mmr_gpu_last_batch_ms(const mmr_gpu_context *context);
 /* Kernel launches of the last batch. */
 MMR_API uint32_t mmr_gpu_last_batch_launches(const mmr_gpu_context *context);
 
+/*
+ * Bits per slice of the chunked entropy decoder for the following batches: each
+ * restart interval (the whole scan without DRI) is cut into slices of this many
+ * bits that decode in parallel. Accepted: multiples of 32 in 128..1048576; 0
+ * restores the context's automatic choice. Output never depends on it.
+ */
+MMR_API mmr_status mmr_gpu_set_slice_bits(mmr_gpu_context *context, uint32_t bits);
+
 /* Stage times of the last batch (CUDA events on the context stream) and its sizes. */
 typedef struct mmr_gpu_batch_stats {
     size_t struct_size;

@@ -248,6 +248,12 @@ class Context:
     def last_batch_launches(self) -> int:
         return _lib.load().mmr_gpu_last_batch_launches(self._h)
 
+    def set_slice_bits(self, bits: int) -> None:
+        """Bits per entropy-decoder slice for later batches (0: automatic). Output never depends on it."""
+        st = _lib.load().mmr_gpu_set_slice_bits(self._h, bits)
+        if st != STATUS_OK:
+            raise MmrError(st, _lib.last_error())
+
     def stats(self) -> dict:
         """Stage times (ms, CUDA events on the context stream) and sizes of the last batch."""
         s = _lib.BatchStats()

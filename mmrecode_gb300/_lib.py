@@ -104,6 +104,7 @@ SIGNATURES = {
     "mmr_gpu_decode_batch": ([ctypes.c_void_p, ctypes.POINTER(GpuItem), ctypes.c_size_t], ctypes.c_int32),
     "mmr_gpu_last_batch_ms": ([ctypes.c_void_p], ctypes.c_double),
     "mmr_gpu_last_batch_launches": ([ctypes.c_void_p], ctypes.c_uint32),
+    "mmr_gpu_set_slice_bits": ([ctypes.c_void_p, ctypes.c_uint32], ctypes.c_int32),
     "mmr_gpu_last_batch_stats": ([ctypes.c_void_p, ctypes.POINTER(BatchStats)], ctypes.c_int32),
     "mmr_mjpeg_encode_ex": ([ctypes.POINTER(VideoFrameView), ctypes.POINTER(JpegEncodeOptions), ctypes.POINTER(Buffer)],
                             ctypes.c_int32),

@@ -460,6 +460,12 @@ MMR_API uint32_t mmr_gpu_last_batch_launches(const mmr_gpu_context *context) {
     return context ? context->last_launches : 0;
 }
 
+MMR_API mmr_status mmr_gpu_set_slice_bits(mmr_gpu_context *context, uint32_t bits) {
+    if (!context) return invalid_argument("context is null");
+    if (!context->engine->set_slice_bits(bits)) return invalid_argument("slice bits must be 0 or a multiple of 32 in 128..1048576");
+    return finish(MMR_STATUS_OK, "");
+}
+
 MMR_API mmr_status mmr_gpu_last_batch_stats(const mmr_gpu_context *context, mmr_gpu_batch_stats *stats) {
     if (!context || !stats) return invalid_argument("context or stats is null");
     if (stats->struct_size != sizeof(mmr_gpu_batch_stats)) return invalid_argument("stats struct_size mismatch");

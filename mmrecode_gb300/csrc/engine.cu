@@ -656,7 +656,7 @@ struct Engine::Impl {
     cudaEvent_t ev[8] = {};
 };
 
-Engine::Engine(int device) : device_(device), slice_bits_(kSliceBitsDefault), impl_(new Impl) {
+Engine::Engine(int device) : device_(device), slice_bits_(0), impl_(new Impl) {
     MMR_CUDA(cudaSetDevice(device));
     MMR_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
     for (auto &e : impl_->ev) MMR_CUDA(cudaEventCreate(&e));
@@ -738,13 +738,13 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
         std::vector<JBlockRange> ranges;
         std::vector<RgbJob> rgbjobs;
         std::vector<uint64_t> rgbfirst(1, 0);
+        std::vector<uint32_t> rgbcta(1, 0);
         std::map<std::vector<uint8_t>, uint32_t> lut_index;
         std::vector<uint32_t> item_ok(n, 1);
         size_t in_bytes = 0, tok_bytes = 0, planes_bytes = 0, out_bytes = 0;
         uint32_t rst_total = 0;
         uint64_t blocks = 0;
         uint64_t n_slots = 0;
-        const uint32_t slice_bits = slice_bits_;
         std::vector<size_t> in_off(n, 0), out_off(n, 0), planes_off(n, SIZE_MAX);
         std::vector<std::array<size_t, 6>> plane_geom(n);  // (offset, bytes) of up to 3 planes
         // per JPEG plan: JFrame index (or -1)
@@ -837,6 +837,8 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
                 F.rst_off = rst_total;
                 rst_total += p.n_intervals;
                 if (p.ncomp <= 4) {
+                    const uint32_t slice_bits = slice_bits_ ? slice_bits_ : kSliceBitsDefault;
+                    F.slice_bits = slice_bits;
                     F.slot_first = (uint32_t)n_slots;
                     F.slot_count = (uint32_t)((8 * (uint64_t)it.len + slice_bits - 1) / slice_bits + p.n_intervals);
                     n_slots += F.slot_count;
@@ -880,6 +882,7 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
                     J.item = (uint32_t)i;
                     rgbjobs.push_back(J);
                     rgbfirst.push_back(rgbfirst.back() + (uint64_t)p.W * p.H);
+                    rgbcta.push_back(rgbcta.back() + rgb_ctas(p.W, p.H));
                 }
             }
             jframe_of[k] = (int)jframes.size();
@@ -958,6 +961,7 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
                 J.item = (uint32_t)i;
                 rgbjobs.push_back(J);
                 rgbfirst.push_back(rgbfirst.back() + (uint64_t)p.W * p.H);
+                rgbcta.push_back(rgbcta.back() + rgb_ctas(p.W, p.H));
             }
             dframes.push_back(F);
             DvState S;
@@ -1028,7 +1032,7 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
         size_t o_items = blob.add_vec(all_items), o_ranges = blob.add_vec(ranges), o_itemok = blob.add_vec(item_ok),
                o_dframes = blob.add_vec(dframes), o_dstates = blob.add_vec(dstates), o_segfirst = blob.add_vec(seg_first),
                o_diffirst = blob.add_vec(dif_first), o_rgbjobs = blob.add_vec(rgbjobs),
-               o_rgbfirst = blob.add_vec(rgbfirst);
+               o_rgbcta = blob.add_vec(rgbcta);
         uint32_t zero_counter = 0;
         size_t o_fixcount = blob.add(&zero_counter, 4);
         uint32_t zero_dirty[kSyncPasses] = {};
@@ -1081,7 +1085,6 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
         JL.fix_count = reinterpret_cast<uint32_t *>(db + o_fixcount);
         JL.fix_capacity = fix_capacity;
         JL.fixup_grid = 4 * 152;
-        JL.slice_bits = slice_bits;
         JL.n_slots = (uint32_t)n_slots;
         JL.slot_item = I.d_slot_item.as<uint32_t>();
         JL.ivs = I.d_ivs.as<IvInfo>();
@@ -1129,11 +1132,11 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
         MMR_CUDA(cudaEventRecord(I.ev[5], s));
         RgbLaunch RL;
         RL.jobs = reinterpret_cast<const RgbJob *>(db + o_rgbjobs);
-        RL.first = reinterpret_cast<const uint64_t *>(db + o_rgbfirst);
+        RL.cta_first = reinterpret_cast<const uint32_t *>(db + o_rgbcta);
         RL.n_jobs = (uint32_t)rgbjobs.size();
-        RL.n_pixels = rgbfirst.back();
+        RL.n_ctas = rgbcta.back();
         RL.item_ok = JL.item_ok;
-        if (RL.n_pixels) {
+        if (RL.n_ctas) {
             launch_rgb(RL, s);
             launches_ += 1;
         }

@@ -88,10 +88,11 @@ public:
     cudaStream_t stream() const { return stream_; }
     // Number of this engine's kernel launches in the last decode() call.
     uint32_t last_launches() const { return launches_; }
-    // Bits per slice of the chunked entropy decoder (a multiple of 32, >= 128).
+    // Bits per slice of the chunked entropy decoder (a multiple of 32 in
+    // 128..2^20); 0 selects the automatic per-frame choice.
     uint32_t slice_bits() const { return slice_bits_; }
     bool set_slice_bits(uint32_t bits) {
-        if (bits < 128 || bits % 32 || bits > (1u << 20)) return false;
+        if (bits != 0 && (bits < 128 || bits % 32 || bits > (1u << 20))) return false;
         slice_bits_ = bits;
         return true;
     }

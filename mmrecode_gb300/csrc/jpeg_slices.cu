@@ -263,7 +263,7 @@ __global__ void slice_plan_kernel(JpegLaunch L) {
     const uint32_t n_int = F.n_intervals;
     const uint32_t n_rst = min(st.n_rst, n_int), n_tok = st.n_tokens;
     const RstEntry *rst = L.rsts + F.rst_off;
-    const uint32_t S = L.slice_bits;
+    const uint32_t S = F.slice_bits;
     uint32_t used = 0;
     for (uint32_t c = 0; c < n_int; c += 32) {
         const uint32_t iv = c + lane;
@@ -333,7 +333,7 @@ __global__ void __launch_bounds__(kSliceThreads) slice_spec_kernel(JpegLaunch L)
         return;
     }
     const JFrame &F = *s.F;
-    const uint32_t S = L.slice_bits;
+    const uint32_t S = F.slice_bits;
     const unsigned long long p0 = (unsigned long long)s.j * S;
     const unsigned long long lbits = (unsigned long long)(s.v.barrier - s.v.start) * 8;
     const uint32_t lim = clamp_u32(lbits - p0);  // bits before the barrier, from p0
@@ -436,7 +436,7 @@ __device__ bool resync_slice(const JpegLaunch &L, uint32_t slot, const SliceRef 
         return old_exit != kStErr;
     }
     const JFrame &F = *s.F;
-    const uint32_t S = L.slice_bits;
+    const uint32_t S = F.slice_bits;
     const unsigned long long p0 = from >> 16;
     const unsigned long long nominal = (unsigned long long)s.j * S;
     const uint32_t rel = (uint32_t)(p0 - nominal);  // < one symbol: from is the first boundary past nominal

@@ -39,7 +39,6 @@ struct JpegLaunch {
     uint32_t fix_capacity;
     uint32_t fixup_grid;         // CTAs of the grid-stride fixup pass
     // chunked entropy decoder (frames with <= 4 components; items [0, n_items_small))
-    uint32_t slice_bits;         // multiple of 32
     uint32_t n_slots;
     uint32_t *slot_item;         // per slot: item, UINT32_MAX when unused
     IvInfo *ivs;                 // per item
@@ -82,12 +81,13 @@ void launch_dv_idct(const DvLaunch &L, cudaStream_t s);
 
 struct RgbLaunch {
     const RgbJob *jobs;
-    const uint64_t *first;  // n_jobs + 1 prefix of pixels
+    const uint32_t *cta_first;  // n_jobs + 1 prefix of CTAs (rgb_ctas per job)
     uint32_t n_jobs;
-    uint64_t n_pixels;
+    uint32_t n_ctas;
     const uint32_t *item_ok;
 };
 
+uint32_t rgb_ctas(uint32_t w, uint32_t h);
 void launch_rgb(const RgbLaunch &L, cudaStream_t s);
 
 // DV VLC lookup: level-1 indexed by the next 10 bits; long codes index a

@@ -66,6 +66,8 @@ struct JFrame {
     uint32_t item;          // caller's batch item
     uint32_t slot_first;    // first slice slot of the chunked entropy decoder
     uint32_t slot_count;    // slots reserved: ceil(8 * in_len / slice_bits) + n_intervals
+    uint32_t slice_bits;    // bits per slice (multiple of 32, >= 128)
+    uint32_t pad;
 };
 
 // --------------------------------------------- chunked entropy decoding ----

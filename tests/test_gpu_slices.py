@@ -1,0 +1,108 @@
+"""Chunked entropy decoder: output and diagnostics must not depend on the slice size.
+
+Every restart interval (the whole scan without DRI) decodes as fixed-size bit
+slices that synchronise with each other. These cases sweep the slice size from
+the smallest allowed (128 bits: most blocks straddle several slices) to larger
+than any interval (one slice, the serial decode), on valid streams and on
+corrupted restart-less streams whose first error lies deep inside a scan.
+"""
+
+import random
+
+import pytest
+
+import mmrecode_gb300 as m
+import oracle
+from mmrecode_gb300 import synth
+from helpers import assert_same_decode, frame_planes_gpu, prefixed
+
+pytestmark = pytest.mark.gpu
+
+SLICE_SIZES = (128, 160, 256, 992, 2048, 8192, 1 << 20)
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = m.Context()
+    yield c
+    c.set_slice_bits(0)
+    c.close()
+
+
+def check(ctx, packets, label, output=m.OUTPUT_PLANAR):
+    refs = [oracle.jpeg_decode(p) for p in packets]
+    for bits in SLICE_SIZES:
+        ctx.set_slice_bits(bits)
+        results = ctx.decode_batch(packets, m.CODEC_MJPEG, output)
+        for i, ((r, payload), ref) in enumerate(zip(results, refs)):
+            tag = f"{label}[{i}] slice_bits={bits}"
+            assert r.status == ref.status, f"{tag}: {r.status} {r.message} vs {ref.status} {ref.message}"
+            if ref.status:
+                assert r.message == prefixed(ref.status, ref.message), tag
+                continue
+            if output == m.OUTPUT_RGB24:
+                assert payload == oracle.rgb24(ref.frame), tag
+            else:
+                f = m.frame_from_batch(r, payload)
+                assert_same_decode(0, "", frame_planes_gpu(f), ref, tag)
+    ctx.set_slice_bits(0)
+
+
+def test_slice_bits_argument_checks(ctx):
+    for bad in (1, 96, 100, 130, (1 << 20) + 32):
+        with pytest.raises(m.MmrError) as e:
+            ctx.set_slice_bits(bad)
+        assert e.value.status == m.INVALID_ARGUMENT
+    ctx.set_slice_bits(0)
+
+
+def test_valid_streams_every_slice_size(ctx):
+    packets = (synth.mjpeg_stream(301, 2, 640, 480, "420", 75, 0) +
+               synth.mjpeg_stream(302, 2, 96, 64, "422", 80, 6) +
+               synth.mjpeg_stream(303, 2, 208, 112, "444", 60, 1) +
+               synth.mjpeg_stream(304, 1, 320, 240, "422", 95, 40))
+    check(ctx, packets, "valid")
+
+
+def test_dense_blocks_straddle_many_slices(ctx):
+    # quality 100 with noise: most coefficients are non-zero, a block spans
+    # several 128-bit slices
+    packets = synth.mjpeg_stream(305, 2, 128, 96, "444", 100, 0) + synth.mjpeg_stream(306, 1, 256, 64, "420", 100, 3)
+    check(ctx, packets, "dense", output=m.OUTPUT_RGB24)
+
+
+def test_corruption_deep_in_restartless_scans(ctx):
+    rnd = random.Random(307)
+    bases = synth.mjpeg_stream(308, 2, 320, 240, "420", 85, 0) + synth.mjpeg_stream(309, 1, 320, 240, "422", 70, 0)
+    packets = []
+    for k in range(36):
+        d = bytearray(bases[k % len(bases)])
+        ds = d.index(b"\xff\xda") + 2 + (d[d.index(b"\xff\xda") + 2] << 8 | d[d.index(b"\xff\xda") + 3])
+        kind = k % 4
+        p = rnd.randrange(ds + (len(d) - ds) // 4, len(d) - 2)
+        if kind == 0:
+            d[p] = rnd.randrange(256)
+        elif kind == 1:
+            d = d[:p]
+        elif kind == 2:
+            del d[p:p + rnd.randint(1, 5)]
+        else:
+            d[p:p] = bytes([rnd.randrange(256) for _ in range(rnd.randint(1, 3))])
+        packets.append(bytes(d))
+    check(ctx, packets, "corrupt")
+
+
+def test_corruption_at_slice_boundaries(ctx):
+    base = synth.mjpeg_stream(310, 1, 160, 128, "420", 90, 0)[0]
+    sos = base.index(b"\xff\xda")
+    ds = sos + 2 + (base[sos + 2] << 8 | base[sos + 3])
+    packets = []
+    for off in (16, 32, 64, 127, 128, 129, 256, 1024):
+        for val in (0x00, 0xFF, 0x5A):
+            p = ds + off
+            if p >= len(base) - 2:
+                continue
+            d = bytearray(base)
+            d[p] = val
+            packets.append(bytes(d))
+    check(ctx, packets, "boundary")
