@@ -736,6 +736,7 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
         std::vector<uint16_t> quant;
         std::vector<uint2> items_small, items_big;
         std::vector<JBlockRange> ranges;
+        std::vector<uint32_t> idct_cta(1, 0);
         std::vector<RgbJob> rgbjobs;
         std::vector<uint64_t> rgbfirst(1, 0);
         std::vector<uint32_t> rgbcta(1, 0);
@@ -850,7 +851,10 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
                     r.first = blocks + p.comps[c].blk_base;
                     r.frame = (uint32_t)jframes.size();
                     r.comp = c;
-                    if (p.comps[c].bw * p.comps[c].bh) ranges.push_back(r);
+                    if (p.comps[c].bw * p.comps[c].bh) {
+                        ranges.push_back(r);
+                        idct_cta.push_back(idct_cta.back() + idct_ctas(p.comps[c].bw * p.comps[c].bh));
+                    }
                 }
                 blocks += p.n_blocks;
                 // planes: straight into a device output, else scratch
@@ -989,8 +993,7 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
         I.d_segerr.ensure(std::max<size_t>(seg_first.back(), 256));
         // samples the fp32 IDCT leaves to the exact pass: expected ~0.1 per block; when the
         // queue fills, the kernel recomputes in place instead
-        uint32_t fix_capacity = (uint32_t)std::min<uint64_t>(blocks / 2 + 65536, 0x7fffffffu);
-        I.d_fix.ensure((size_t)fix_capacity * 8);
+        I.d_fix.ensure(std::max<size_t>(blocks * 16, 256));
         if (n_slots > 0xffffffffull) throw std::runtime_error("batch too large for the chunked entropy decoder");
         I.d_slot_item.ensure(std::max<size_t>(n_slots * 4, 256));
         I.d_sync.ensure(std::max<size_t>(n_slots * sizeof(SliceSync), 256));
@@ -1029,12 +1032,12 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
                o_luts = blob.add_vec(luts), o_symbols = blob.add_vec(symbols), o_quant = blob.add_vec(quant);
         std::vector<uint2> all_items(items_small);
         all_items.insert(all_items.end(), items_big.begin(), items_big.end());
-        size_t o_items = blob.add_vec(all_items), o_ranges = blob.add_vec(ranges), o_itemok = blob.add_vec(item_ok),
+        size_t o_items = blob.add_vec(all_items), o_ranges = blob.add_vec(ranges), o_idctcta = blob.add_vec(idct_cta), o_itemok = blob.add_vec(item_ok),
                o_dframes = blob.add_vec(dframes), o_dstates = blob.add_vec(dstates), o_segfirst = blob.add_vec(seg_first),
                o_diffirst = blob.add_vec(dif_first), o_rgbjobs = blob.add_vec(rgbjobs),
                o_rgbcta = blob.add_vec(rgbcta);
-        uint32_t zero_counter = 0;
-        size_t o_fixcount = blob.add(&zero_counter, 4);
+        uint32_t zero_counters[2] = {0, 0};
+        size_t o_fixcount = blob.add(zero_counters, 8);
         uint32_t zero_dirty[kSyncPasses] = {};
         size_t o_dirty = blob.add(zero_dirty, sizeof(zero_dirty));
         size_t blob_size = std::max<size_t>(blob.bytes.size(), 256);
@@ -1079,11 +1082,12 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
         JL.dc = I.d_dc.as<int32_t>();
         JL.ranges = reinterpret_cast<const JBlockRange *>(db + o_ranges);
         JL.n_ranges = (uint32_t)ranges.size();
+        JL.idct_cta_first = reinterpret_cast<const uint32_t *>(db + o_idctcta);
+        JL.n_idct_ctas = idct_cta.back();
         JL.n_blocks = blocks;
         JL.item_ok = reinterpret_cast<uint32_t *>(db + o_itemok);
-        JL.fix = I.d_fix.as<unsigned long long>();
+        JL.fix = I.d_fix.as<ulonglong2>();
         JL.fix_count = reinterpret_cast<uint32_t *>(db + o_fixcount);
-        JL.fix_capacity = fix_capacity;
         JL.fixup_grid = 4 * 152;
         JL.n_slots = (uint32_t)n_slots;
         JL.slot_item = I.d_slot_item.as<uint32_t>();
@@ -1154,7 +1158,7 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
         if (back_d) MMR_CUDA(cudaMemcpyAsync(hb + o_b2, db + o_dstates, back_d, cudaMemcpyDeviceToHost, s));
         if (back_ok) MMR_CUDA(cudaMemcpyAsync(hb + o_b3, db + o_itemok, back_ok, cudaMemcpyDeviceToHost, s));
         if (back_seg) MMR_CUDA(cudaMemcpyAsync(hb + o_b4, I.d_segerr.ptr, back_seg, cudaMemcpyDeviceToHost, s));
-        MMR_CUDA(cudaMemcpyAsync(hb + o_b5, db + o_fixcount, 4, cudaMemcpyDeviceToHost, s));
+        MMR_CUDA(cudaMemcpyAsync(hb + o_b5, db + o_fixcount + 4, 4, cudaMemcpyDeviceToHost, s));
         for (size_t i = 0; i < n; i++) {
             Item &it = items[i];
             if (it.status != kOk || it.out_on_device || !it.out_bytes) continue;

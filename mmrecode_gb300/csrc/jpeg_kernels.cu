@@ -591,7 +591,10 @@ __device__ __forceinline__ uint8_t exact_sample(const int32_t *c, int stride, in
     return (uint8_t)fmin(fmax(px, 0.0), 255.0);
 }
 
-constexpr int kIdctBlocks = 32;  // blocks per CTA, 8 threads (one column each) per block
+constexpr int kIdctBlocks = 64;  // blocks per CTA, all of one (frame, component) range
+constexpr int kIdctThreads = kIdctBlocks * 4;
+constexpr int kIdctStride = 68;     // floats per staged block: 16-byte rows, 8 blocks on distinct banks
+constexpr int kIdctOutStride = 72;  // output bytes per staged block: 8-byte rows, 8 blocks on distinct banks
 
 __device__ __forceinline__ uint32_t find_range(const JpegLaunch &L, uint64_t g) {
     uint32_t lo = 0, hi = L.n_ranges;
@@ -603,93 +606,194 @@ __device__ __forceinline__ uint32_t find_range(const JpegLaunch &L, uint64_t g) 
     return lo;
 }
 
-__global__ void __launch_bounds__(kIdctBlocks * 8) idct_kernel(JpegLaunch L) {
-    __shared__ int32_t s_c[kIdctBlocks][65];
-    __shared__ float s_f[kIdctBlocks][65];
-    int lb = threadIdx.x >> 3, x = threadIdx.x & 7;
-    uint64_t g = (uint64_t)blockIdx.x * kIdctBlocks + lb;
-    bool valid = g < L.n_blocks;
-    uint32_t r = 0;
-    const JFrame *F = nullptr;
-    const JComp *C = nullptr;
-    if (valid) {
-        r = find_range(L, g);
-        F = &L.frames[L.ranges[r].frame];
-        C = &L.comps[F->comp_off + L.ranges[r].comp];
-        valid = L.item_ok[F->item] != 0;
-    }
-    uint64_t l1 = 0;  // sum |c| over this thread's row
-    if (valid) {
-        const uint16_t *Q = L.quant + F->quant_off + C->q * 64;
-        int4 v = reinterpret_cast<const int4 *>(L.coef + g * 64)[x];
+// Dequantises block g into fp32 rows q and q+4 of `blk` (the product of an
+// int16 level and an 8-bit quantiser is exact in fp32; the DC is the decoder's
+// dequantised int32, rounded to fp32 like every c in the bound). Returns the
+// sum of |c| over the two rows.
+__device__ __forceinline__ float stage_rows(const JpegLaunch &L, uint64_t g, uint32_t q, const float *Qf, float *blk) {
+    const int4 *src = reinterpret_cast<const int4 *>(L.coef + g * 64);
+    float l1 = 0.0f;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const int row = q + 4 * h;
+        const int4 v = src[row];
         const int16_t *lv = reinterpret_cast<const int16_t *>(&v);
+        const float4 qa = reinterpret_cast<const float4 *>(Qf + row * 8)[0];
+        const float4 qb = reinterpret_cast<const float4 *>(Qf + row * 8)[1];
+        const float qv[8] = {qa.x, qa.y, qa.z, qa.w, qb.x, qb.y, qb.z, qb.w};
+        float f[8];
 #pragma unroll
-        for (int j = 0; j < 8; j++) {
-            int32_t c = (j == 0 && x == 0) ? L.dc[g] : (int32_t)lv[j] * (int32_t)Q[x * 8 + j];
-            s_c[lb][x * 8 + j] = c;
-            s_f[lb][x * 8 + j] = (float)c;
-            l1 += (uint64_t)(c < 0 ? -(int64_t)c : (int64_t)c);
-        }
+        for (int j = 0; j < 8; j++) f[j] = (float)lv[j] * qv[j];
+        if (row == 0) f[0] = (float)L.dc[g];
+#pragma unroll
+        for (int j = 0; j < 8; j++) l1 += fabsf(f[j]);
+        reinterpret_cast<float4 *>(blk + row * 8)[0] = make_float4(f[0], f[1], f[2], f[3]);
+        reinterpret_cast<float4 *>(blk + row * 8)[1] = make_float4(f[4], f[5], f[6], f[7]);
     }
-    // C1 over the block's 8 threads (lanes 8k..8k+7 of the warp)
+    return l1;
+}
+
+// Sample of an fp32 transform value. Rounding it provably equals rounding the
+// binary64 value when no half-integer lies within delta of acc, i.e. when acc
+// is closer than 0.5 - delta to its nearest integer (with delta >= 0.5 nothing
+// is certain); the exact pass settles the rest, ties included, so rintf's
+// ties-to-even never decides a sample. Clamping after an agreed rounding agrees.
+__device__ __forceinline__ uint32_t round_sample(float acc, float near, bool &unsure) {
+    const float r = rintf(acc);
+    unsure = !(fabsf(acc - r) < near);
+    return (uint32_t)fminf(fmaxf(r + 128.0f, 0.0f), 255.0f);
+}
+
+// Transform of one staged block by its four threads; thread q produces output
+// columns q and 7 - q into out[row * stride + col]. Both passes use the even/odd
+// split of the basis: M[7-x][u] = (-1)^u M[x][u] holds for the fp32 roundings of
+// the reference's literals (the literals themselves differ from exact symmetry by
+// < 2e-15, far inside the fp32 rounding), so
+//   s[x] = E + O, s[7-x] = E - O,  E = sum_{u even} M[x][u] c[u], O = sum_{u odd}.
+// Per output this is 4 FMAs per half and one add: each pass's error is <= 5u of
+// the sum of |terms|, plus u for each rounded M and c, <= 13u B after both
+// passes, inside the 19u B the decision bound allows. |s| <= Mmax^2 C1 < C1/4, so
+// the relative term 2^-40 |s| of the bound is folded into 2^-42 C1.
+// Returns the samples left to the exact pass as bits (row * 8 + column).
+__device__ __forceinline__ unsigned long long idct_block(const float *blk, uint32_t q, float c1, uint8_t *out,
+                                                         int stride) {
+    float mq[8];
 #pragma unroll
-    for (int o = 1; o < 8; o <<= 1) l1 += __shfl_xor_sync(0xffffffffu, l1, o);
-    __syncthreads();
-    if (!valid) return;
-    float mrow[8];
-#pragma unroll
-    for (int u = 0; u < 8; u++) mrow[u] = c_idct32[x * 8 + u];
-    float t[8];
+    for (int u = 0; u < 8; u++) mq[u] = c_idct32[q * 8 + u];
+    float ta[8], tb[8];
 #pragma unroll
     for (int v = 0; v < 8; v++) {
-        float acc = 0.0f;
-#pragma unroll
-        for (int u = 0; u < 8; u++) acc = fmaf(mrow[u], s_f[lb][v * 8 + u], acc);
-        t[v] = acc;
+        const float4 c0 = reinterpret_cast<const float4 *>(blk + v * 8)[0];
+        const float4 c1v = reinterpret_cast<const float4 *>(blk + v * 8)[1];
+        float e = c0.x * mq[0];
+        e = fmaf(mq[2], c0.z, e);
+        e = fmaf(mq[4], c1v.x, e);
+        e = fmaf(mq[6], c1v.z, e);
+        float o = c0.y * mq[1];
+        o = fmaf(mq[3], c0.w, o);
+        o = fmaf(mq[5], c1v.y, o);
+        o = fmaf(mq[7], c1v.w, o);
+        ta[v] = e + o;
+        tb[v] = e - o;
     }
-    const float delta_base = (float)l1 * 0x1p-21f + 0x1p-30f;
-    uint64_t local = g - L.ranges[r].first;
-    uint32_t gx = (uint32_t)(local % C->bw), gy = (uint32_t)(local / C->bw);
-    uint32_t col = gx * 8 + x;
-    uint8_t *plane = F->planes + C->out_off;
+    // 2^-21 C1 >= 19u Mmax^2 C1 with a 1.75x margin
+    const float near = 0.5f - (c1 * (0x1p-21f + 0x1p-42f) + 0x1p-30f);
+    uint32_t bits = 0;  // bit 2*row (column q), 2*row+1 (column 7-q)
 #pragma unroll
-    for (int y = 0; y < 8; y++) {
-        float acc = 0.0f;
+    for (int y = 0; y < 4; y++) {
 #pragma unroll
-        for (int v = 0; v < 8; v++) acc = fmaf(c_idct32[y * 8 + v], t[v], acc);
-        uint32_t row = gy * 8 + y;
-        if (row >= C->plane_h || col >= C->plane_w) continue;
-        float delta = delta_base + fabsf(acc) * 0x1p-40f;
-        int out;
-        bool certain = true;
-        if (acc + delta < 0.5f - 128.0f) out = 0;
-        else if (acc - delta > 254.5f - 128.0f) out = 255;
-        else {
-            float fl = floorf(acc);
-            float fr = acc - fl;  // exact for |acc| < 2^23
-            certain = fabsf(fr - 0.5f) > delta && delta < 0.25f;
-            int rr = (int)fl + (fr > 0.5f ? 1 : 0) + 128;
-            out = rr < 0 ? 0 : rr > 255 ? 255 : rr;
+        for (int side = 0; side < 2; side++) {
+            const float *t = side ? tb : ta;
+            float e = t[0] * c_idct32[y * 8 + 0];
+            e = fmaf(c_idct32[y * 8 + 2], t[2], e);
+            e = fmaf(c_idct32[y * 8 + 4], t[4], e);
+            e = fmaf(c_idct32[y * 8 + 6], t[6], e);
+            float o = t[1] * c_idct32[y * 8 + 1];
+            o = fmaf(c_idct32[y * 8 + 3], t[3], o);
+            o = fmaf(c_idct32[y * 8 + 5], t[5], o);
+            o = fmaf(c_idct32[y * 8 + 7], t[7], o);
+            const uint32_t col = side ? 7 - q : q;
+            bool u0, u1;
+            out[y * stride + col] = (uint8_t)round_sample(e + o, near, u0);
+            out[(7 - y) * stride + col] = (uint8_t)round_sample(e - o, near, u1);
+            bits |= (u0 ? 1u : 0u) << (2 * y + side);
+            bits |= (u1 ? 1u : 0u) << (2 * (7 - y) + side);
         }
-        uint64_t dst = (uint64_t)row * C->plane_w + col;
-        if (certain) {
-            plane[dst] = (uint8_t)out;
-            continue;
+    }
+    unsigned long long mask = 0;
+    if (bits) {
+#pragma unroll
+        for (int row = 0; row < 8; row++) {
+            if (bits & (1u << (2 * row))) mask |= 1ull << (row * 8 + q);
+            if (bits & (2u << (2 * row))) mask |= 1ull << (row * 8 + 7 - q);
         }
-        uint32_t slot = atomicAdd(L.fix_count, 1u);
-        if (slot < L.fix_capacity) L.fix[slot] = (g << 6) | (uint64_t)(y * 8 + x);
-        else plane[dst] = exact_sample(&s_c[lb][0], 8, y, x);  // queue full: exact in place
+    }
+    return mask;
+}
+
+// Planar output: a CTA transforms 64 blocks of one (frame, component) range, four
+// threads per block, and writes each block row as one 8-byte store.
+__global__ void __launch_bounds__(kIdctThreads, 4) idct_kernel(JpegLaunch L) {
+    __shared__ __align__(16) float s_f[kIdctBlocks * kIdctStride];
+    __shared__ __align__(16) uint8_t s_o[kIdctBlocks * kIdctOutStride];
+    __shared__ __align__(16) float s_q[64];
+    __shared__ uint32_t s_range;
+    if (threadIdx.x == 0) {
+        uint32_t lo = 0, hi = L.n_ranges;
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (L.idct_cta_first[mid] <= blockIdx.x) lo = mid;
+            else hi = mid;
+        }
+        s_range = lo;
+    }
+    __syncthreads();
+    const uint32_t r = s_range;
+    const JBlockRange R = L.ranges[r];
+    const JFrame &F = L.frames[R.frame];
+    if (!L.item_ok[F.item]) return;
+    const JComp &C = L.comps[F.comp_off + R.comp];
+    if (threadIdx.x < 64) s_q[threadIdx.x] = (float)L.quant[F.quant_off + C.q * 64 + threadIdx.x];
+    __syncthreads();
+    const uint32_t nblk = C.bw * C.bh;
+    const uint32_t lb = threadIdx.x >> 2, q = threadIdx.x & 3;
+    const uint32_t local = (blockIdx.x - L.idct_cta_first[r]) * kIdctBlocks + lb;
+    const bool valid = local < nblk;
+    const uint64_t g = R.first + local;
+    float *blk = s_f + lb * kIdctStride;
+    float l1 = valid ? stage_rows(L, g, q, s_q, blk) : 0.0f;
+#pragma unroll
+    for (int o = 1; o < 4; o <<= 1) l1 += __shfl_xor_sync(0xffffffffu, l1, o);
+    __syncwarp();
+    const uint32_t gx = local % C.bw, gy = local / C.bw;
+    unsigned long long mask = 0;
+    if (valid) {
+        mask = idct_block(blk, q, l1, s_o + lb * kIdctOutStride, 8);
+    }
+    if (mask) {
+        // only samples inside the plane are written, and only those go to the exact pass
+        const uint32_t vis_w = gx * 8 >= C.plane_w ? 0 : min(8u, C.plane_w - gx * 8);
+        const uint32_t vis_h = gy * 8 >= C.plane_h ? 0 : min(8u, C.plane_h - gy * 8);
+        const unsigned long long colm = 0x0101010101010101ull * ((1u << vis_w) - 1u);
+        const unsigned long long rowm = vis_h >= 8 ? ~0ull : ((1ull << (8 * vis_h)) - 1ull);
+        mask &= colm & rowm;
+    }
+#pragma unroll
+    for (int o = 1; o < 4; o <<= 1) mask |= __shfl_xor_sync(0xffffffffu, mask, o);
+    if (q == 0 && mask) {  // one entry per block: the queue holds n_blocks entries
+        const uint32_t slot = atomicAdd(L.fix_count, 1u);
+        L.fix[slot] = make_ulonglong2(g, mask);
+        atomicAdd(L.fix_count + 1, (uint32_t)__popcll(mask));
+    }
+    __syncwarp();
+    if (!valid) return;
+    // rows 2q and 2q+1 of the block, 8 bytes each, clipped to the plane (blocks of
+    // the MCU padding may lie wholly outside it)
+    uint8_t *plane = F.planes + C.out_off;
+    const uint32_t col0 = gx * 8;
+    if (col0 >= C.plane_w) return;
+    const uint32_t ncol = min(8u, C.plane_w - col0);
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const uint32_t row = 2 * q + h, prow = gy * 8 + row;
+        if (prow >= C.plane_h) continue;
+        uint8_t *dst = plane + (uint64_t)prow * C.plane_w + col0;
+        const uint8_t *srow = s_o + lb * kIdctOutStride + row * 8;
+        if (ncol == 8 && (((uintptr_t)dst) & 7) == 0) {
+            *reinterpret_cast<uint2 *>(dst) = *reinterpret_cast<const uint2 *>(srow);
+        } else {
+            for (uint32_t c = 0; c < ncol; c++) dst[c] = srow[c];
+        }
     }
 }
 
 // Exact reference-order recomputation of the queued samples.
 __global__ void __launch_bounds__(256) idct_fixup_kernel(JpegLaunch L) {
-    uint32_t n = min(*L.fix_count, L.fix_capacity);
+    const uint32_t n = *L.fix_count;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        unsigned long long e = L.fix[i];
-        uint64_t g = e >> 6;
-        int y = (int)(e >> 3) & 7, x = (int)e & 7;
-        uint32_t r = find_range(L, g);
+        const ulonglong2 e = L.fix[i];
+        const uint64_t g = e.x;
+        const uint32_t r = find_range(L, g);
         const JFrame *F = &L.frames[L.ranges[r].frame];
         const JComp *C = &L.comps[F->comp_off + L.ranges[r].comp];
         const uint16_t *Q = L.quant + F->quant_off + C->q * 64;
@@ -703,9 +807,13 @@ __global__ void __launch_bounds__(256) idct_fixup_kernel(JpegLaunch L) {
             for (int j = 0; j < 8; j++) c[k * 8 + j] = (int32_t)lv[j] * (int32_t)Q[k * 8 + j];
         }
         c[0] = L.dc[g];
-        uint64_t local = g - L.ranges[r].first;
-        uint32_t gx = (uint32_t)(local % C->bw), gy = (uint32_t)(local / C->bw);
-        F->planes[C->out_off + (uint64_t)(gy * 8 + y) * C->plane_w + gx * 8 + x] = exact_sample(c, 8, y, x);
+        const uint32_t local = (uint32_t)(g - L.ranges[r].first);
+        const uint32_t gx = local % C->bw, gy = local / C->bw;
+        uint8_t *plane = F->planes + C->out_off;
+        for (unsigned long long m = e.y; m; m &= m - 1) {
+            const int b = __ffsll((long long)m) - 1, y = b >> 3, x = b & 7;
+            plane[(uint64_t)(gy * 8 + y) * C->plane_w + gx * 8 + x] = exact_sample(c, 8, y, x);
+        }
     }
 }
 
@@ -726,10 +834,11 @@ void launch_jpeg_entropy(const JpegLaunch &L, cudaStream_t s) {
     if (L.n_frames) resolve_kernel<<<(L.n_frames + 127) / 128, 128, 0, s>>>(L);
 }
 
+uint32_t idct_ctas(uint32_t blocks) { return (blocks + kIdctBlocks - 1) / kIdctBlocks; }
+
 void launch_jpeg_idct(const JpegLaunch &L, cudaStream_t s) {
-    if (L.n_blocks == 0) return;
-    uint64_t grid = (L.n_blocks + kIdctBlocks - 1) / kIdctBlocks;
-    idct_kernel<<<(unsigned)grid, kIdctBlocks * 8, 0, s>>>(L);
+    if (L.n_blocks == 0 || L.n_idct_ctas == 0) return;
+    idct_kernel<<<L.n_idct_ctas, kIdctThreads, 0, s>>>(L);
     idct_fixup_kernel<<<L.fixup_grid, 256, 0, s>>>(L);
 }
 

@@ -32,11 +32,12 @@ struct JpegLaunch {
     int32_t *dc;                 // dequantised DC per block
     const JBlockRange *ranges;
     uint32_t n_ranges;
+    const uint32_t *idct_cta_first;  // n_ranges + 1 prefix of transform CTAs (idct_ctas per range)
+    uint32_t n_idct_ctas;
     uint64_t n_blocks;
     uint32_t *item_ok;           // per batch item: 1 while decoding has not failed
-    unsigned long long *fix;     // samples the fp32 IDCT could not decide: (block << 6) | (y*8+x)
-    uint32_t *fix_count;         // zero-initialised per batch
-    uint32_t fix_capacity;
+    ulonglong2 *fix;             // blocks the fp32 IDCT could not fully decide: (block, sample mask)
+    uint32_t *fix_count;         // entries, then samples; zero-initialised per batch
     uint32_t fixup_grid;         // CTAs of the grid-stride fixup pass
     // chunked entropy decoder (frames with <= 4 components; items [0, n_items_small))
     uint32_t n_slots;
@@ -58,6 +59,7 @@ void launch_jpeg_entropy(const JpegLaunch &L, cudaStream_t s);   // frames with 
 void launch_jpeg_slices(const JpegLaunch &L, cudaStream_t s);    // frames with <= 4 components
 int jpeg_slice_launches(const JpegLaunch &L);
 void launch_jpeg_idct(const JpegLaunch &L, cudaStream_t s);
+uint32_t idct_ctas(uint32_t blocks);
 
 struct DvLaunch {
     const DvFrame *frames;
