@@ -301,6 +301,7 @@ void build_lut(const uint8_t *key, size_t key_len, uint32_t sym_off, bool ac, Hu
     for (int l = 0; l < 18; l++) lut->maxcode[l] = -1;
     const uint8_t *counts = key;
     const uint8_t *symbols = key + 16;
+    constexpr uint32_t FB = kHuffFastBits;
     uint32_t code = 0, k = 0;
     for (int l = 1; l <= 16; l++) {
         uint32_t n = counts[l - 1];
@@ -309,21 +310,38 @@ void build_lut(const uint8_t *key, size_t key_len, uint32_t sym_off, bool ac, Hu
             lut->maxcode[l] = (int32_t)(code + n - 1);
         }
         for (uint32_t i = 0; i < n; i++) {
+            const uint8_t sym = symbols[k];
             if (l <= 9) {
                 uint32_t first = code << (9 - l), cnt = 1u << (9 - l);
-                uint8_t sym = symbols[k];
-                uint32_t run = ac ? sym >> 4 : 0, size = ac ? sym & 15 : sym;
-                bool fast_ok = ac ? (size >= 1 && size <= 10) : (size >= 1 && size <= 11);
-                for (uint32_t j = 0; j < cnt; j++) {
-                    // the first code symbol of each 9-bit pattern wins (codes are prefix-free)
-                    if (lut->fast[first + j]) continue;
-                    lut->fast[first + j] = (uint16_t)((l << 8) | sym);
-                    if (fast_ok && l + size <= 9) {
-                        uint32_t bits = (first + j) & ((1u << (9 - l)) - 1);  // the bits after the code
-                        int32_t v = (int32_t)(bits >> (9 - l - size));
-                        if (v < (1 << (size - 1))) v += 1 - (1 << size);  // receive_extend
-                        lut->fastv[first + j] =
-                            (int32_t)((uint32_t)v << 16) | (int32_t)((size << 12) | (run << 8) | (l + size));
+                for (uint32_t j = 0; j < cnt; j++)  // the first code of each 9-bit pattern wins
+                    if (!lut->fast[first + j]) lut->fast[first + j] = (uint16_t)((l << 8) | sym);
+            }
+            if ((uint32_t)l <= FB) {
+                uint32_t run = 0, size = 0, kind = kFastCoef;
+                bool ok;
+                if (ac) {
+                    run = sym >> 4;
+                    size = sym & 15;
+                    if (sym == 0x00) kind = kFastEob, ok = true;
+                    else if (sym == 0xf0) kind = kFastZrl, ok = true;
+                    else ok = size >= 1 && size <= 10;
+                } else {
+                    size = sym;
+                    ok = size <= 11;
+                }
+                if (kind != kFastCoef) size = 0;
+                if (ok && l + size <= FB) {
+                    const uint32_t rest = FB - l - size;  // bits after the magnitude
+                    for (uint32_t m = 0; m < (1u << size); m++) {
+                        int32_t v = 0;
+                        if (size) {
+                            v = (int32_t)m;
+                            if (v < (1 << (size - 1))) v += 1 - (1 << size);  // receive_extend
+                        }
+                        const uint32_t e = ((uint32_t)v << 16) | (kind << 13) | (size << 9) | (run << 5) | (l + size);
+                        const uint32_t base = (code << (FB - l)) | (m << rest);
+                        for (uint32_t j = 0; j < (1u << rest); j++)
+                            if (!lut->fastv[base + j]) lut->fastv[base + j] = e;
                     }
                 }
             }
@@ -730,6 +748,7 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
         std::vector<JState> jstates;
         std::vector<uint32_t> tile_first(1, 0);
         std::vector<JSched> sched;
+        std::vector<JBlockRec> brecs;
         std::vector<JComp> comps;
         std::vector<HuffLut> luts;
         std::vector<uint8_t> symbols;
@@ -834,6 +853,25 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
                         luts.push_back(L);
                     }
                     F.lut[s] = f->second;
+                }
+                for (const JSched &e : p.sched) {
+                    const JComp &C = p.comps[e.comp];
+                    JBlockRec R;
+                    memset(&R, 0, sizeof(R));
+                    R.dc_lut = F.lut[e.dc];
+                    R.ac_lut = F.lut[4 + e.ac];
+                    R.comp = e.comp;
+                    R.q0 = p.quant[C.q][0];
+                    if (p.interleaved) {
+                        R.base_off = C.blk_base + (uint32_t)e.by * C.bw + e.bx;
+                        R.mul_x = C.h;
+                        R.mul_y = C.v * C.bw;
+                    } else {
+                        R.base_off = C.blk_base;
+                        R.mul_x = 1;
+                        R.mul_y = C.bw;
+                    }
+                    brecs.push_back(R);
                 }
                 F.rst_off = rst_total;
                 rst_total += p.n_intervals;
@@ -1028,7 +1066,7 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
 
         // ------------------------------------------------------ plan blob
         size_t o_jframes = blob.add_vec(jframes), o_jstates = blob.add_vec(jstates),
-               o_tile_first = blob.add_vec(tile_first), o_sched = blob.add_vec(sched), o_comps = blob.add_vec(comps),
+               o_tile_first = blob.add_vec(tile_first), o_sched = blob.add_vec(sched), o_brec = blob.add_vec(brecs), o_comps = blob.add_vec(comps),
                o_luts = blob.add_vec(luts), o_symbols = blob.add_vec(symbols), o_quant = blob.add_vec(quant);
         std::vector<uint2> all_items(items_small);
         all_items.insert(all_items.end(), items_big.begin(), items_big.end());
@@ -1069,6 +1107,7 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
         JL.tile_rst = I.d_tile_rst.as<uint32_t>();
         JL.rsts = I.d_rsts.as<RstEntry>();
         JL.sched = reinterpret_cast<const JSched *>(db + o_sched);
+        JL.brec = reinterpret_cast<const JBlockRec *>(db + o_brec);
         JL.comps = reinterpret_cast<const JComp *>(db + o_comps);
         JL.luts = reinterpret_cast<const HuffLut *>(db + o_luts);
         JL.n_luts = (uint32_t)luts.size();

@@ -1,0 +1,186 @@
+// Baseline JPEG Huffman symbol decoding shared by the entropy kernels.
+//
+// Bits come from the unstuffed token stream as big-endian 32-bit words. A
+// reader may hold bits past its interval's barrier, so every use of bits is
+// checked against the count before the barrier (`avail`), which is exactly
+// where the reference reader (crates/codecs/mjpeg/src/entropy.rs:74-166) would
+// meet the next marker or the end of the data.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "plan.h"
+
+namespace mmr {
+
+__device__ __forceinline__ uint32_t bswap32(uint32_t x) { return __byte_perm(x, 0, 0x0123); }
+
+struct Bits {
+    const uint32_t *words;
+    uint32_t wpos;  // next word to load
+    int nbits;      // bits held in buf (>= 32 after refill)
+    uint64_t buf;   // next bits, MSB first
+    uint32_t used;  // bits consumed, counted from the reader's base position
+};
+
+// Reader at token-stream bit `bit`; `used` is the base-relative position there.
+__device__ __forceinline__ void bits_init(Bits &r, const uint8_t *tok, unsigned long long bit, uint32_t used) {
+    r.words = reinterpret_cast<const uint32_t *>(tok);
+    const uint32_t w0 = (uint32_t)(bit >> 5), skip = (uint32_t)bit & 31;
+    r.buf = (uint64_t)bswap32(__ldg(r.words + w0)) << (32 + skip);
+    r.nbits = 32 - (int)skip;
+    r.wpos = w0 + 1;
+    r.used = used;
+}
+
+__device__ __forceinline__ void refill(Bits &r) {
+    if (r.nbits <= 32) {
+        r.buf |= (uint64_t)bswap32(__ldg(r.words + r.wpos)) << (32 - r.nbits);
+        r.wpos++;
+        r.nbits += 32;
+    }
+}
+
+__device__ __forceinline__ void take(Bits &r, int n) {
+    r.buf <<= n;
+    r.nbits -= n;
+    r.used += n;
+}
+
+// Code length of the next Huffman code (entropy.rs:57-70), 0 when none of
+// length <= 16 matches; *sym its symbol.
+__device__ __forceinline__ int slow_symbol(const HuffLut *__restrict__ T, const uint8_t *__restrict__ symbols,
+                                           uint64_t buf, uint32_t *sym) {
+    const uint32_t e = __ldg(&T->fast[buf >> 55]);
+    if (e) {
+        *sym = e & 0xff;
+        return (int)(e >> 8);
+    }
+    const uint32_t code16 = (uint32_t)(buf >> 48);
+#pragma unroll 1
+    for (int l = 10; l <= 16; l++) {
+        const int32_t c = (int32_t)(code16 >> (16 - l));
+        if (c <= __ldg(&T->maxcode[l])) {
+            *sym = __ldg(&symbols[__ldg(&T->sym_off) + __ldg(&T->valptr[l]) + c]);
+            return l;
+        }
+    }
+    return 0;
+}
+
+enum : int { kSymError = 0, kSymDc, kSymAc, kSymRun, kSymEob };
+constexpr uint16_t kBarrierErr = 0xffff;  // the symbol runs into the interval's barrier
+
+// Decodes one symbol for coefficient index k (0: DC), in the reference's order
+// of checks (decoder.rs:501-546). kSymDc: val = DC difference, k = 1. kSymAc:
+// level val at zigzag index `at`, k past it (64 completes the block). kSymRun:
+// sixteen zeros. kSymEob: block complete (EOB, or a zero run reaching index 64).
+// kSymError: err (kBarrierErr when the symbol runs into the barrier) and errbit,
+// the reader position the reference reports.
+__device__ __forceinline__ int next_symbol(Bits &r, uint32_t avail, const HuffLut *__restrict__ T,
+                                           const uint8_t *__restrict__ symbols, int &k, int &at, int32_t &val,
+                                           uint16_t &err, uint32_t &errbit) {
+    refill(r);
+    const uint32_t fv = __ldg(&T->fastv[r.buf >> (64 - kHuffFastBits)]);
+    const uint32_t total = fv & 31;
+    if (total != 0 && total <= avail) {
+        const uint32_t kind = (fv >> 13) & 3;
+        if (k == 0) {  // DC lookups hold only difference entries
+            val = (int32_t)fv >> 16;
+            take(r, (int)total);
+            k = 1;
+            return kSymDc;
+        }
+        if (kind == kFastCoef) {
+            const int run = (int)(fv >> 5) & 15;
+            if (k + run < 64) {
+                val = (int32_t)fv >> 16;
+                take(r, (int)total);
+                at = k + run;
+                k = at + 1;
+                return kSymAc;
+            }
+        } else if (kind == kFastEob) {
+            take(r, (int)total);
+            k = 64;
+            return kSymEob;
+        } else if (k + 16 <= 64) {  // ZRL
+            take(r, (int)total);
+            k += 16;
+            return k == 64 ? kSymEob : kSymRun;
+        }
+    }
+    uint32_t sym;
+    const int l = slow_symbol(T, symbols, r.buf, &sym);
+    if (l == 0 || (uint32_t)l > avail) {
+        err = (l == 0 && avail >= 16) ? (uint16_t)kJNoHuffCode : kBarrierErr;
+        errbit = r.used + 16;
+        return kSymError;
+    }
+    int size, run;
+    if (k == 0) {
+        size = (int)sym;
+        run = 0;
+        if (size > 11) {
+            take(r, l);
+            err = kJDcCategory;
+            errbit = r.used;
+            return kSymError;
+        }
+    } else {
+        run = (int)(sym >> 4);
+        size = (int)(sym & 15);
+        if (size == 0) {
+            take(r, l);
+            if (run == 0) {
+                k = 64;
+                return kSymEob;
+            }
+            if (run != 15) {
+                err = kJAcZeroSize;
+                errbit = r.used;
+                return kSymError;
+            }
+            k += 16;
+            if (k > 64) {
+                err = kJZrlOverrun;
+                errbit = r.used;
+                return kSymError;
+            }
+            return k == 64 ? kSymEob : kSymRun;
+        }
+        if (size > 10) {
+            take(r, l);
+            err = kJAcCategory;
+            errbit = r.used;
+            return kSymError;
+        }
+        if (k + run >= 64) {
+            take(r, l);
+            err = kJAcRun;
+            errbit = r.used;
+            return kSymError;
+        }
+    }
+    if ((uint32_t)(l + size) > avail) {
+        err = kBarrierErr;
+        errbit = r.used;
+        return kSymError;
+    }
+    int32_t v = 0;
+    if (size) {  // receive_extend (entropy.rs:168-182)
+        v = (int32_t)((r.buf << l) >> (64 - size));
+        v = v < (1 << (size - 1)) ? v + 1 - (1 << size) : v;
+    }
+    take(r, l + size);
+    val = v;
+    if (k == 0) {
+        k = 1;
+        return kSymDc;
+    }
+    at = k + run;
+    k = at + 1;
+    return kSymAc;
+}
+
+}  // namespace mmr

@@ -14,6 +14,7 @@
 //       block write (decoder.rs:550-565).
 #include <cuda_runtime.h>
 
+#include "entropy_core.h"
 #include "kernels.h"
 #include "tables.h"
 
@@ -247,77 +248,12 @@ __global__ void __launch_bounds__(kScanThreads) scan_emit_kernel(JpegLaunch L) {
 
 // ------------------------------------------------------------ entropy -----
 //
-// One restart interval per thread, written as a flat loop that decodes one
-// Huffman symbol per iteration (DC or AC, chosen by the coefficient index k),
-// so the threads of a warp stay in step whatever their block boundaries.
-// Bits come from the unstuffed token stream as big-endian 32-bit words; the
-// reader may hold bits past the interval's barrier, so every use of bits is
-// checked against the count before the barrier (`limit`), which is exactly
-// where the reference reader would meet the next marker or the end of data.
-// Codes whose code and magnitude bits fit in 9 bits decode with one lookup
-// (HuffLut::fastv); others follow the reference's order of checks.
-
-constexpr int kLutCache = 6;  // deduplicated Huffman lookups held in shared memory
-
-__device__ __forceinline__ uint32_t bswap32(uint32_t x) { return __byte_perm(x, 0, 0x0123); }
-
-struct Reader {
-    const uint32_t *words;
-    uint32_t wpos;   // next word to load
-    uint64_t buf;    // next bits, MSB first
-    int nbits;       // bits held in buf (>= 32 after refill)
-    uint32_t used;   // bits consumed since the interval start
-    uint32_t limit;  // bits before the barrier
-};
-
-__device__ __forceinline__ void reader_init(Reader &r, const uint8_t *tok, uint32_t start, uint32_t end) {
-    r.words = reinterpret_cast<const uint32_t *>(tok);
-    uint32_t w0 = start >> 2, skip = (start & 3) * 8;
-    r.buf = (uint64_t)bswap32(__ldg(r.words + w0)) << (32 + skip);
-    r.nbits = 32 - (int)skip;
-    r.wpos = w0 + 1;
-    r.used = 0;
-    r.limit = (end - start) * 8;
-}
-
-__device__ __forceinline__ void refill(Reader &r) {
-    if (r.nbits <= 32) {
-        r.buf |= (uint64_t)bswap32(__ldg(r.words + r.wpos)) << (32 - r.nbits);
-        r.wpos++;
-        r.nbits += 32;
-    }
-}
-
-__device__ __forceinline__ void take(Reader &r, int n) {
-    r.buf <<= n;
-    r.nbits -= n;
-    r.used += n;
-}
-
-// Symbol for the next bits (entropy.rs:57-70): code length, 0 when no code of
-// length <= 16 matches.
-__device__ __forceinline__ int slow_symbol(const HuffLut *T, const uint8_t *__restrict__ symbols, uint64_t buf,
-                                           uint32_t *sym) {
-    uint32_t e = T->fast[buf >> 55];
-    if (e) {
-        *sym = e & 0xff;
-        return (int)(e >> 8);
-    }
-    uint32_t code16 = (uint32_t)(buf >> 48);
-#pragma unroll 1
-    for (int l = 10; l <= 16; l++) {
-        int32_t c = (int32_t)(code16 >> (16 - l));
-        if (c <= T->maxcode[l]) {
-            *sym = symbols[T->sym_off + T->valptr[l] + c];
-            return l;
-        }
-    }
-    return 0;
-}
+// Frames with more than four components (their DC predictors do not fit the
+// chunked decoder's per-slice sums): one restart interval per thread, a flat
+// loop decoding one Huffman symbol per iteration (entropy_core.h).
 
 template <int MAXC>
-__device__ void decode_interval(const JpegLaunch &L, uint32_t item, int16_t *stage, const HuffLut *s_lut,
-                                const uint8_t *s_zz) {
+__device__ void decode_interval(const JpegLaunch &L, uint32_t item, int16_t *stage, const uint8_t *s_zz) {
     uint2 it = L.items[item];
     const uint32_t f = it.x, iv = it.y;
     const JFrame *Fp = L.frames + f;
@@ -325,14 +261,8 @@ __device__ void decode_interval(const JpegLaunch &L, uint32_t item, int16_t *sta
     unsigned long long termv = st->term;
     if (!Fp->decode || termv == ~0ull || ((termv >> 8) & 1)) return;
     const uint32_t n_int = Fp->n_intervals, ri = Fp->ri, total_mcus = Fp->total_mcus, mcu_cols = Fp->mcu_cols;
-    const uint32_t sched_len = Fp->sched_len, interleaved = Fp->interleaved;
-    const JSched *sched = L.sched + Fp->sched_off;
-    const JComp *comps = L.comps + Fp->comp_off;
-    const uint16_t *quant = L.quant + Fp->quant_off;
+    const uint32_t sched_len = Fp->sched_len;
     const uint64_t blk_off = Fp->blk_off;
-    uint32_t lut_idx[8];
-#pragma unroll
-    for (int s = 0; s < 8; s++) lut_idx[s] = Fp->lut[s];
     const uint32_t n_rst = min(st->n_rst, n_int), n_tok = st->n_tokens;
     const RstEntry *rst = L.rsts + Fp->rst_off;
     uint32_t start;
@@ -341,9 +271,10 @@ __device__ void decode_interval(const JpegLaunch &L, uint32_t item, int16_t *sta
     else return;  // no RST precedes this interval: an earlier interval fails its restart check
     const bool barrier_rst = iv < n_rst;
     const uint32_t barrier = barrier_rst ? rst[iv].tok : n_tok;
+    const uint32_t limit = (barrier - start) * 8;
 
-    Reader r;
-    reader_init(r, Fp->tok, start, barrier);
+    Bits r;
+    bits_init(r, Fp->tok, (unsigned long long)start * 8, 0);
     int32_t pred[MAXC];
 #pragma unroll
     for (int c = 0; c < MAXC; c++) pred[c] = 0;
@@ -356,121 +287,50 @@ __device__ void decode_interval(const JpegLaunch &L, uint32_t item, int16_t *sta
     const HuffLut *dcl = nullptr, *acl = nullptr;
     int32_t q0 = 0, dq = 0;
     uint64_t blk = 0;
+    const JBlockRec *recs = L.brec + Fp->sched_off;
     auto setup_block = [&]() {
-        JSched e = sched[si];
-        comp = e.comp;
-        const JComp &C = comps[comp];
-        uint32_t mx = mcu % mcu_cols, my = mcu / mcu_cols;
-        uint32_t gx = interleaved ? mx * C.h + e.bx : mx, gy = interleaved ? my * C.v + e.by : my;
-        blk = blk_off + C.blk_base + (uint64_t)gy * C.bw + gx;
-        q0 = quant[C.q * 64];
-        uint32_t di = lut_idx[e.dc], ai = lut_idx[4 + e.ac];
-        dcl = di < kLutCache ? s_lut + di : L.luts + di;
-        acl = ai < kLutCache ? s_lut + ai : L.luts + ai;
+        const JBlockRec R = recs[si];
+        comp = R.comp;
+        const uint32_t mx = mcu % mcu_cols, my = mcu / mcu_cols;
+        blk = blk_off + R.base_off + mx * R.mul_x + (uint64_t)my * R.mul_y;
+        q0 = R.q0;
+        dcl = L.luts + R.dc_lut;
+        acl = L.luts + R.ac_lut;
     };
     setup_block();
     int k = 0;
     uint16_t kind = kDiagNone;
     uint32_t errpos = 0;
-    const uint16_t barrier_kind = barrier_rst ? kJMarkerInData : kJEndOfData;
     for (;;) {
-        refill(r);
-        const HuffLut *T = k == 0 ? dcl : acl;
-        const uint32_t avail = r.limit - r.used;
-        const int32_t fv = T->fastv[r.buf >> 55];
-        int run, size, codelen, val = 0;
-        bool have_val;
-        if (fv != 0 && (uint32_t)(fv & 0xff) <= avail) {
-            run = (fv >> 8) & 15;
-            size = (fv >> 12) & 15;
-            codelen = (fv & 0xff) - size;
-            val = fv >> 16;
-            have_val = true;
-        } else {
-            uint32_t sym;
-            codelen = slow_symbol(T, L.symbols, r.buf, &sym);
-            if (codelen == 0 || (uint32_t)codelen > avail) {
-                kind = (codelen == 0 && avail >= 16) ? (uint16_t)kJNoHuffCode : barrier_kind;
-                errpos = r.used + 16;
-                break;
-            }
-            have_val = false;
-            if (k == 0) {  // decoder.rs:503-506
-                run = 0;
-                size = (int)sym;
-                if (size > 11) {
-                    take(r, codelen);
-                    kind = kJDcCategory;
-                    errpos = r.used;
-                    break;
-                }
-            } else {  // decoder.rs:519-537
-                run = (int)(sym >> 4);
-                size = (int)(sym & 15);
-                if (size == 0) {
-                    take(r, codelen);
-                    if (run != 0) {
-                        if (run != 15) {
-                            kind = kJAcZeroSize;
-                            errpos = r.used;
-                            break;
-                        }
-                        k += 16;
-                        if (k > 64) {
-                            kind = kJZrlOverrun;
-                            errpos = r.used;
-                            break;
-                        }
-                        if (k < 64) continue;
-                    }
-                    k = 64;  // EOB, or a zero run ending exactly at index 64
-                }
-                if (size > 10) {
-                    take(r, codelen);
-                    kind = kJAcCategory;
-                    errpos = r.used;
-                    break;
-                }
-            }
+        int at;
+        int32_t val;
+        uint16_t err;
+        uint32_t eb;
+        const int sy = next_symbol(r, limit - r.used, k == 0 ? dcl : acl, L.symbols, k, at, val, err, eb);
+        if (sy == kSymError) {
+            kind = err;
+            errpos = eb;
+            break;
         }
-        if (k < 64) {
-            if (k > 0 && k + run >= 64) {  // decoder.rs:538-541, before the magnitude bits
-                take(r, codelen);
-                kind = kJAcRun;
+        if (sy == kSymDc) {  // decoder.rs:507-515
+            int64_t p = (int64_t)pred[comp] + val;
+            if (p > INT32_MAX || p < INT32_MIN) {
+                kind = kJDcPredOverflow;
                 errpos = r.used;
                 break;
             }
-            if ((uint32_t)(codelen + size) > avail) {  // magnitude bits run into the barrier
-                kind = barrier_kind;
+            pred[comp] = (int32_t)p;
+            int64_t d = p * (int64_t)q0;
+            if (d > INT32_MAX || d < INT32_MIN) {
+                kind = kJDcDeqOverflow;
+                errpos = r.used;
                 break;
             }
-            if (!have_val && size) {  // receive_extend (entropy.rs:168-182)
-                int32_t v = (int32_t)((r.buf << codelen) >> (64 - size));
-                val = v < (1 << (size - 1)) ? v + 1 - (1 << size) : v;
-            }
-            take(r, codelen + size);
-            if (k == 0) {  // decoder.rs:507-515
-                int64_t p = (int64_t)pred[comp] + val;
-                if (p > INT32_MAX || p < INT32_MIN) {
-                    kind = kJDcPredOverflow;
-                    errpos = r.used;
-                    break;
-                }
-                pred[comp] = (int32_t)p;
-                int64_t d = p * (int64_t)q0;
-                if (d > INT32_MAX || d < INT32_MIN) {
-                    kind = kJDcDeqOverflow;
-                    errpos = r.used;
-                    break;
-                }
-                dq = (int32_t)d;
-                k = 1;
-                continue;
-            }
-            k += run;
-            stage[s_zz[k]] = (int16_t)val;
-            if (++k < 64) continue;
+            dq = (int32_t)d;
+            continue;
         }
+        if (sy == kSymAc) stage[s_zz[at]] = (int16_t)val;
+        if (k < 64) continue;
         // block complete: levels + dequantised DC out, staging cleared
         int4 *dst = reinterpret_cast<int4 *>(L.coef + blk * 64);
 #pragma unroll
@@ -489,10 +349,8 @@ __device__ void decode_interval(const JpegLaunch &L, uint32_t item, int16_t *sta
 
     Diag out = make_diag(kDiagNone);
     if (kind != kDiagNone) {
-#pragma unroll
-        for (int q = 0; q < 8; q++) stage4[q] = make_int4(0, 0, 0, 0);
-        if (kind == kJMarkerInData) out = make_diag(kJMarkerInData, barrier, 0xd0 + rst[iv].number);
-        else if (kind == kJEndOfData) out = make_diag(kJEndOfData, n_tok);
+        if (kind == kBarrierErr)
+            out = barrier_rst ? make_diag(kJMarkerInData, barrier, 0xd0 + rst[iv].number) : make_diag(kJEndOfData, n_tok);
         else out = make_diag(kind, start + (errpos + 7) / 8);
     } else if (iv + 1 < n_int) {
         // consume_restart before the next interval (entropy.rs:111-134)
@@ -512,21 +370,16 @@ __device__ void decode_interval(const JpegLaunch &L, uint32_t item, int16_t *sta
 
 template <int MAXC>
 __global__ void __launch_bounds__(kEntropyThreads) entropy_kernel(JpegLaunch L, uint32_t first, uint32_t count) {
-    __shared__ __align__(16) HuffLut s_lut[kLutCache];
     __shared__ __align__(16) int16_t s_stage[kEntropyThreads * kStageStride];
     __shared__ uint8_t s_zz[64];
-    const uint32_t nl = min(L.n_luts, (uint32_t)kLutCache);
-    const int4 *src = reinterpret_cast<const int4 *>(L.luts);
-    int4 *dst = reinterpret_cast<int4 *>(s_lut);
-    for (uint32_t i = threadIdx.x; i < nl * (uint32_t)(sizeof(HuffLut) / 16); i += blockDim.x) dst[i] = src[i];
-    if (threadIdx.x < 64) s_zz[threadIdx.x] = (uint8_t)c_zigzag[threadIdx.x];
     int4 *mine = reinterpret_cast<int4 *>(s_stage + threadIdx.x * kStageStride);
 #pragma unroll
     for (int q = 0; q < 8; q++) mine[q] = make_int4(0, 0, 0, 0);
+    if (threadIdx.x < 64) s_zz[threadIdx.x] = (uint8_t)c_zigzag[threadIdx.x];
     __syncthreads();
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= count) return;
-    decode_interval<MAXC>(L, first + i, s_stage + threadIdx.x * kStageStride, s_lut, s_zz);
+    decode_interval<MAXC>(L, first + i, s_stage + threadIdx.x * kStageStride, s_zz);
 }
 
 __global__ void resolve_kernel(JpegLaunch L) {

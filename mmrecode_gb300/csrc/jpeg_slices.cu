@@ -32,6 +32,7 @@
 // one the serial decoder stops at.
 #include <cuda_runtime.h>
 
+#include "entropy_core.h"
 #include "kernels.h"
 #include "tables.h"
 
@@ -45,164 +46,9 @@ constexpr unsigned long long kStGuess = ~0ull - 1;  // start not yet derived fro
 constexpr int kSliceThreads = 128;
 constexpr int kStride = 72;  // int16 per staged block (144 B: conflict-free 16 B rows)
 constexpr int kKeyBits = 26;
-constexpr uint16_t kBarrierErr = 0xffff;
 
 __device__ __forceinline__ unsigned long long pack_state(unsigned long long p, uint32_t si, uint32_t k) {
     return (p << 16) | (si << 8) | k;
-}
-
-__device__ __forceinline__ uint32_t bswap32(uint32_t x) { return __byte_perm(x, 0, 0x0123); }
-
-// Big-endian bit reader over unstuffed tokens, 32-bit word loads. It may hold
-// bits past the interval's barrier; callers never use more than `avail` bits.
-struct Bits {
-    const uint32_t *words;
-    uint32_t wpos;
-    int nbits;
-    uint64_t buf;
-    uint32_t used;  // bits consumed, counted from the reader's base position
-};
-
-__device__ __forceinline__ void bits_init(Bits &r, const uint8_t *tok, unsigned long long bit, uint32_t used) {
-    r.words = reinterpret_cast<const uint32_t *>(tok);
-    const uint32_t w0 = (uint32_t)(bit >> 5), skip = (uint32_t)bit & 31;
-    r.buf = (uint64_t)bswap32(__ldg(r.words + w0)) << (32 + skip);
-    r.nbits = 32 - (int)skip;
-    r.wpos = w0 + 1;
-    r.used = used;
-}
-
-__device__ __forceinline__ void refill(Bits &r) {
-    if (r.nbits <= 32) {
-        r.buf |= (uint64_t)bswap32(__ldg(r.words + r.wpos)) << (32 - r.nbits);
-        r.wpos++;
-        r.nbits += 32;
-    }
-}
-
-__device__ __forceinline__ void take(Bits &r, int n) {
-    r.buf <<= n;
-    r.nbits -= n;
-    r.used += n;
-}
-
-// Code length of the next Huffman code (entropy.rs:57-70), 0 when none of length <= 16 matches.
-__device__ __forceinline__ int slow_symbol(const HuffLut *__restrict__ T, const uint8_t *__restrict__ symbols,
-                                           uint64_t buf, uint32_t *sym) {
-    const uint32_t e = __ldg(&T->fast[buf >> 55]);
-    if (e) {
-        *sym = e & 0xff;
-        return (int)(e >> 8);
-    }
-    const uint32_t code16 = (uint32_t)(buf >> 48);
-#pragma unroll 1
-    for (int l = 10; l <= 16; l++) {
-        const int32_t c = (int32_t)(code16 >> (16 - l));
-        if (c <= __ldg(&T->maxcode[l])) {
-            *sym = __ldg(&symbols[__ldg(&T->sym_off) + __ldg(&T->valptr[l]) + c]);
-            return l;
-        }
-    }
-    return 0;
-}
-
-enum : int { kSymError = 0, kSymDc, kSymAc, kSymRun, kSymEob };
-
-// Decodes one symbol for coefficient index k (0: DC), in the reference's order of
-// checks (decoder.rs:501-546). kSymDc: val = DC difference, k = 1. kSymAc: level
-// val at zigzag index `at`, k past it (64 completes the block). kSymRun: sixteen
-// zeros. kSymEob: block complete. kSymError: err (kBarrierErr when the symbol runs
-// into the barrier) and errbit, the reader position the reference reports.
-__device__ __forceinline__ int next_symbol(Bits &r, uint32_t avail, const HuffLut *__restrict__ T,
-                                           const uint8_t *__restrict__ symbols, int &k, int &at, int32_t &val,
-                                           uint16_t &err, uint32_t &errbit) {
-    refill(r);
-    const int32_t fv = __ldg(&T->fastv[r.buf >> 55]);
-    if (fv != 0) {
-        const int total = fv & 0xff, run = (fv >> 8) & 15;
-        if ((uint32_t)total <= avail && (k == 0 || k + run < 64)) {
-            val = fv >> 16;
-            take(r, total);
-            if (k == 0) {
-                k = 1;
-                return kSymDc;
-            }
-            at = k + run;
-            k = at + 1;
-            return kSymAc;
-        }
-    }
-    uint32_t sym;
-    const int l = slow_symbol(T, symbols, r.buf, &sym);
-    if (l == 0 || (uint32_t)l > avail) {
-        err = (l == 0 && avail >= 16) ? (uint16_t)kJNoHuffCode : kBarrierErr;
-        errbit = r.used + 16;
-        return kSymError;
-    }
-    int size, run;
-    if (k == 0) {
-        size = (int)sym;
-        run = 0;
-        if (size > 11) {
-            take(r, l);
-            err = kJDcCategory;
-            errbit = r.used;
-            return kSymError;
-        }
-    } else {
-        run = (int)(sym >> 4);
-        size = (int)(sym & 15);
-        if (size == 0) {
-            take(r, l);
-            if (run == 0) {
-                k = 64;
-                return kSymEob;
-            }
-            if (run != 15) {
-                err = kJAcZeroSize;
-                errbit = r.used;
-                return kSymError;
-            }
-            k += 16;
-            if (k > 64) {
-                err = kJZrlOverrun;
-                errbit = r.used;
-                return kSymError;
-            }
-            return k == 64 ? kSymEob : kSymRun;
-        }
-        if (size > 10) {
-            take(r, l);
-            err = kJAcCategory;
-            errbit = r.used;
-            return kSymError;
-        }
-        if (k + run >= 64) {
-            take(r, l);
-            err = kJAcRun;
-            errbit = r.used;
-            return kSymError;
-        }
-    }
-    if ((uint32_t)(l + size) > avail) {
-        err = kBarrierErr;
-        errbit = r.used;
-        return kSymError;
-    }
-    int32_t v = 0;
-    if (size) {  // receive_extend (entropy.rs:168-182)
-        v = (int32_t)((r.buf << l) >> (64 - size));
-        v = v < (1 << (size - 1)) ? v + 1 - (1 << size) : v;
-    }
-    take(r, l + size);
-    val = v;
-    if (k == 0) {
-        k = 1;
-        return kSymDc;
-    }
-    at = k + run;
-    k = at + 1;
-    return kSymAc;
 }
 
 // Tables of MCU block si.
@@ -213,11 +59,11 @@ struct BlockTabs {
 };
 
 __device__ __forceinline__ BlockTabs block_tabs(const JpegLaunch &L, const JFrame &F, uint32_t si) {
-    const JSched e = L.sched[F.sched_off + si];
+    const JBlockRec &R = L.brec[F.sched_off + si];
     BlockTabs t;
-    t.comp = e.comp;
-    t.dc = L.luts + F.lut[e.dc];
-    t.ac = L.luts + F.lut[4 + e.ac];
+    t.comp = R.comp;
+    t.dc = L.luts + R.dc_lut;
+    t.ac = L.luts + R.ac_lut;
     return t;
 }
 
@@ -607,10 +453,13 @@ __device__ __forceinline__ void report(const JpegLaunch &L, const SliceRef &s, u
 
 __global__ void __launch_bounds__(kSliceThreads) slice_decode_kernel(JpegLaunch L) {
     __shared__ __align__(16) int16_t s_stage[kSliceThreads * kStride];
+    __shared__ uint8_t s_zz[64];  // lanes index it freely: a shared table serves them in one pass
     int16_t *stage = s_stage + threadIdx.x * kStride;
     int4 *stage4 = reinterpret_cast<int4 *>(stage);
 #pragma unroll
     for (int q = 0; q < 8; q++) stage4[q] = make_int4(0, 0, 0, 0);
+    if (threadIdx.x < 64) s_zz[threadIdx.x] = c_slice_zz[threadIdx.x];
+    __syncthreads();
     const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
     SliceRef s;
     if (!slice_ref(L, slot, s)) return;
@@ -636,11 +485,11 @@ __global__ void __launch_bounds__(kSliceThreads) slice_decode_kernel(JpegLaunch 
     uint16_t err;
     uint32_t eb;
     if (k != 0) {  // the block straddling the start belongs to an earlier slice
-        const BlockTabs tb = block_tabs(L, F, si);
+        const HuffLut *acl = block_tabs(L, F, si).ac;
         for (;;) {
-            const int sy = next_symbol(r, lim - r.used, tb.ac, L.symbols, k, at, val, err, eb);
+            const int sy = next_symbol(r, lim - r.used, acl, L.symbols, k, at, val, err, eb);
             if (sy == kSymError) return;
-            if (sy == kSymEob || (sy == kSymAc && k == 64)) break;
+            if (k == 64) break;
         }
         si = si + 1 == sched_len ? 0 : si + 1;
         k = 0;
@@ -648,35 +497,40 @@ __global__ void __launch_bounds__(kSliceThreads) slice_decode_kernel(JpegLaunch 
     long long pred[4];
 #pragma unroll
     for (int c = 0; c < 4; c++) pred[c] = P.dc[c];
-    const JComp *comps = L.comps + F.comp_off;
-    const uint16_t *quant = L.quant + F.quant_off;
-    const RstEntry *rst = L.rsts + F.rst_off;
-    const uint32_t mcu0 = iv * F.ri;
-    for (uint32_t owned = 0; owned < nown; owned++) {
-        const uint32_t b = P.base + owned;
-        const uint32_t mcu = mcu0 + b / sched_len;
-        const JSched e = L.sched[F.sched_off + si];
-        const JComp &C = comps[e.comp];
-        const HuffLut *dcl = L.luts + F.lut[e.dc];
-        const HuffLut *acl = L.luts + F.lut[4 + e.ac];
-        const uint32_t mx = mcu % F.mcu_cols, my = mcu / F.mcu_cols;
-        const uint32_t gx = F.interleaved ? mx * C.h + e.bx : mx, gy = F.interleaved ? my * C.v + e.by : my;
-        const uint64_t blk = F.blk_off + C.blk_base + (uint64_t)gy * C.bw + gx;
-        const int32_t q0 = quant[C.q * 64];
+    // MCU of the first owned block, then advanced block by block
+    const uint32_t mcu = iv * F.ri + P.base / sched_len;
+    const uint32_t mcu_cols = F.mcu_cols;
+    uint32_t mx = mcu % mcu_cols, my = mcu / mcu_cols;
+    uint32_t b = P.base;
+    const uint32_t bend = P.base + nown;
+    const HuffLut *dcl, *acl;
+    uint64_t blk;
+    int32_t q0, dq = 0;
+    uint32_t comp;
+    const JBlockRec *recs = L.brec + F.sched_off;
+    auto setup = [&]() {
+        const JBlockRec R = recs[si];
+        comp = R.comp;
+        dcl = L.luts + R.dc_lut;
+        acl = L.luts + R.ac_lut;
+        blk = F.blk_off + R.base_off + mx * R.mul_x + (uint64_t)my * R.mul_y;
+        q0 = R.q0;
+    };
+    setup();
+    uint32_t sym_at = r.used;  // start of the symbol being decoded
+    for (;;) {
+        sym_at = r.used;
+        const int sy = next_symbol(r, lim - r.used, k == 0 ? dcl : acl, L.symbols, k, at, val, err, eb);
         uint16_t kind = kDiagNone;
         uint32_t errpos = 0;
-        unsigned long long symstart = p0 + r.used;
-        int32_t dq = 0;
-        // DC (decoder.rs:501-515)
-        int sy = next_symbol(r, lim - r.used, dcl, L.symbols, k, at, val, err, eb);
         if (sy == kSymError) {
             kind = err;
             errpos = eb;
-        } else {
+        } else if (sy == kSymDc) {  // decoder.rs:507-515
             long long pc = 0;
 #pragma unroll
             for (int c = 0; c < 4; c++)
-                if (e.comp == (uint32_t)c) pc = pred[c];
+                if (comp == (uint32_t)c) pc = pred[c];
             const long long pn = pc + val;
             if (pn > INT32_MAX || pn < INT32_MIN) {
                 kind = kJDcPredOverflow;
@@ -684,7 +538,7 @@ __global__ void __launch_bounds__(kSliceThreads) slice_decode_kernel(JpegLaunch 
             } else {
 #pragma unroll
                 for (int c = 0; c < 4; c++)
-                    if (e.comp == (uint32_t)c) pred[c] = pn;
+                    if (comp == (uint32_t)c) pred[c] = pn;
                 const long long d = pn * (long long)q0;
                 if (d > INT32_MAX || d < INT32_MIN) {
                     kind = kJDcDeqOverflow;
@@ -692,28 +546,24 @@ __global__ void __launch_bounds__(kSliceThreads) slice_decode_kernel(JpegLaunch 
                 }
                 dq = (int32_t)d;
             }
-        }
-        // AC (decoder.rs:517-546)
-        while (kind == kDiagNone && k < 64) {
-            symstart = p0 + r.used;
-            sy = next_symbol(r, lim - r.used, acl, L.symbols, k, at, val, err, eb);
-            if (sy == kSymAc) stage[c_slice_zz[at]] = (int16_t)val;
-            else if (sy == kSymError) {
-                kind = err;
-                errpos = eb;
-            }
+            if (kind == kDiagNone) continue;
+        } else {
+            if (sy == kSymAc) stage[s_zz[at]] = (int16_t)val;
+            if (k < 64) continue;
         }
         if (kind != kDiagNone) {
             Diag d;
             if (kind == kBarrierErr) {
-                d = (s.v.flags & 1) ? make_diag(kJMarkerInData, s.v.barrier, 0xd0 + rst[iv].number)
-                                    : make_diag(kJEndOfData, L.states[L.items[s.item].x].n_tokens);
+                d = (s.v.flags & 1)
+                        ? make_diag(kJMarkerInData, s.v.barrier, 0xd0 + L.rsts[F.rst_off + iv].number)
+                        : make_diag(kJEndOfData, L.states[L.items[s.item].x].n_tokens);
             } else {
                 d = make_diag(kind, s.v.start + (uint32_t)((p0 + errpos + 7) / 8));
             }
-            report(L, s, slot, symstart, d, 0);
+            report(L, s, slot, p0 + sym_at, d, 0);
             return;
         }
+        // block complete
         int4 *dst = reinterpret_cast<int4 *>(L.coef + blk * 64);
 #pragma unroll
         for (int q = 0; q < 8; q++) {
@@ -726,8 +576,16 @@ __global__ void __launch_bounds__(kSliceThreads) slice_decode_kernel(JpegLaunch 
             report(L, s, slot, endbit, make_diag(kDiagNone, s.v.start + (uint32_t)((endbit + 7) / 8)), 1);
             return;
         }
+        if (++b == bend) return;
+        if (++si == sched_len) {
+            si = 0;
+            if (++mx == mcu_cols) {
+                mx = 0;
+                my++;
+            }
+        }
+        setup();
         k = 0;
-        si = si + 1 == sched_len ? 0 : si + 1;
     }
 }
 

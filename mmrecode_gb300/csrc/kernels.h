@@ -19,6 +19,7 @@ struct JpegLaunch {
     uint32_t *tile_rst;
     RstEntry *rsts;
     const JSched *sched;
+    const JBlockRec *brec;       // parallel to sched
     const JComp *comps;
     const HuffLut *luts;
     uint32_t n_luts;

@@ -11,17 +11,21 @@ namespace mmr {
 // fast[] resolves every code of length <= 9 from the next 9 bits; longer codes use
 // maxcode/valptr (JPEG Annex F.2.2.3), which for canonical codes finds the same
 // code as the reference's length-by-length search.
+constexpr int kHuffFastBits = 11;
+enum : uint32_t { kFastCoef = 0, kFastEob = 1, kFastZrl = 2 };
+
 struct HuffLut {
     uint16_t fast[512];    // (length << 8) | symbol; 0 when the code is longer than 9 bits or absent
-    // Code and magnitude bits together within the next 9 bits, for symbols that decode
-    // without error (DC size <= 11; AC size 1..10): value << 16 | size << 12 | run << 8 |
-    // total bits; 0 otherwise (EOB, ZRL, invalid symbols and long codes take the slow path).
-    int32_t fastv[512];
+    // Whole symbols within the next 11 bits: value << 16 | kind << 13 | size << 9 |
+    // run << 5 | total bits (code + magnitude). DC lookups hold differences of size
+    // 0..11; AC lookups levels of size 1..10 (kFastCoef), EOB and ZRL. 0: slow path
+    // (longer symbols, and every symbol the reference rejects).
+    uint32_t fastv[1 << kHuffFastBits];
     int32_t maxcode[18];   // largest code of each length 1..16, -1 if none
     int32_t valptr[18];    // symbol index of a length's first code, minus that code
     uint32_t sym_off;      // first symbol in the symbol pool
     uint32_t nsym;
-    uint32_t pad[2];       // size multiple of 16 (copied to shared memory with 16-byte loads)
+    uint32_t pad[2];       // size multiple of 16
 };
 
 // One frame component (SOF0 order).
@@ -40,6 +44,19 @@ struct JSched {
     uint8_t bx, by;  // block position inside the MCU
     uint8_t dc, ac;  // Huffman table slots
     uint8_t pad[2];
+};
+
+// Everything the entropy decoders need for one MCU block position, in one
+// 32-byte record (parallel to the schedule): lookups, DC quantiser, and the
+// block index of MCU (mx, my) as base_off + mx * mul_x + my * mul_y.
+struct JBlockRec {
+    uint32_t dc_lut, ac_lut;
+    uint32_t base_off;  // frame-relative block of MCU (0, 0)
+    uint32_t mul_y;
+    uint32_t mul_x;
+    uint32_t comp;      // frame component (scan components = frame components)
+    int32_t q0;         // DC quantiser
+    uint32_t pad;
 };
 
 struct JFrame {
