@@ -317,19 +317,18 @@ void build_lut(const uint8_t *key, size_t key_len, uint32_t sym_off, bool ac, Hu
                     if (!lut->fast[first + j]) lut->fast[first + j] = (uint16_t)((l << 8) | sym);
             }
             if ((uint32_t)l <= FB) {
-                uint32_t run = 0, size = 0, kind = kFastCoef;
+                uint32_t size = 0, adv = 1, eob = 0;
                 bool ok;
                 if (ac) {
-                    run = sym >> 4;
                     size = sym & 15;
-                    if (sym == 0x00) kind = kFastEob, ok = true;
-                    else if (sym == 0xf0) kind = kFastZrl, ok = true;
+                    adv = (sym >> 4) + 1;
+                    if (sym == 0x00) eob = kFastEob, adv = 0, ok = true;
+                    else if (sym == 0xf0) adv = 16, ok = true;
                     else ok = size >= 1 && size <= 10;
                 } else {
                     size = sym;
                     ok = size <= 11;
                 }
-                if (kind != kFastCoef) size = 0;
                 if (ok && l + size <= FB) {
                     const uint32_t rest = FB - l - size;  // bits after the magnitude
                     for (uint32_t m = 0; m < (1u << size); m++) {
@@ -338,7 +337,7 @@ void build_lut(const uint8_t *key, size_t key_len, uint32_t sym_off, bool ac, Hu
                             v = (int32_t)m;
                             if (v < (1 << (size - 1))) v += 1 - (1 << size);  // receive_extend
                         }
-                        const uint32_t e = ((uint32_t)v << 16) | (kind << 13) | (size << 9) | (run << 5) | (l + size);
+                        const uint32_t e = ((uint32_t)v << 16) | eob | (adv << 5) | (l + size);
                         const uint32_t base = (code << (FB - l)) | (m << rest);
                         for (uint32_t j = 0; j < (1u << rest); j++)
                             if (!lut->fastv[base + j]) lut->fastv[base + j] = e;

@@ -68,54 +68,34 @@ __device__ __forceinline__ int slow_symbol(const HuffLut *__restrict__ T, const 
     return 0;
 }
 
-enum : int { kSymError = 0, kSymDc, kSymAc, kSymRun, kSymEob };
 constexpr uint16_t kBarrierErr = 0xffff;  // the symbol runs into the interval's barrier
 
-// Decodes one symbol for coefficient index k (0: DC), in the reference's order
-// of checks (decoder.rs:501-546). kSymDc: val = DC difference, k = 1. kSymAc:
-// level val at zigzag index `at`, k past it (64 completes the block). kSymRun:
-// sixteen zeros. kSymEob: block complete (EOB, or a zero run reaching index 64).
-// kSymError: err (kBarrierErr when the symbol runs into the barrier) and errbit,
-// the reader position the reference reports.
-__device__ __forceinline__ int next_symbol(Bits &r, uint32_t avail, const HuffLut *__restrict__ T,
-                                           const uint8_t *__restrict__ symbols, int &k, int &at, int32_t &val,
-                                           uint16_t &err, uint32_t &errbit) {
+// Decodes one symbol for coefficient index k (0: the DC symbol), in the
+// reference's order of checks (decoder.rs:501-546). On success returns true,
+// moves k (1 after the DC difference, past an AC level, 16 on for ZRL, 64 at
+// EOB) and sets val: the DC difference or the AC level, 0 for EOB and ZRL, to be
+// stored at zigzag index k - 1 (a zero stored past the last level changes
+// nothing). On failure returns false with err (kBarrierErr when the symbol runs
+// into the barrier) and errbit, the reader position the reference reports.
+__device__ __forceinline__ bool decode_symbol(Bits &r, uint32_t avail, const HuffLut *__restrict__ T,
+                                              const uint8_t *__restrict__ symbols, int &k, int32_t &val,
+                                              uint16_t &err, uint32_t &errbit) {
     refill(r);
     const uint32_t fv = __ldg(&T->fastv[r.buf >> (64 - kHuffFastBits)]);
     const uint32_t total = fv & 31;
-    if (total != 0 && total <= avail) {
-        const uint32_t kind = (fv >> 13) & 3;
-        if (k == 0) {  // DC lookups hold only difference entries
-            val = (int32_t)fv >> 16;
-            take(r, (int)total);
-            k = 1;
-            return kSymDc;
-        }
-        if (kind == kFastCoef) {
-            const int run = (int)(fv >> 5) & 15;
-            if (k + run < 64) {
-                val = (int32_t)fv >> 16;
-                take(r, (int)total);
-                at = k + run;
-                k = at + 1;
-                return kSymAc;
-            }
-        } else if (kind == kFastEob) {
-            take(r, (int)total);
-            k = 64;
-            return kSymEob;
-        } else if (k + 16 <= 64) {  // ZRL
-            take(r, (int)total);
-            k += 16;
-            return k == 64 ? kSymEob : kSymRun;
-        }
+    const int kn = (fv & kFastEob) ? 64 : k + (int)((fv >> 5) & 127);
+    if (total - 1u < avail && kn <= 64) {
+        val = (int32_t)fv >> 16;
+        take(r, (int)total);
+        k = kn;
+        return true;
     }
     uint32_t sym;
     const int l = slow_symbol(T, symbols, r.buf, &sym);
     if (l == 0 || (uint32_t)l > avail) {
         err = (l == 0 && avail >= 16) ? (uint16_t)kJNoHuffCode : kBarrierErr;
         errbit = r.used + 16;
-        return kSymError;
+        return false;
     }
     int size, run;
     if (k == 0) {
@@ -125,47 +105,48 @@ __device__ __forceinline__ int next_symbol(Bits &r, uint32_t avail, const HuffLu
             take(r, l);
             err = kJDcCategory;
             errbit = r.used;
-            return kSymError;
+            return false;
         }
     } else {
         run = (int)(sym >> 4);
         size = (int)(sym & 15);
         if (size == 0) {
             take(r, l);
+            val = 0;
             if (run == 0) {
                 k = 64;
-                return kSymEob;
+                return true;
             }
             if (run != 15) {
                 err = kJAcZeroSize;
                 errbit = r.used;
-                return kSymError;
+                return false;
             }
-            k += 16;
-            if (k > 64) {
+            if (k + 16 > 64) {
                 err = kJZrlOverrun;
                 errbit = r.used;
-                return kSymError;
+                return false;
             }
-            return k == 64 ? kSymEob : kSymRun;
+            k += 16;
+            return true;
         }
         if (size > 10) {
             take(r, l);
             err = kJAcCategory;
             errbit = r.used;
-            return kSymError;
+            return false;
         }
         if (k + run >= 64) {
             take(r, l);
             err = kJAcRun;
             errbit = r.used;
-            return kSymError;
+            return false;
         }
     }
     if ((uint32_t)(l + size) > avail) {
         err = kBarrierErr;
         errbit = r.used;
-        return kSymError;
+        return false;
     }
     int32_t v = 0;
     if (size) {  // receive_extend (entropy.rs:168-182)
@@ -174,13 +155,8 @@ __device__ __forceinline__ int next_symbol(Bits &r, uint32_t avail, const HuffLu
     }
     take(r, l + size);
     val = v;
-    if (k == 0) {
-        k = 1;
-        return kSymDc;
-    }
-    at = k + run;
-    k = at + 1;
-    return kSymAc;
+    k += run + 1;
+    return true;
 }
 
 }  // namespace mmr

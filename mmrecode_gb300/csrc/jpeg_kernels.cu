@@ -302,17 +302,16 @@ __device__ void decode_interval(const JpegLaunch &L, uint32_t item, int16_t *sta
     uint16_t kind = kDiagNone;
     uint32_t errpos = 0;
     for (;;) {
-        int at;
         int32_t val;
         uint16_t err;
         uint32_t eb;
-        const int sy = next_symbol(r, limit - r.used, k == 0 ? dcl : acl, L.symbols, k, at, val, err, eb);
-        if (sy == kSymError) {
+        const int k0 = k;
+        if (!decode_symbol(r, limit - r.used, k0 == 0 ? dcl : acl, L.symbols, k, val, err, eb)) {
             kind = err;
             errpos = eb;
             break;
         }
-        if (sy == kSymDc) {  // decoder.rs:507-515
+        if (k0 == 0) {  // decoder.rs:507-515
             int64_t p = (int64_t)pred[comp] + val;
             if (p > INT32_MAX || p < INT32_MIN) {
                 kind = kJDcPredOverflow;
@@ -329,7 +328,7 @@ __device__ void decode_interval(const JpegLaunch &L, uint32_t item, int16_t *sta
             dq = (int32_t)d;
             continue;
         }
-        if (sy == kSymAc) stage[s_zz[at]] = (int16_t)val;
+        stage[s_zz[k - 1]] = (int16_t)val;
         if (k < 64) continue;
         // block complete: levels + dequantised DC out, staging cleared
         int4 *dst = reinterpret_cast<int4 *>(L.coef + blk * 64);

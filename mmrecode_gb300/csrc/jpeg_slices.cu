@@ -191,9 +191,11 @@ __global__ void __launch_bounds__(kSliceThreads) slice_spec_kernel(JpegLaunch L)
     BlockTabs tb = block_tabs(L, F, si);
     uint32_t blocks = 0;
     int32_t dc[4] = {0, 0, 0, 0};
+    int32_t dcv = 0;  // DC difference of the block in progress (0 before its DC symbol)
     SliceSpec *sp = L.spec + slot;
     uint32_t q = 0, recorded = 0;
     const uint32_t step = S / (kSliceCheckpoints + 1);
+    uint32_t next_mark = guess ? step : 0xffffffffu;
     unsigned long long exit_state = kStErr;
     for (;;) {
         const uint32_t pr = r.used;
@@ -201,31 +203,26 @@ __global__ void __launch_bounds__(kSliceThreads) slice_spec_kernel(JpegLaunch L)
             exit_state = pack_state(p0 + pr, si, k);
             break;
         }
-        if (guess) {
+        if (pr >= next_mark) {
             while (q < (uint32_t)kSliceCheckpoints && pr >= (q + 1) * step) {
                 SlicePoint cp;
                 cp.state = pack_state(p0 + pr, si, k);
                 cp.blocks = blocks;
                 cp.pad = 0;
 #pragma unroll
-                for (int c = 0; c < 4; c++) cp.dc[c] = dc[c];
+                for (int c = 0; c < 4; c++) cp.dc[c] = dc[c] + (tb.comp == (uint32_t)c ? dcv : 0);
                 sp->cp[q] = cp;
                 recorded |= 1u << q;
                 q++;
             }
+            next_mark = q < (uint32_t)kSliceCheckpoints ? (q + 1) * step : 0xffffffffu;
         }
-        if (k == 0) blocks++;
-        int at;
+        const int k0 = k;
+        blocks += k0 == 0;
         int32_t val;
         uint16_t err;
         uint32_t eb;
-        const int sy = next_symbol(r, lim - pr, k == 0 ? tb.dc : tb.ac, L.symbols, k, at, val, err, eb);
-        if (sy == kSymDc) {
-            add_dc(dc, tb.comp, val);
-            continue;
-        }
-        if (sy == kSymRun || (sy == kSymAc && k < 64)) continue;
-        if (sy == kSymError) {
+        if (!decode_symbol(r, lim - pr, k0 == 0 ? tb.dc : tb.ac, L.symbols, k, val, err, eb)) {
             if (!guess || err == kBarrierErr) break;  // exit_state stays kStErr
             // A decode from a guessed state met an invalid symbol: start again one bit
             // later; what came before cannot lead to the exit, so its checkpoints go.
@@ -235,16 +232,22 @@ __global__ void __launch_bounds__(kSliceThreads) slice_spec_kernel(JpegLaunch L)
             blocks = 0;
 #pragma unroll
             for (int c = 0; c < 4; c++) dc[c] = 0;
+            dcv = 0;
             k = 1;
             si = 0;
             tb = block_tabs(L, F, si);
             bits_init(r, F.tok, tokbit + p0 + pr + 1, pr + 1);
             continue;
         }
-        k = 0;  // block complete
+        dcv = k0 == 0 ? val : dcv;
+        if (k < 64) continue;
+        add_dc(dc, tb.comp, dcv);  // block complete
+        dcv = 0;
+        k = 0;
         si = si + 1 == F.sched_len ? 0 : si + 1;
         tb = block_tabs(L, F, si);
     }
+    add_dc(dc, tb.comp, dcv);  // the block in progress is counted, with its DC if decoded
     if (guess) {
         for (uint32_t x = 0; x < (uint32_t)kSliceCheckpoints; x++)
             if (!(recorded & (1u << x))) sp->cp[x].state = kStErr;
@@ -295,10 +298,12 @@ __device__ bool resync_slice(const JpegLaunch &L, uint32_t slot, const SliceRef 
     BlockTabs tb = block_tabs(L, F, si);
     uint32_t blocks = 0;
     int32_t dc[4] = {0, 0, 0, 0};
+    int32_t dcv = 0;
     const SliceSpec *sp = L.spec + slot;
     const uint32_t step = S / (kSliceCheckpoints + 1);
     uint32_t q = 0;
     while (q < (uint32_t)kSliceCheckpoints && (q + 1) * step <= rel) q++;  // marks already behind
+    uint32_t next_mark = q < (uint32_t)kSliceCheckpoints ? (q + 1) * step : 0xffffffffu;
     unsigned long long exit_state = kStErr;
     for (;;) {
         const uint32_t pr = r.used;
@@ -307,37 +312,42 @@ __device__ bool resync_slice(const JpegLaunch &L, uint32_t slot, const SliceRef 
             exit_state = pack_state(p0 + pr, si, k);
             break;
         }
-        bool matched = false;
-        while (q < (uint32_t)kSliceCheckpoints && pn >= (q + 1) * step) {
-            const unsigned long long cs = sp->cp[q].state;
-            if (cs != kStErr && cs == pack_state(p0 + pr, si, k)) {
-                const SlicePoint cp = sp->cp[q], e = sp->exit;
-                exit_state = e.state;
-                blocks += e.blocks - cp.blocks;
+        if (pn >= next_mark) {
+            bool matched = false;
+            while (q < (uint32_t)kSliceCheckpoints && pn >= (q + 1) * step) {
+                const unsigned long long cs = sp->cp[q].state;
+                if (cs != kStErr && cs == pack_state(p0 + pr, si, k)) {
+                    // the rest of the slice is the speculative decode's: take its tail
+                    const SlicePoint cp = sp->cp[q], e = sp->exit;
+                    exit_state = e.state;
+                    add_dc(dc, tb.comp, dcv);
+                    dcv = 0;
+                    blocks += e.blocks - cp.blocks;
 #pragma unroll
-                for (int c = 0; c < 4; c++) dc[c] += e.dc[c] - cp.dc[c];
-                matched = true;
-                break;
+                    for (int c = 0; c < 4; c++) dc[c] += e.dc[c] - cp.dc[c];
+                    matched = true;
+                    break;
+                }
+                q++;
             }
-            q++;
+            if (matched) break;
+            next_mark = q < (uint32_t)kSliceCheckpoints ? (q + 1) * step : 0xffffffffu;
         }
-        if (matched) break;
-        if (k == 0) blocks++;
-        int at;
+        const int k0 = k;
+        blocks += k0 == 0;
         int32_t val;
         uint16_t err;
         uint32_t eb;
-        const int sy = next_symbol(r, lim - pr, k == 0 ? tb.dc : tb.ac, L.symbols, k, at, val, err, eb);
-        if (sy == kSymDc) {
-            add_dc(dc, tb.comp, val);
-            continue;
-        }
-        if (sy == kSymRun || (sy == kSymAc && k < 64)) continue;
-        if (sy == kSymError) break;  // exit_state stays kStErr
+        if (!decode_symbol(r, lim - pr, k0 == 0 ? tb.dc : tb.ac, L.symbols, k, val, err, eb)) break;
+        dcv = k0 == 0 ? val : dcv;
+        if (k < 64) continue;
+        add_dc(dc, tb.comp, dcv);
+        dcv = 0;
         k = 0;
         si = si + 1 == F.sched_len ? 0 : si + 1;
         tb = block_tabs(L, F, si);
     }
+    add_dc(dc, tb.comp, dcv);
     out.exit = exit_state;
     out.blocks = blocks;
 #pragma unroll
@@ -480,17 +490,13 @@ __global__ void __launch_bounds__(kSliceThreads) slice_decode_kernel(JpegLaunch 
     bits_init(r, F.tok, (uint64_t)s.v.start * 8 + p0, 0);
     int k = (int)(from & 0xff);
     uint32_t si = (uint32_t)(from >> 8) & 0xff;
-    int at;
     int32_t val;
     uint16_t err;
     uint32_t eb;
     if (k != 0) {  // the block straddling the start belongs to an earlier slice
         const HuffLut *acl = block_tabs(L, F, si).ac;
-        for (;;) {
-            const int sy = next_symbol(r, lim - r.used, acl, L.symbols, k, at, val, err, eb);
-            if (sy == kSymError) return;
-            if (k == 64) break;
-        }
+        while (k < 64)
+            if (!decode_symbol(r, lim - r.used, acl, L.symbols, k, val, err, eb)) return;
         si = si + 1 == sched_len ? 0 : si + 1;
         k = 0;
     }
@@ -505,7 +511,7 @@ __global__ void __launch_bounds__(kSliceThreads) slice_decode_kernel(JpegLaunch 
     const uint32_t bend = P.base + nown;
     const HuffLut *dcl, *acl;
     uint64_t blk;
-    int32_t q0, dq = 0;
+    int32_t q0;
     uint32_t comp;
     const JBlockRec *recs = L.brec + F.sched_off;
     auto setup = [&]() {
@@ -517,24 +523,34 @@ __global__ void __launch_bounds__(kSliceThreads) slice_decode_kernel(JpegLaunch 
         q0 = R.q0;
     };
     setup();
-    uint32_t sym_at = r.used;  // start of the symbol being decoded
+    // The DC difference is staged at zigzag index 0 like a level and turned into the
+    // dequantised DC when the block completes; an error inside the block first
+    // settles the DC checks the reference makes right after the DC symbol.
+    uint32_t blk_at = r.used;  // start of the block's DC symbol
+    uint32_t dc_end = 0;       // reader position after the DC difference
     for (;;) {
-        sym_at = r.used;
-        const int sy = next_symbol(r, lim - r.used, k == 0 ? dcl : acl, L.symbols, k, at, val, err, eb);
+        const uint32_t sym_at = r.used;
+        const int k0 = k;
+        const bool ok = decode_symbol(r, lim - sym_at, k0 == 0 ? dcl : acl, L.symbols, k, val, err, eb);
+        if (ok) {
+            stage[s_zz[k - 1]] = (int16_t)val;
+            dc_end = k0 == 0 ? r.used : dc_end;
+            if (k < 64) continue;
+        }
+        // block complete, or an error: the block's DC checks (decoder.rs:507-515) first
         uint16_t kind = kDiagNone;
-        uint32_t errpos = 0;
-        if (sy == kSymError) {
-            kind = err;
-            errpos = eb;
-        } else if (sy == kSymDc) {  // decoder.rs:507-515
+        uint32_t errpos = 0, ev_at = sym_at;
+        int32_t dq = 0;
+        if (ok || k0 > 0) {
             long long pc = 0;
 #pragma unroll
             for (int c = 0; c < 4; c++)
                 if (comp == (uint32_t)c) pc = pred[c];
-            const long long pn = pc + val;
+            const long long pn = pc + stage[0];
             if (pn > INT32_MAX || pn < INT32_MIN) {
                 kind = kJDcPredOverflow;
-                errpos = r.used;
+                errpos = dc_end;
+                ev_at = blk_at;
             } else {
 #pragma unroll
                 for (int c = 0; c < 4; c++)
@@ -542,14 +558,15 @@ __global__ void __launch_bounds__(kSliceThreads) slice_decode_kernel(JpegLaunch 
                 const long long d = pn * (long long)q0;
                 if (d > INT32_MAX || d < INT32_MIN) {
                     kind = kJDcDeqOverflow;
-                    errpos = r.used;
+                    errpos = dc_end;
+                    ev_at = blk_at;
                 }
                 dq = (int32_t)d;
             }
-            if (kind == kDiagNone) continue;
-        } else {
-            if (sy == kSymAc) stage[s_zz[at]] = (int16_t)val;
-            if (k < 64) continue;
+        }
+        if (kind == kDiagNone && !ok) {
+            kind = err;
+            errpos = eb;
         }
         if (kind != kDiagNone) {
             Diag d;
@@ -560,10 +577,9 @@ __global__ void __launch_bounds__(kSliceThreads) slice_decode_kernel(JpegLaunch 
             } else {
                 d = make_diag(kind, s.v.start + (uint32_t)((p0 + errpos + 7) / 8));
             }
-            report(L, s, slot, p0 + sym_at, d, 0);
+            report(L, s, slot, p0 + ev_at, d, 0);
             return;
         }
-        // block complete
         int4 *dst = reinterpret_cast<int4 *>(L.coef + blk * 64);
 #pragma unroll
         for (int q = 0; q < 8; q++) {
@@ -586,6 +602,7 @@ __global__ void __launch_bounds__(kSliceThreads) slice_decode_kernel(JpegLaunch 
         }
         setup();
         k = 0;
+        blk_at = r.used;
     }
 }
 

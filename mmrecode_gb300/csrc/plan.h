@@ -12,14 +12,15 @@ namespace mmr {
 // maxcode/valptr (JPEG Annex F.2.2.3), which for canonical codes finds the same
 // code as the reference's length-by-length search.
 constexpr int kHuffFastBits = 11;
-enum : uint32_t { kFastCoef = 0, kFastEob = 1, kFastZrl = 2 };
+constexpr uint32_t kFastEob = 1u << 12;
 
 struct HuffLut {
     uint16_t fast[512];    // (length << 8) | symbol; 0 when the code is longer than 9 bits or absent
-    // Whole symbols within the next 11 bits: value << 16 | kind << 13 | size << 9 |
-    // run << 5 | total bits (code + magnitude). DC lookups hold differences of size
-    // 0..11; AC lookups levels of size 1..10 (kFastCoef), EOB and ZRL. 0: slow path
-    // (longer symbols, and every symbol the reference rejects).
+    // Whole symbols within the next 11 bits: value << 16 | eob << 12 | advance << 5 |
+    // total bits (code + magnitude). advance moves the coefficient index k: 1 for a
+    // DC difference (size 0..11), run + 1 for an AC level (size 1..10), 16 for ZRL;
+    // EOB sets k to 64. 0: slow path (longer symbols, and every symbol the
+    // reference rejects).
     uint32_t fastv[1 << kHuffFastBits];
     int32_t maxcode[18];   // largest code of each length 1..16, -1 if none
     int32_t valptr[18];    // symbol index of a length's first code, minus that code
