@@ -758,6 +758,8 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
         std::vector<RgbJob> rgbjobs;
         std::vector<uint64_t> rgbfirst(1, 0);
         std::vector<uint32_t> rgbcta(1, 0);
+        std::vector<FusedJob> fjobs[3];
+        std::vector<uint32_t> fcta[3] = {{0}, {0}, {0}};
         std::map<std::vector<uint8_t>, uint32_t> lut_index;
         std::vector<uint32_t> item_ok(n, 1);
         size_t in_bytes = 0, tok_bytes = 0, planes_bytes = 0, out_bytes = 0;
@@ -883,7 +885,23 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
                 }
                 F.blk_off = blocks;
                 F.n_blocks = p.n_blocks;
-                for (uint32_t c = 0; c < p.ncomp; c++) {
+                // RGB straight from coefficients for the standard MCU layouts
+                int fused_v = -1;
+                if (can_output && it.output == kOutRgb24 && p.fmt != kGray8 && p.ncomp == 3 && p.interleaved &&
+                    p.comps[0].h == p.hmax && p.comps[0].v == p.vmax && p.comps[1].h == 1 && p.comps[1].v == 1 &&
+                    p.comps[2].h == 1 && p.comps[2].v == 1)
+                    fused_v = fused_variant(p.hmax, p.vmax);
+                if (fused_v >= 0) {
+                    FusedJob fj;
+                    memset(&fj, 0, sizeof(fj));
+                    fj.frame = (uint32_t)jframes.size();
+                    fj.strips_x = fused_strips_x(fused_v, p.mcu_cols);
+                    fj.width = p.W;
+                    fj.height = p.H;
+                    fjobs[fused_v].push_back(fj);
+                    fcta[fused_v].push_back(fcta[fused_v].back() + fj.strips_x * p.mcu_rows);
+                }
+                for (uint32_t c = 0; c < p.ncomp && fused_v < 0; c++) {
                     JBlockRange r;
                     r.first = blocks + p.comps[c].blk_base;
                     r.frame = (uint32_t)jframes.size();
@@ -896,14 +914,14 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
                 blocks += p.n_blocks;
                 // planes: straight into a device output, else scratch
                 bool direct = can_output && it.output == kOutPlanar;
-                if (!direct) {
+                if (!direct && fused_v < 0) {
                     planes_off[i] = planes_bytes;
                     planes_bytes = align_up(planes_bytes + p.planar_bytes, 256);
                 }
                 F.item_base = 0;  // set below
                 auto &lst = p.ncomp <= 4 ? items_small : items_big;
                 for (uint32_t v = 0; v < p.n_intervals; v++) lst.push_back(make_uint2((uint32_t)jframes.size(), v));
-                if (can_output && it.output == kOutRgb24) {
+                if (can_output && it.output == kOutRgb24 && fused_v < 0) {
                     RgbJob J;
                     memset(&J, 0, sizeof(J));
                     J.w = p.W;
@@ -1062,6 +1080,8 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
             J.planes = planes_ptr(J.item);
             J.out = out_ptr(J.item);
         }
+        for (auto &list : fjobs)
+            for (auto &J : list) J.out = out_ptr(jframes[J.frame].item);
 
         // ------------------------------------------------------ plan blob
         size_t o_jframes = blob.add_vec(jframes), o_jstates = blob.add_vec(jstates),
@@ -1073,6 +1093,11 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
                o_dframes = blob.add_vec(dframes), o_dstates = blob.add_vec(dstates), o_segfirst = blob.add_vec(seg_first),
                o_diffirst = blob.add_vec(dif_first), o_rgbjobs = blob.add_vec(rgbjobs),
                o_rgbcta = blob.add_vec(rgbcta);
+        size_t o_fjobs[3], o_fcta[3];
+        for (int v = 0; v < 3; v++) {
+            o_fjobs[v] = blob.add_vec(fjobs[v]);
+            o_fcta[v] = blob.add_vec(fcta[v]);
+        }
         uint32_t zero_counters[2] = {0, 0};
         size_t o_fixcount = blob.add(zero_counters, 8);
         uint32_t zero_dirty[kSyncPasses] = {};
@@ -1143,8 +1168,17 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
             launch_jpeg_entropy(JL, s);
             MMR_CUDA(cudaEventRecord(I.ev[3], s));
             launch_jpeg_idct(JL, s);
+            FusedLaunch FL[3];
+            for (int v = 0; v < 3; v++) {
+                FL[v].jobs = reinterpret_cast<const FusedJob *>(db + o_fjobs[v]);
+                FL[v].cta_first = reinterpret_cast<const uint32_t *>(db + o_fcta[v]);
+                FL[v].n_jobs = (uint32_t)fjobs[v].size();
+                FL[v].n_ctas = fcta[v].back();
+                launches_ += FL[v].n_ctas ? 1 : 0;
+            }
+            launch_jpeg_idct_rgb(JL, FL, s);
             launches_ += (JL.n_tiles ? 3 : 0) + (JL.n_slots ? jpeg_slice_launches(JL) : 0) +
-                         (n_items > JL.n_items_small ? 1 : 0) + 1 + (blocks ? 2 : 0);
+                         (n_items > JL.n_items_small ? 1 : 0) + 1 + (JL.n_idct_ctas ? 2 : 0);
         } else {
             MMR_CUDA(cudaEventRecord(I.ev[2], s));
             MMR_CUDA(cudaEventRecord(I.ev[3], s));

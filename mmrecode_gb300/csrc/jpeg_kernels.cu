@@ -15,13 +15,13 @@
 #include <cuda_runtime.h>
 
 #include "entropy_core.h"
+#include "idct_core.h"
 #include "kernels.h"
 #include "tables.h"
 
 namespace mmr {
 
 __constant__ int c_zigzag[64] = MMR_ZIGZAG_INIT;
-__constant__ double c_idct[64] = MMR_IDCT_MATRIX_INIT;
 
 namespace {
 
@@ -115,6 +115,19 @@ __device__ __forceinline__ TileRef tile_ref(const JpegLaunch &L, uint32_t t) {
     return r;
 }
 
+// True when the 16 bytes at p (p >= data_start, p + 16 <= len) hold no 0xFF and the
+// byte before them is not 0xFF: then all 16 are plain data bytes. Loads the bytes
+// into *v (one 16-byte load when the packet is 16-byte aligned).
+__device__ __forceinline__ bool plain_chunk(const uint8_t *in, uint32_t ds, uint32_t p, uint4 *v) {
+    if ((((uintptr_t)in) & 15) != 0) return false;
+    *v = *reinterpret_cast<const uint4 *>(in + p);
+    const uint32_t w[4] = {v->x, v->y, v->z, v->w};
+    bool ff = p > ds && in[p - 1] == 0xff;
+#pragma unroll
+    for (int i = 0; i < 4; i++) ff |= __vcmpeq4(w[i], 0xffffffffu) != 0;
+    return !ff;
+}
+
 __global__ void __launch_bounds__(kScanThreads) scan_count_kernel(JpegLaunch L) {
     uint32_t t = blockIdx.x;
     TileRef tr = tile_ref(L, t);
@@ -124,7 +137,10 @@ __global__ void __launch_bounds__(kScanThreads) scan_count_kernel(JpegLaunch L) 
     uint32_t p0 = tr.base + threadIdx.x * 16;
     uint32_t tokens = 0, rsts = 0;
     unsigned long long term = ~0ull;
-    if (p0 < len) {
+    uint4 v;
+    if (p0 >= ds && p0 + 16 <= len && plain_chunk(in, ds, p0, &v)) {
+        tokens = 16;
+    } else if (p0 < len) {
         bool prev_ff = p0 > ds && in[p0 - 1] == 0xff;
 #pragma unroll 4
         for (int k = 0; k < 16; k++) {
@@ -190,6 +206,8 @@ __global__ void __launch_bounds__(256) scan_prefix_kernel(JpegLaunch L) {
 }
 
 __global__ void __launch_bounds__(kScanThreads) scan_emit_kernel(JpegLaunch L) {
+    // tokens of this tile, staged at their destination's offset within a 16-byte line
+    __shared__ __align__(16) uint8_t s_tok[kScanTile + 32];
     uint32_t t = blockIdx.x;
     TileRef tr = tile_ref(L, t);
     const JFrame &F = L.frames[tr.frame];
@@ -202,46 +220,73 @@ __global__ void __launch_bounds__(kScanThreads) scan_emit_kernel(JpegLaunch L) {
     uint32_t p0 = tr.base + threadIdx.x * 16;
     uint8_t kinds[16], bytes[16];
     uint32_t tokens = 0, rsts = 0;
-    bool prev_ff = p0 > ds && p0 < len && in[p0 - 1] == 0xff;
+    uint4 v;
+    const bool plain = p0 >= ds && p0 + 16 <= term && plain_chunk(in, ds, p0, &v);
+    if (plain) {
+        tokens = 16;
+    } else {
+        bool prev_ff = p0 > ds && p0 < len && in[p0 - 1] == 0xff;
 #pragma unroll
-    for (int k = 0; k < 16; k++) {
-        uint32_t p = p0 + k;
-        kinds[k] = kByteNone;
-        bytes[k] = 0;
-        if (p < ds || p >= term) continue;
-        uint8_t b = in[p];
-        uint32_t code = 0;
-        int kind = classify(in, len, p, b, prev_ff, &code);
-        kinds[k] = (uint8_t)kind;
-        bytes[k] = kind == kByteRst ? (uint8_t)(code - 0xd0) : b;
-        tokens += (kind == kBytePlain || kind == kByteStuffed);
-        rsts += kind == kByteRst;
-        prev_ff = b == 0xff;
+        for (int k = 0; k < 16; k++) {
+            uint32_t p = p0 + k;
+            kinds[k] = kByteNone;
+            bytes[k] = 0;
+            if (p < ds || p >= term) continue;
+            uint8_t b = in[p];
+            uint32_t code = 0;
+            int kind = classify(in, len, p, b, prev_ff, &code);
+            kinds[k] = (uint8_t)kind;
+            bytes[k] = kind == kByteRst ? (uint8_t)(code - 0xd0) : b;
+            tokens += (kind == kBytePlain || kind == kByteStuffed);
+            rsts += kind == kByteRst;
+            prev_ff = b == 0xff;
+        }
     }
     uint32_t etok, erst, ttok, trst;
     block_excl_scan2<kScanThreads>(tokens, rsts, etok, erst, ttok, trst);
-    uint32_t tok_pos = L.tile_tok[t] + etok;
-    uint32_t rst_idx = L.tile_rst[t] + erst;
-    RstEntry *rst = L.rsts + F.rst_off;
+    const uint32_t tile_tok = L.tile_tok[t];
+    const uint32_t mis = (uint32_t)((uintptr_t)(F.tok + tile_tok) & 15);
+    uint8_t *st = s_tok + mis + etok;
+    if (plain) {
+        const uint32_t w[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-    for (int k = 0; k < 16; k++) {
-        int kind = kinds[k];
-        if (kind == kBytePlain) F.tok[tok_pos++] = bytes[k];
-        else if (kind == kByteStuffed) F.tok[tok_pos++] = 0xff;
-        else if (kind == kByteRst) {
-            if (rst_idx < F.n_intervals) {
-                RstEntry e;
-                e.tok = tok_pos;
-                e.number = bytes[k];
-                rst[rst_idx] = e;
+        for (int i = 0; i < 16; i++) st[i] = (uint8_t)(w[i >> 2] >> (8 * (i & 3)));
+    } else {
+        uint32_t tok_pos = tile_tok + etok, n = 0;
+        uint32_t rst_idx = L.tile_rst[t] + erst;
+        RstEntry *rst = L.rsts + F.rst_off;
+#pragma unroll
+        for (int k = 0; k < 16; k++) {
+            int kind = kinds[k];
+            if (kind == kBytePlain) st[n++] = bytes[k];
+            else if (kind == kByteStuffed) st[n++] = 0xff;
+            else if (kind == kByteRst) {
+                if (rst_idx < F.n_intervals) {
+                    RstEntry e;
+                    e.tok = tok_pos + n;
+                    e.number = bytes[k];
+                    rst[rst_idx] = e;
+                }
+                rst_idx++;
             }
-            rst_idx++;
+        }
+    }
+    __syncthreads();
+    // copy out: whole 16-byte lines as vectors, the partial first and last lines by byte
+    uint8_t *dst = F.tok + tile_tok - mis;  // 16-byte aligned
+    const uint32_t span = mis + ttok, lines = (span + 15) / 16;
+    for (uint32_t l = threadIdx.x; l < lines; l += blockDim.x) {
+        const uint32_t b0 = l * 16, b1 = b0 + 16;
+        if (b0 >= mis && b1 <= span) {
+            *reinterpret_cast<uint4 *>(dst + b0) = *reinterpret_cast<const uint4 *>(s_tok + b0);
+        } else {
+            for (uint32_t b = max(b0, mis); b < min(b1, span); b++) dst[b] = s_tok[b];
         }
     }
     // The last tile that starts before the terminator publishes the totals (the
     // terminator may sit exactly on the next tile's first byte).
     if (threadIdx.x == 0 && term <= tr.base + (uint32_t)kScanTile) {
-        L.states[tr.frame].n_tokens = L.tile_tok[t] + ttok;
+        L.states[tr.frame].n_tokens = tile_tok + ttok;
         L.states[tr.frame].n_rst = L.tile_rst[t] + trst;
     }
 }
@@ -396,52 +441,7 @@ __global__ void resolve_kernel(JpegLaunch L) {
 }
 
 // ---------------------------------------------------------------- IDCT ----
-//
-// transform.rs:86-109 computes, in binary64 and in this order,
-//   t[v][x] = sum_u M[x][u] * c[v][u]            (from 0.0, u = 0..7)
-//   s[y][x] = sum_v M[y][v] * t[v][x]            (from 0.0, v = 0..7)
-//   sample  = clamp(round_half_away(s + 128.0), 0, 255)
-// GB300 issues binary64 at a small fraction of its fp32 rate, so every sample
-// is first computed in fp32 and kept only when it provably rounds like the
-// binary64 value:
-//   S  = sum_v sum_u M[y][v] M[x][u] c[v][u]   (exact real value, double M)
-//   B  = sum_v sum_u |M[y][v]| |M[x][u]| |c[v][u]|  <=  Mmax^2 * C1,
-//        C1 = sum |c|, Mmax = max |M| = 0.49039264 (Mmax^2 < 0.2405)
-//   fp32 path (M and c rounded to fp32, FMA accumulation, u = 2^-24):
-//        |s32 - S| <= (2u + 8u) + (u + 8u) ... = 19u * B + O(u^2) B   (pass 1 error
-//        10u A with A = sum_u |M||c|, propagated through pass 2, plus pass 2's
-//        own 8u; standard recursive-summation bounds, Higham ch. 3)
-//   binary64 reference: |s64 - S| <= 16 * 2^-53 * B, and its +128.0 rounds
-//        by at most 2^-53 |s + 128|.
-// With delta = 2^-21 * C1 + 2^-40 |s32| + 2^-30 (2^-21 * C1 >= 19u * 0.2405 C1
-// with 1.7x margin), if no half-integer lies within delta of s32 + 128 both
-// values round to the same integer; samples certain to clamp are kept too.
-// Every other sample is queued and recomputed in the exact reference order by
-// fixup_kernel (or in place when the queue is full). Zero coefficients are
-// skipped in the exact path: a zero term adds +-0.0, which leaves any sum that
-// is not -0.0 unchanged, and these sums are never -0.0.
-
-__constant__ float c_idct32[64] = MMR_IDCT_MATRIX_INIT;
-
-__device__ __forceinline__ uint8_t exact_sample(const int32_t *c, int stride, int y, int x) {
-    double t[8];
-#pragma unroll
-    for (int v = 0; v < 8; v++) {
-        double acc = 0.0;
-#pragma unroll
-        for (int u = 0; u < 8; u++) {
-            int32_t cv = c[v * stride + u];
-            if (cv) acc = __dadd_rn(acc, __dmul_rn(c_idct[x * 8 + u], (double)cv));
-        }
-        t[v] = acc;
-    }
-    double acc = 0.0;
-#pragma unroll
-    for (int v = 0; v < 8; v++)
-        if (t[v] != 0.0) acc = __dadd_rn(acc, __dmul_rn(c_idct[y * 8 + v], t[v]));
-    double px = round(__dadd_rn(acc, 128.0));
-    return (uint8_t)fmin(fmax(px, 0.0), 255.0);
-}
+// (the transform core and its exactness bound live in idct_core.h)
 
 constexpr int kIdctBlocks = 64;  // blocks per CTA, all of one (frame, component) range
 constexpr int kIdctThreads = kIdctBlocks * 4;
@@ -456,111 +456,6 @@ __device__ __forceinline__ uint32_t find_range(const JpegLaunch &L, uint64_t g) 
         else hi = mid;
     }
     return lo;
-}
-
-// Dequantises block g into fp32 rows q and q+4 of `blk` (the product of an
-// int16 level and an 8-bit quantiser is exact in fp32; the DC is the decoder's
-// dequantised int32, rounded to fp32 like every c in the bound). Returns the
-// sum of |c| over the two rows.
-__device__ __forceinline__ float stage_rows(const JpegLaunch &L, uint64_t g, uint32_t q, const float *Qf, float *blk) {
-    const int4 *src = reinterpret_cast<const int4 *>(L.coef + g * 64);
-    float l1 = 0.0f;
-#pragma unroll
-    for (int h = 0; h < 2; h++) {
-        const int row = q + 4 * h;
-        const int4 v = src[row];
-        const int16_t *lv = reinterpret_cast<const int16_t *>(&v);
-        const float4 qa = reinterpret_cast<const float4 *>(Qf + row * 8)[0];
-        const float4 qb = reinterpret_cast<const float4 *>(Qf + row * 8)[1];
-        const float qv[8] = {qa.x, qa.y, qa.z, qa.w, qb.x, qb.y, qb.z, qb.w};
-        float f[8];
-#pragma unroll
-        for (int j = 0; j < 8; j++) f[j] = (float)lv[j] * qv[j];
-        if (row == 0) f[0] = (float)L.dc[g];
-#pragma unroll
-        for (int j = 0; j < 8; j++) l1 += fabsf(f[j]);
-        reinterpret_cast<float4 *>(blk + row * 8)[0] = make_float4(f[0], f[1], f[2], f[3]);
-        reinterpret_cast<float4 *>(blk + row * 8)[1] = make_float4(f[4], f[5], f[6], f[7]);
-    }
-    return l1;
-}
-
-// Sample of an fp32 transform value. Rounding it provably equals rounding the
-// binary64 value when no half-integer lies within delta of acc, i.e. when acc
-// is closer than 0.5 - delta to its nearest integer (with delta >= 0.5 nothing
-// is certain); the exact pass settles the rest, ties included, so rintf's
-// ties-to-even never decides a sample. Clamping after an agreed rounding agrees.
-__device__ __forceinline__ uint32_t round_sample(float acc, float near, bool &unsure) {
-    const float r = rintf(acc);
-    unsure = !(fabsf(acc - r) < near);
-    return (uint32_t)fminf(fmaxf(r + 128.0f, 0.0f), 255.0f);
-}
-
-// Transform of one staged block by its four threads; thread q produces output
-// columns q and 7 - q into out[row * stride + col]. Both passes use the even/odd
-// split of the basis: M[7-x][u] = (-1)^u M[x][u] holds for the fp32 roundings of
-// the reference's literals (the literals themselves differ from exact symmetry by
-// < 2e-15, far inside the fp32 rounding), so
-//   s[x] = E + O, s[7-x] = E - O,  E = sum_{u even} M[x][u] c[u], O = sum_{u odd}.
-// Per output this is 4 FMAs per half and one add: each pass's error is <= 5u of
-// the sum of |terms|, plus u for each rounded M and c, <= 13u B after both
-// passes, inside the 19u B the decision bound allows. |s| <= Mmax^2 C1 < C1/4, so
-// the relative term 2^-40 |s| of the bound is folded into 2^-42 C1.
-// Returns the samples left to the exact pass as bits (row * 8 + column).
-__device__ __forceinline__ unsigned long long idct_block(const float *blk, uint32_t q, float c1, uint8_t *out,
-                                                         int stride) {
-    float mq[8];
-#pragma unroll
-    for (int u = 0; u < 8; u++) mq[u] = c_idct32[q * 8 + u];
-    float ta[8], tb[8];
-#pragma unroll
-    for (int v = 0; v < 8; v++) {
-        const float4 c0 = reinterpret_cast<const float4 *>(blk + v * 8)[0];
-        const float4 c1v = reinterpret_cast<const float4 *>(blk + v * 8)[1];
-        float e = c0.x * mq[0];
-        e = fmaf(mq[2], c0.z, e);
-        e = fmaf(mq[4], c1v.x, e);
-        e = fmaf(mq[6], c1v.z, e);
-        float o = c0.y * mq[1];
-        o = fmaf(mq[3], c0.w, o);
-        o = fmaf(mq[5], c1v.y, o);
-        o = fmaf(mq[7], c1v.w, o);
-        ta[v] = e + o;
-        tb[v] = e - o;
-    }
-    // 2^-21 C1 >= 19u Mmax^2 C1 with a 1.75x margin
-    const float near = 0.5f - (c1 * (0x1p-21f + 0x1p-42f) + 0x1p-30f);
-    uint32_t bits = 0;  // bit 2*row (column q), 2*row+1 (column 7-q)
-#pragma unroll
-    for (int y = 0; y < 4; y++) {
-#pragma unroll
-        for (int side = 0; side < 2; side++) {
-            const float *t = side ? tb : ta;
-            float e = t[0] * c_idct32[y * 8 + 0];
-            e = fmaf(c_idct32[y * 8 + 2], t[2], e);
-            e = fmaf(c_idct32[y * 8 + 4], t[4], e);
-            e = fmaf(c_idct32[y * 8 + 6], t[6], e);
-            float o = t[1] * c_idct32[y * 8 + 1];
-            o = fmaf(c_idct32[y * 8 + 3], t[3], o);
-            o = fmaf(c_idct32[y * 8 + 5], t[5], o);
-            o = fmaf(c_idct32[y * 8 + 7], t[7], o);
-            const uint32_t col = side ? 7 - q : q;
-            bool u0, u1;
-            out[y * stride + col] = (uint8_t)round_sample(e + o, near, u0);
-            out[(7 - y) * stride + col] = (uint8_t)round_sample(e - o, near, u1);
-            bits |= (u0 ? 1u : 0u) << (2 * y + side);
-            bits |= (u1 ? 1u : 0u) << (2 * (7 - y) + side);
-        }
-    }
-    unsigned long long mask = 0;
-    if (bits) {
-#pragma unroll
-        for (int row = 0; row < 8; row++) {
-            if (bits & (1u << (2 * row))) mask |= 1ull << (row * 8 + q);
-            if (bits & (2u << (2 * row))) mask |= 1ull << (row * 8 + 7 - q);
-        }
-    }
-    return mask;
 }
 
 // Planar output: a CTA transforms 64 blocks of one (frame, component) range, four
@@ -593,7 +488,7 @@ __global__ void __launch_bounds__(kIdctThreads, 4) idct_kernel(JpegLaunch L) {
     const bool valid = local < nblk;
     const uint64_t g = R.first + local;
     float *blk = s_f + lb * kIdctStride;
-    float l1 = valid ? stage_rows(L, g, q, s_q, blk) : 0.0f;
+    float l1 = valid ? stage_rows(L.coef, L.dc, g, q, s_q, blk) : 0.0f;
 #pragma unroll
     for (int o = 1; o < 4; o <<= 1) l1 += __shfl_xor_sync(0xffffffffu, l1, o);
     __syncwarp();

@@ -62,6 +62,26 @@ int jpeg_slice_launches(const JpegLaunch &L);
 void launch_jpeg_idct(const JpegLaunch &L, cudaStream_t s);
 uint32_t idct_ctas(uint32_t blocks);
 
+// MJPEG frames decoded straight to RGB24 (three components, chroma 1x1, luma
+// 1x1, 2x1 or 2x2): one launch per layout, a CTA per strip of MCUs.
+struct FusedJob {
+    uint32_t frame;     // JFrame index
+    uint32_t strips_x;  // strips per MCU row
+    uint32_t width, height;
+    uint8_t *out;       // width * height * 3 bytes
+};
+
+struct FusedLaunch {
+    const FusedJob *jobs;
+    const uint32_t *cta_first;  // n_jobs + 1 prefix of CTAs (strips_x * mcu_rows per job)
+    uint32_t n_jobs;
+    uint32_t n_ctas;
+};
+
+int fused_variant(uint32_t hmax, uint32_t vmax);  // 0: 1x1, 1: 2x1, 2: 2x2, -1: not fused
+uint32_t fused_strips_x(int variant, uint32_t mcu_cols);
+void launch_jpeg_idct_rgb(const JpegLaunch &L, const FusedLaunch *FL, cudaStream_t s);  // FL[3]
+
 struct DvLaunch {
     const DvFrame *frames;
     DvState *states;

@@ -84,3 +84,32 @@ def test_unaligned_device_destinations(ctx):
         assert host[offs[i]:offs[i] + needs[i]] == oracle.rgb24(ref.frame), i
         assert host[prev_end:offs[i]] == bytes(offs[i] - prev_end), f"bytes before item {i} were written"
         prev_end = offs[i] + needs[i]
+
+
+def _dc_frame(hm, vm, mcus_x, mcus_y, values):
+    """Three-component frame of DC-only blocks; values cycles through dequantised DCs
+    (4 mod 8 gives a sample exactly halfway between two integers)."""
+    from helpers import encode_blocks, jpeg, stuff
+    comps = [(1, hm, vm, 0), (2, 1, 1, 0), (3, 1, 1, 0)]
+    pred = [0, 0, 0]
+    blocks, k = [], 0
+    for _ in range(mcus_x * mcus_y):
+        for c, n in ((0, hm * vm), (1, 1), (2, 1)):
+            for _ in range(n):
+                d = values[k % len(values)]
+                k += 1
+                blocks.append((d - pred[c], [(0, (-1) ** k * (k % 5))] if k % 3 == 0 and k % 5 else [], True))
+                pred[c] = d
+    return jpeg(8 * hm * mcus_x, 8 * vm * mcus_y, comps, entropy=stuff(encode_blocks(blocks).raw_bytes()))
+
+
+def test_exact_samples_inside_the_fused_conversion(ctx):
+    values = [4, -4, 12, -1020, 1020, 0, 516, -516, 1, 996, -1004]
+    packets = [_dc_frame(hm, vm, 9, 3, values) for hm, vm in ((1, 1), (2, 1), (2, 2))]
+    results = ctx.decode_batch(packets, m.CODEC_MJPEG, m.OUTPUT_RGB24)
+    for i, (pkt, (r, payload)) in enumerate(zip(packets, results)):
+        ref = oracle.jpeg_decode(pkt)
+        assert ref.status == 0 and r.status == 0, (i, r.message, ref.message)
+        assert payload == oracle.rgb24(ref.frame), i
+    stats = ctx.stats()
+    assert stats["idct_exact_samples"] > 0
