@@ -150,16 +150,18 @@ def _peaks():
         return 6800.0, "fallback"
 
 
-def _traffic_per_block():
-    """DRAM bytes per coefficient block of the transform + colour stage, from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "jpeg_idct_rgb_1080p422.md")
-    try:
-        for line in open(path):
-            if line.startswith("traffic_bytes_per_block:"):
-                return float(line.split(":")[1])
-    except OSError:
-        pass
-    return None
+def _profile_figures():
+    """Per-kernel figures from the committed ncu summaries: lines 'key: kernel value'."""
+    out = {}
+    for name in sorted(os.listdir(os.path.join(ROOT, "profiles"))):
+        try:
+            for line in open(os.path.join(ROOT, "profiles", name)):
+                parts = line.split()
+                if len(parts) == 3 and parts[0] in ("traffic_bytes_per_block:", "issue_active_pct:"):
+                    out[(parts[0][:-1], parts[1])] = float(parts[2])
+        except (OSError, ValueError):
+            pass
+    return out
 
 
 def make_workload(rank: int):
@@ -318,25 +320,35 @@ def main():
     def avg(key):
         return sum(s[key] for s in stages) / len(stages)
     blocks = stages[-1]["jpeg_blocks"]
-    entropy_ms, idct_ms, rgb_ms, scan_ms = avg("entropy_ms"), avg("idct_ms"), avg("rgb_ms"), avg("scan_ms")
     peak, peak_kind = _peaks()
-    transform_bytes = blocks * 128 + n * rgb_bytes
-    entropy_bytes = in_bytes + blocks * 128
+    figures = _profile_figures()
     exact_frac = stages[-1]["idct_exact_samples"] / max(1, blocks * 64)
-    stage_times = {"scan": scan_ms, "entropy": entropy_ms, "idct": idct_ms, "rgb": rgb_ms,
-                   "upload": avg("upload_ms"), "download": avg("download_ms")}
-    if idct_ms + rgb_ms >= entropy_ms:
-        achieved = transform_bytes / ((idct_ms + rgb_ms) / 1e3) / 1e9
-        tpb = _traffic_per_block()
-        roofline = {"bound": "hbm", "kernel": "jpeg idct + rgb (transform/colour stage)", "achieved": achieved,
-                    "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                    "traffic": tpb * blocks if tpb else None,
-                    "algorithmic_bytes_per_launch": transform_bytes}
-    else:
-        achieved = entropy_bytes / (entropy_ms / 1e3) / 1e9
-        roofline = {"bound": "hbm", "kernel": "jpeg entropy (issue-bound; HBM fraction shown)", "achieved": achieved,
-                    "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
-                    "algorithmic_bytes_per_launch": entropy_bytes}
+    stage_times = {k: avg(k + "_ms") for k in ("scan", "entropy", "idct", "rgb", "upload", "download",
+                                              "slice_spec", "slice_sync", "slice_decode")}
+    # algorithmic bytes per launch of each kernel of the step (every kernel runs once per step)
+    kernels = {
+        # reads the compressed tokens, writes 64 int16 levels + one int32 DC per block
+        "slice_decode_kernel": (stage_times["slice_decode"], in_bytes + blocks * 132),
+        # reads the tokens once more (no output beyond per-slice states)
+        "slice_spec_kernel": (stage_times["slice_spec"], in_bytes),
+        # reads levels + DC, writes interleaved RGB
+        "idct_rgb_kernel": (stage_times["idct"], blocks * 132 + n * rgb_bytes),
+    }
+
+    def roof(name):
+        ms, nbytes = kernels[name]
+        achieved = nbytes / (ms / 1e3) / 1e9
+        tpb = figures.get(("traffic_bytes_per_block", name))
+        out = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "peak_kind": peak_kind,
+               "unit": "GB/s", "frac": achieved / peak, "traffic": tpb * blocks if tpb else None,
+               "algorithmic_bytes_per_launch": nbytes, "ms_per_launch": ms}
+        issue = figures.get(("issue_active_pct", name))
+        if issue is not None:
+            out["issue_active_pct_ncu"] = issue
+        return out
+    dominant = max(kernels, key=lambda k: kernels[k][0])
+    roofline = roof(dominant)
+    roofline_transform = roof("idct_rgb_kernel")
 
     cpu = None
     bit_exact = None
@@ -380,6 +392,7 @@ def main():
             "stage_ms": stage_times,
             "idct_exact_sample_fraction": exact_frac,
             "roofline": roofline,
+            "roofline_transform_colour": roofline_transform,
             "cpu_baseline": cpu,
             "bit_exact_sample": bit_exact,
             "gpu_launches": launches,

@@ -112,6 +112,8 @@ typedef struct mmr_gpu_batch_stats {
     uint64_t input_bytes, output_bytes, jpeg_blocks, dv_blocks, rgb_pixels;
     uint64_t idct_exact_samples; /* samples the fp32 IDCT left to the exact binary64 pass */
     uint32_t launches;
+    /* inside entropy_ms: speculative slice decode, slice synchronisation + block prefix, final decode */
+    double slice_spec_ms, slice_sync_ms, slice_decode_ms;
 } mmr_gpu_batch_stats;
 
 MMR_API mmr_status mmr_gpu_last_batch_stats(const mmr_gpu_context *context, mmr_gpu_batch_stats *stats);

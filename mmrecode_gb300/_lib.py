@@ -70,7 +70,8 @@ class BatchStats(ctypes.Structure):
         "total_ms", "upload_ms", "scan_ms", "entropy_ms", "idct_ms", "dv_ms", "rgb_ms", "download_ms")] + [
         (n, ctypes.c_uint64) for n in ("input_bytes", "output_bytes", "jpeg_blocks", "dv_blocks", "rgb_pixels",
                                       "idct_exact_samples")] + [
-        ("launches", ctypes.c_uint32)]
+        ("launches", ctypes.c_uint32)] + [
+        (n, ctypes.c_double) for n in ("slice_spec_ms", "slice_sync_ms", "slice_decode_ms")]
 
 
 class JpegEncodeOptions(ctypes.Structure):

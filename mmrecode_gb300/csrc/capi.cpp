@@ -485,6 +485,9 @@ MMR_API mmr_status mmr_gpu_last_batch_stats(const mmr_gpu_context *context, mmr_
     stats->rgb_pixels = t.rgb_pixels;
     stats->idct_exact_samples = t.idct_exact_samples;
     stats->launches = context->last_launches;
+    stats->slice_spec_ms = t.slice_spec_ms;
+    stats->slice_sync_ms = t.slice_sync_ms;
+    stats->slice_decode_ms = t.slice_decode_ms;
     return finish(MMR_STATUS_OK, "");
 }
 

@@ -671,12 +671,14 @@ struct Engine::Impl {
     std::vector<uint32_t> vlc;
     // stage boundaries: start, uploads, scan, entropy, idct, dv, rgb, end
     cudaEvent_t ev[8] = {};
+    cudaEvent_t marks[3] = {};  // inside the entropy stage
 };
 
 Engine::Engine(int device) : device_(device), slice_bits_(0), impl_(new Impl) {
     MMR_CUDA(cudaSetDevice(device));
     MMR_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
     for (auto &e : impl_->ev) MMR_CUDA(cudaEventCreate(&e));
+    for (auto &e : impl_->marks) MMR_CUDA(cudaEventCreate(&e));
     impl_->vlc = build_dv_vlc();
     impl_->d_vlc.ensure(impl_->vlc.size() * 4);
     MMR_CUDA(cudaMemcpy(impl_->d_vlc.ptr, impl_->vlc.data(), impl_->vlc.size() * 4, cudaMemcpyHostToDevice));
@@ -686,6 +688,8 @@ Engine::~Engine() {
     cudaSetDevice(device_);
     if (stream_) cudaStreamSynchronize(stream_);
     for (auto &e : impl_->ev)
+        if (e) cudaEventDestroy(e);
+    for (auto &e : impl_->marks)
         if (e) cudaEventDestroy(e);
     delete impl_;
     if (stream_) cudaStreamDestroy(stream_);
@@ -760,12 +764,23 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
         std::vector<uint32_t> rgbcta(1, 0);
         std::vector<FusedJob> fjobs[3];
         std::vector<uint32_t> fcta[3] = {{0}, {0}, {0}};
+
         std::map<std::vector<uint8_t>, uint32_t> lut_index;
         std::vector<uint32_t> item_ok(n, 1);
         size_t in_bytes = 0, tok_bytes = 0, planes_bytes = 0, out_bytes = 0;
         uint32_t rst_total = 0;
         uint64_t blocks = 0;
         uint64_t n_slots = 0;
+        // Automatic slice size: about 64k slices over the batch's compressed MJPEG
+        // bits, 1024..4096 bits each (small batches want parallelism, large ones
+        // fewer slice boundaries).
+        uint32_t auto_bits = 1024;
+        {
+            uint64_t total_bits = 0;
+            for (size_t i = 0; i < n; i++)
+                if (items[i].codec == kCodecMjpeg) total_bits += 8 * (uint64_t)items[i].len;
+            while (auto_bits < 4096 && (uint64_t)auto_bits * 2 * 65536 <= total_bits) auto_bits *= 2;
+        }
         std::vector<size_t> in_off(n, 0), out_off(n, 0), planes_off(n, SIZE_MAX);
         std::vector<std::array<size_t, 6>> plane_geom(n);  // (offset, bytes) of up to 3 planes
         // per JPEG plan: JFrame index (or -1)
@@ -877,7 +892,7 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
                 F.rst_off = rst_total;
                 rst_total += p.n_intervals;
                 if (p.ncomp <= 4) {
-                    const uint32_t slice_bits = slice_bits_ ? slice_bits_ : kSliceBitsDefault;
+                    const uint32_t slice_bits = slice_bits_ ? slice_bits_ : auto_bits;
                     F.slice_bits = slice_bits;
                     F.slot_first = (uint32_t)n_slots;
                     F.slot_count = (uint32_t)((8 * (uint64_t)it.len + slice_bits - 1) / slice_bits + p.n_intervals);
@@ -900,6 +915,7 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
                     fj.height = p.H;
                     fjobs[fused_v].push_back(fj);
                     fcta[fused_v].push_back(fcta[fused_v].back() + fj.strips_x * p.mcu_rows);
+
                 }
                 for (uint32_t c = 0; c < p.ncomp && fused_v < 0; c++) {
                     JBlockRange r;
@@ -1049,6 +1065,7 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
         // samples the fp32 IDCT leaves to the exact pass: expected ~0.1 per block; when the
         // queue fills, the kernel recomputes in place instead
         I.d_fix.ensure(std::max<size_t>(blocks * 16, 256));
+
         if (n_slots > 0xffffffffull) throw std::runtime_error("batch too large for the chunked entropy decoder");
         I.d_slot_item.ensure(std::max<size_t>(n_slots * 4, 256));
         I.d_sync.ensure(std::max<size_t>(n_slots * sizeof(SliceSync), 256));
@@ -1098,6 +1115,7 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
             o_fjobs[v] = blob.add_vec(fjobs[v]);
             o_fcta[v] = blob.add_vec(fcta[v]);
         }
+
         uint32_t zero_counters[2] = {0, 0};
         size_t o_fixcount = blob.add(zero_counters, 8);
         uint32_t zero_dirty[kSyncPasses] = {};
@@ -1164,7 +1182,7 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
         if (!jframes.empty()) {
             launch_jpeg_scan(JL, s);
             MMR_CUDA(cudaEventRecord(I.ev[2], s));
-            launch_jpeg_slices(JL, s);
+            launch_jpeg_slices(JL, s, I.marks);
             launch_jpeg_entropy(JL, s);
             MMR_CUDA(cudaEventRecord(I.ev[3], s));
             launch_jpeg_idct(JL, s);
@@ -1174,7 +1192,7 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
                 FL[v].cta_first = reinterpret_cast<const uint32_t *>(db + o_fcta[v]);
                 FL[v].n_jobs = (uint32_t)fjobs[v].size();
                 FL[v].n_ctas = fcta[v].back();
-                launches_ += FL[v].n_ctas ? 1 : 0;
+                launches_ += fused_launches(FL[v]);
             }
             launch_jpeg_idct_rgb(JL, FL, s);
             launches_ += (JL.n_tiles ? 3 : 0) + (JL.n_slots ? jpeg_slice_launches(JL) : 0) +
@@ -1251,6 +1269,13 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
                              &times->dv_ms, &times->rgb_ms, &times->download_ms};
             for (int k = 1; k < 8; k++) MMR_CUDA(cudaEventElapsedTime(dst[k], I.ev[k - 1], I.ev[k]));
             MMR_CUDA(cudaEventElapsedTime(&times->device_ms, I.ev[0], I.ev[7]));
+            if (!jframes.empty()) {
+                MMR_CUDA(cudaEventElapsedTime(&times->slice_spec_ms, I.ev[2], I.marks[0]));
+                MMR_CUDA(cudaEventElapsedTime(&times->slice_sync_ms, I.marks[0], I.marks[1]));
+                MMR_CUDA(cudaEventElapsedTime(&times->slice_decode_ms, I.marks[1], I.marks[2]));
+            } else {
+                times->slice_spec_ms = times->slice_sync_ms = times->slice_decode_ms = 0;
+            }
             times->jpeg_blocks = blocks;
             times->idct_exact_samples = *reinterpret_cast<const uint32_t *>(hb + o_b5);
             times->dv_blocks = dv_blocks;

@@ -69,6 +69,9 @@ struct EngineTimes {
     float dv_ms = 0;        // DV segment decode + transform
     float rgb_ms = 0;       // colour conversion
     float download_ms = 0;  // read-back
+    // inside entropy_ms: the chunked decoder's speculative pass, its sync passes +
+    // block prefix, and its final decode
+    float slice_spec_ms = 0, slice_sync_ms = 0, slice_decode_ms = 0;
     uint64_t input_bytes = 0, output_bytes = 0, jpeg_blocks = 0, dv_blocks = 0, rgb_pixels = 0;
     uint64_t idct_exact_samples = 0;  // MJPEG samples recomputed in exact binary64 order
 };

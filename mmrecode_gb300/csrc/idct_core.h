@@ -18,18 +18,19 @@ namespace mmr {
 //   S  = sum_v sum_u M[y][v] M[x][u] c[v][u]   (exact real value, double M)
 //   B  = sum_v sum_u |M[y][v]| |M[x][u]| |c[v][u]|  <=  Mmax^2 * C1,
 //        C1 = sum |c|, Mmax = max |M| = 0.49039264 (Mmax^2 < 0.2405)
-//   fp32 path (M and c rounded to fp32, FMA accumulation, u = 2^-24): any
-//        evaluation whose passes each round at most 8 times per output obeys
-//        |s32 - S| <= (2u + 8u) + (u + 8u) ... = 19u * B + O(u^2) B   (pass 1 error
-//        10u A with A = sum_u |M||c|, propagated through pass 2, plus pass 2's
-//        own 8u; standard recursive-summation bounds, Higham ch. 3); the even/odd
-//        evaluation of idct_block rounds 5 times per pass output, inside it.
+//   fp32 path (idct_block; M and c rounded to fp32, u = 2^-24): each pass output
+//        is fl(E +- O) with E, O chains of four FMAs, so it carries at most 5
+//        roundings over its sum of |terms| (Higham ch. 3: gamma_5), plus u each
+//        for rounding M and c to fp32:
+//          pass 1   |t32 - t| <= 7u A,   A = sum_u |M[x][u]| |c[v][u]|
+//          pass 2   |s32 - S| <= 5u B + u B + 7u B = 13u B   (+ O(u^2) B)
 //   binary64 reference: |s64 - S| <= 16 * 2^-53 * B, and its +128.0 rounds
 //        by at most 2^-53 |s + 128|.
-// With delta = 2^-21 * C1 + 2^-40 |s32| + 2^-30 (2^-21 * C1 >= 19u * 0.2405 C1
-// with 1.7x margin; |s32| <= C1 / 4 turns the middle term into 2^-42 C1), if no
-// half-integer lies within delta of s32 (+128 shifts by an integer) both values
-// round to the same integer, and so clamp to the same sample.
+// With delta = 2^-22 * C1 + 2^-40 |s32| + 2^-30 (2^-22 * C1 = 4u C1 >=
+// 13u * 0.2405 C1 = 3.13u C1, margin 1.28 over the bound; |s32| <= C1 / 4 turns
+// the middle term into 2^-42 C1), if no half-integer lies within delta of s32
+// (+128 shifts by an integer) both values round to the same integer, and so
+// clamp to the same sample.
 // Every other sample is recomputed in the exact reference order. Zero
 // coefficients are skipped in the exact path: a zero term adds +-0.0, which
 // leaves any sum that is not -0.0 unchanged, and these sums are never -0.0.
@@ -114,8 +115,8 @@ __device__ __forceinline__ uint32_t round_sample(float acc, float near, bool &un
 //   s[x] = E + O, s[7-x] = E - O,  E = sum_{u even} M[x][u] c[u], O = sum_{u odd}.
 // Per output this is 4 FMAs per half and one add: each pass's error is <= 5u of
 // the sum of |terms|, plus u for each rounded M and c, <= 13u B after both
-// passes, inside the 19u B the decision bound allows. |s| <= Mmax^2 C1 < C1/4, so
-// the relative term 2^-40 |s| of the bound is folded into 2^-42 C1.
+// passes (the bound above). |s| <= Mmax^2 C1 < C1/4, so the relative term
+// 2^-40 |s| of the bound is folded into 2^-42 C1.
 // Returns the samples left to the exact pass as bits (row * 8 + column).
 __device__ __forceinline__ unsigned long long idct_block(const float *blk, uint32_t q, float c1, uint8_t *out,
                                                          int stride) {
@@ -138,8 +139,8 @@ __device__ __forceinline__ unsigned long long idct_block(const float *blk, uint3
         ta[v] = e + o;
         tb[v] = e - o;
     }
-    // 2^-21 C1 >= 19u Mmax^2 C1 with a 1.75x margin
-    const float near = 0.5f - (c1 * (0x1p-21f + 0x1p-42f) + 0x1p-30f);
+    // delta = 2^-22 C1 >= 13u Mmax^2 C1 (margin 1.28), see the bound above
+    const float near = 0.5f - (c1 * (0x1p-22f + 0x1p-42f) + 0x1p-30f);
     uint32_t bits = 0;  // bit 2*row (column q), 2*row+1 (column 7-q)
 #pragma unroll
     for (int y = 0; y < 4; y++) {

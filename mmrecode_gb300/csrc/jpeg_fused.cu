@@ -23,52 +23,50 @@ namespace {
 
 constexpr int kFStride = 68;  // floats per staged block (16-byte rows, conflict-free over 8 blocks)
 
-template <int HM, int VM>
+template <int HM, int VM, int NM>
 struct FusedShape {
-    static constexpr int NM = HM * VM == 1 ? 16 : 8;    // MCUs per CTA
-    static constexpr int BPM = HM * VM + 2;             // blocks per MCU
-    static constexpr int NB = NM * BPM;                 // blocks per CTA
+    static constexpr int BPM = HM * VM + 2;  // blocks per MCU
+    static constexpr int NB = NM * BPM;      // blocks per CTA
     static constexpr int THREADS = NB * 4;
-    static constexpr int YW = NM * HM * 8;              // luma tile width (samples)
+    static constexpr int YW = NM * HM * 8;   // luma tile width (samples)
     static constexpr int YH = VM * 8;
-    static constexpr int CW = NM * 8;                   // chroma tile width
-    static constexpr int RW = YW * 3;                   // RGB bytes per tile row
+    static constexpr int CW = NM * 8;        // chroma tile width
+    static constexpr int RW = YW * 3;        // RGB bytes per tile row
 };
 
+// MCUs per CTA of the main pass
 template <int HM, int VM>
-__global__ void __launch_bounds__(FusedShape<HM, VM>::THREADS) idct_rgb_kernel(JpegLaunch L, FusedLaunch FL) {
-    using Sh = FusedShape<HM, VM>;
-    __shared__ __align__(16) float s_f[Sh::NB * kFStride];
-    __shared__ __align__(16) uint8_t s_y[Sh::YH * Sh::YW];
-    __shared__ __align__(16) uint8_t s_c[2][8 * Sh::CW];
-    __shared__ __align__(16) uint8_t s_rgb[Sh::YH * Sh::RW];
-    __shared__ __align__(16) float s_q[3][64];
-    __shared__ uint16_t s_list[Sh::NB * 64];
-    __shared__ unsigned long long s_blk[Sh::NB];
-    __shared__ uint32_t s_job, s_n;
-    if (threadIdx.x == 0) {
-        uint32_t lo = 0, hi = FL.n_jobs;
-        while (hi - lo > 1) {
-            const uint32_t mid = (lo + hi) >> 1;
-            if (FL.cta_first[mid] <= blockIdx.x) lo = mid;
-            else hi = mid;
-        }
-        s_job = lo;
-        s_n = 0;
-    }
-    __syncthreads();
-    const FusedJob J = FL.jobs[s_job];
+__host__ __device__ constexpr int fused_nm() { return HM * VM == 1 ? 16 : 8; }
+
+template <int HM, int VM, int NM>
+struct FusedSmem {
+    using Sh = FusedShape<HM, VM, NM>;
+    __align__(16) float f[Sh::NB * kFStride];
+    __align__(16) uint8_t y[Sh::YH * Sh::YW];
+    __align__(16) uint8_t c[2][8 * Sh::CW];
+    __align__(16) uint8_t rgb[Sh::YH * Sh::RW];
+    __align__(16) float q[3][64];
+    unsigned long long mask[Sh::NB];  // samples left to the exact pass, per block
+    unsigned long long blk[Sh::NB];
+    uint32_t n;
+};
+
+// Converts MCUs mx0 .. mx0+NM-1 of MCU row my of job J to RGB; undecided samples
+// are recomputed in the reference order first, eight threads each.
+template <int HM, int VM, int NM>
+__device__ __forceinline__ void fused_tile(const JpegLaunch &L, const FusedLaunch &FL, uint32_t job, uint32_t my,
+                                           uint32_t mx0, FusedSmem<HM, VM, NM> &S) {
+    using Sh = FusedShape<HM, VM, NM>;
+    const FusedJob J = FL.jobs[job];
     const JFrame &F = L.frames[J.frame];
-    if (!L.item_ok[F.item]) return;
     const JComp *comps = L.comps + F.comp_off;
+    if (threadIdx.x == 0) S.n = 0;
     for (uint32_t i = threadIdx.x; i < 3 * 64; i += blockDim.x)
-        s_q[i >> 6][i & 63] = (float)L.quant[F.quant_off + comps[i >> 6].q * 64 + (i & 63)];
-    const uint32_t strip = blockIdx.x - FL.cta_first[s_job];
-    const uint32_t my = strip / J.strips_x, mx0 = (strip % J.strips_x) * Sh::NM;
-    const uint32_t nm = min((uint32_t)Sh::NM, F.mcu_cols - mx0);
+        S.q[i >> 6][i & 63] = (float)L.quant[F.quant_off + comps[i >> 6].q * 64 + (i & 63)];
+    const uint32_t nm = min((uint32_t)NM, F.mcu_cols - mx0);
     const uint32_t lb = threadIdx.x >> 2, q = threadIdx.x & 3;
     const uint32_t m = lb / Sh::BPM, i = lb % Sh::BPM;
-    const bool valid = m < nm;
+    const bool valid = lb < (uint32_t)Sh::NB && m < nm;
     const uint32_t comp = i < HM * VM ? 0 : i - HM * VM + 1;
     uint64_t g = 0;
     if (valid) {
@@ -76,11 +74,11 @@ __global__ void __launch_bounds__(FusedShape<HM, VM>::THREADS) idct_rgb_kernel(J
         const uint32_t mx = mx0 + m;
         if (comp == 0) g = F.blk_off + C.blk_base + (uint64_t)(my * VM + i / HM) * C.bw + mx * HM + i % HM;
         else g = F.blk_off + C.blk_base + (uint64_t)my * C.bw + mx;
-        if (q == 0) s_blk[lb] = g;
+        if (q == 0) S.blk[lb] = g;
     }
-    __syncthreads();  // s_q
-    float *blk = s_f + lb * kFStride;
-    float l1 = valid ? stage_rows(L.coef, L.dc, g, q, s_q[comp], blk) : 0.0f;
+    __syncthreads();  // q, n
+    float *blk = S.f + lb * kFStride;
+    float l1 = valid ? stage_rows(L.coef, L.dc, g, q, S.q[comp], blk) : 0.0f;
 #pragma unroll
     for (int o = 1; o < 4; o <<= 1) l1 += __shfl_xor_sync(0xffffffffu, l1, o);
     __syncwarp();
@@ -89,67 +87,80 @@ __global__ void __launch_bounds__(FusedShape<HM, VM>::THREADS) idct_rgb_kernel(J
         uint8_t *out;
         int stride;
         if (comp == 0) {
-            out = s_y + (i / HM) * 8 * Sh::YW + (m * HM + i % HM) * 8;
+            out = S.y + (i / HM) * 8 * Sh::YW + (m * HM + i % HM) * 8;
             stride = Sh::YW;
         } else {
-            out = s_c[comp - 1] + m * 8;
+            out = S.c[comp - 1] + m * 8;
             stride = Sh::CW;
         }
         mask = idct_block(blk, q, l1, out, stride);
     }
 #pragma unroll
     for (int o = 1; o < 4; o <<= 1) mask |= __shfl_xor_sync(0xffffffffu, mask, o);
-    if (q == 0 && mask) {
-        const uint32_t n = (uint32_t)__popcll(mask);
-        uint32_t at = atomicAdd(&s_n, n);
-        for (unsigned long long b = mask; b; b &= b - 1) s_list[at++] = (uint16_t)((lb << 6) | (__ffsll((long long)b) - 1));
+    if (q == 0 && lb < (uint32_t)Sh::NB) {
+        S.mask[lb] = mask;
+        if (mask) atomicAdd(&S.n, (uint32_t)__popcll(mask));
     }
     __syncthreads();
-    // samples the fp32 transform left open: reference order, eight threads each
-    const uint32_t n_exact = s_n;
+    const uint32_t n_exact = S.n;
     if (threadIdx.x == 0 && n_exact) atomicAdd(L.fix_count + 1, n_exact);
     if (n_exact) {
         const uint32_t grp = threadIdx.x >> 3, v = threadIdx.x & 7, ngrp = blockDim.x >> 3;
         const unsigned gmask = 0xffu << (threadIdx.x & 24);
-        for (uint32_t e = grp; e < n_exact; e += ngrp) {
-            const uint32_t ent = s_list[e], b = ent >> 6, y = (ent >> 3) & 7, x = ent & 7;
-            const uint32_t bm = b / Sh::BPM, bi = b % Sh::BPM;
-            const uint32_t bc = bi < HM * VM ? 0 : bi - HM * VM + 1;
-            const uint64_t bg = s_blk[b];
-            const uint16_t *Q = L.quant + F.quant_off + comps[bc].q * 64;
-            int32_t crow[8];
+        for (uint32_t b = grp; b < (uint32_t)Sh::NB; b += ngrp) {
+            for (unsigned long long bits = S.mask[b]; bits; bits &= bits - 1) {
+                const uint32_t smp_i = __ffsll((long long)bits) - 1, y = smp_i >> 3, x = smp_i & 7;
+                const uint32_t bm = b / Sh::BPM, bi = b % Sh::BPM;
+                const uint32_t bc = bi < HM * VM ? 0 : bi - HM * VM + 1;
+                const uint64_t bg = S.blk[b];
+                const uint16_t *Q = L.quant + F.quant_off + comps[bc].q * 64;
+                int32_t crow[8];
 #pragma unroll
-            for (int u = 0; u < 8; u++) crow[u] = (int32_t)L.coef[bg * 64 + v * 8 + u] * (int32_t)Q[v * 8 + u];
-            if (v == 0) crow[0] = L.dc[bg];
-            const double tv = exact_row(crow, (int)x);
-            double t[8];
+                for (int u = 0; u < 8; u++) crow[u] = (int32_t)L.coef[bg * 64 + v * 8 + u] * (int32_t)Q[v * 8 + u];
+                if (v == 0) crow[0] = L.dc[bg];
+                const double tv = exact_row(crow, (int)x);
+                double t[8];
 #pragma unroll
-            for (int j = 0; j < 8; j++) t[j] = __shfl_sync(gmask, tv, (threadIdx.x & 24) + j);
-            if (v == 0) {
-                const uint8_t smp = exact_finish(t, (int)y);
-                if (bc == 0) s_y[((bi / HM) * 8 + y) * Sh::YW + (bm * HM + bi % HM) * 8 + x] = smp;
-                else s_c[bc - 1][y * Sh::CW + bm * 8 + x] = smp;
+                for (int j = 0; j < 8; j++) t[j] = __shfl_sync(gmask, tv, (threadIdx.x & 24) + j);
+                if (v == 0) {
+                    const uint8_t smp = exact_finish(t, (int)y);
+                    if (bc == 0) S.y[((bi / HM) * 8 + y) * Sh::YW + (bm * HM + bi % HM) * 8 + x] = smp;
+                    else S.c[bc - 1][y * Sh::CW + bm * 8 + x] = smp;
+                }
             }
         }
     }
     __syncthreads();
-    // colour conversion (terminal_preview.rs:7308-7330, full range) into the RGB tile
+    // colour conversion (terminal_preview.rs:7308-7330, full range), four pixels per
+    // thread: one 32-bit luma load, three 32-bit RGB stores (pixels past the visible
+    // width are computed from padding and never copied out)
     const uint32_t x0 = mx0 * HM * 8, y0 = my * VM * 8;
     const uint32_t vis_w = min((uint32_t)(nm * HM * 8), J.width - x0);
     const uint32_t vis_h = min((uint32_t)Sh::YH, J.height - y0);
-    for (uint32_t p = threadIdx.x; p < vis_h * Sh::YW; p += blockDim.x) {
-        const uint32_t ly = p / Sh::YW, lx = p - ly * Sh::YW;
+    for (uint32_t p = threadIdx.x; p < vis_h * (Sh::YW / 4); p += blockDim.x) {
+        const uint32_t ly = p / (Sh::YW / 4), lx = (p - ly * (Sh::YW / 4)) * 4;
         if (lx >= vis_w) continue;
-        const int32_t Y = s_y[ly * Sh::YW + lx];
-        const uint32_t ci = (ly / VM) * Sh::CW + lx / HM;
-        const int32_t u = (int32_t)s_c[0][ci] - 128, w = (int32_t)s_c[1][ci] - 128;
-        int32_t r = Y + ((359 * w + 128) >> 8);
-        int32_t gg = Y - ((88 * u + 183 * w + 128) >> 8);
-        int32_t b = Y + ((454 * u + 128) >> 8);
-        uint8_t *o = s_rgb + ly * Sh::RW + lx * 3;
-        o[0] = (uint8_t)(r < 0 ? 0 : r > 255 ? 255 : r);
-        o[1] = (uint8_t)(gg < 0 ? 0 : gg > 255 ? 255 : gg);
-        o[2] = (uint8_t)(b < 0 ? 0 : b > 255 ? 255 : b);
+        const uint32_t yq = *reinterpret_cast<const uint32_t *>(S.y + ly * Sh::YW + lx);
+        const uint8_t *cbr = S.c[0] + (ly / VM) * Sh::CW + lx / HM;
+        const uint8_t *crr = S.c[1] + (ly / VM) * Sh::CW + lx / HM;
+        uint32_t bytes[3] = {0, 0, 0};
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const int32_t Y = (int32_t)((yq >> (8 * k)) & 0xff);
+            const int32_t u = (int32_t)cbr[k / HM] - 128, w = (int32_t)crr[k / HM] - 128;
+            const int32_t r = Y + ((359 * w + 128) >> 8);
+            const int32_t gg = Y - ((88 * u + 183 * w + 128) >> 8);
+            const int32_t b = Y + ((454 * u + 128) >> 8);
+            const uint32_t rgb[3] = {(uint32_t)(r < 0 ? 0 : r > 255 ? 255 : r),
+                                     (uint32_t)(gg < 0 ? 0 : gg > 255 ? 255 : gg),
+                                     (uint32_t)(b < 0 ? 0 : b > 255 ? 255 : b)};
+#pragma unroll
+            for (int c = 0; c < 3; c++) bytes[(3 * k + c) >> 2] |= rgb[c] << (8 * ((3 * k + c) & 3));
+        }
+        uint32_t *o = reinterpret_cast<uint32_t *>(S.rgb + ly * Sh::RW + lx * 3);
+        o[0] = bytes[0];
+        o[1] = bytes[1];
+        o[2] = bytes[2];
     }
     __syncthreads();
     // rows out: 16-byte stores when the row is aligned, bytes otherwise
@@ -158,14 +169,39 @@ __global__ void __launch_bounds__(FusedShape<HM, VM>::THREADS) idct_rgb_kernel(J
     for (uint32_t c = threadIdx.x; c < vis_h * chunks; c += blockDim.x) {
         const uint32_t ly = c / chunks, ch = c - ly * chunks;
         uint8_t *dst = J.out + ((uint64_t)(y0 + ly) * J.width + x0) * 3;
-        const uint8_t *src = s_rgb + ly * Sh::RW;
+        const uint8_t *src = S.rgb + ly * Sh::RW;
         const uint32_t b0 = ch * 16, b1 = min(b0 + 16, row_bytes);
-        if (b1 - b0 == 16 && ((((uintptr_t)(dst + b0)) & 15) == 0)) {
+        // (a tile row of 8 RGB pixels is 24 bytes: the source needs the check too)
+        if (b1 - b0 == 16 && ((((uintptr_t)(dst + b0)) | ((uintptr_t)(src + b0))) & 15) == 0) {
             *reinterpret_cast<uint4 *>(dst + b0) = *reinterpret_cast<const uint4 *>(src + b0);
         } else {
             for (uint32_t k = b0; k < b1; k++) dst[k] = src[k];
         }
     }
+}
+
+// Main pass: a CTA per strip of MCUs.
+template <int HM, int VM>
+__global__ void __launch_bounds__(FusedShape<HM, VM, fused_nm<HM, VM>()>::THREADS)
+    idct_rgb_kernel(JpegLaunch L, FusedLaunch FL) {
+    constexpr int NM = fused_nm<HM, VM>();
+    __shared__ __align__(16) FusedSmem<HM, VM, NM> S;
+    __shared__ uint32_t s_job;
+    if (threadIdx.x == 0) {
+        uint32_t lo = 0, hi = FL.n_jobs;
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (FL.cta_first[mid] <= blockIdx.x) lo = mid;
+            else hi = mid;
+        }
+        s_job = lo;
+    }
+    __syncthreads();
+    const uint32_t job = s_job;
+    const FusedJob &J = FL.jobs[job];
+    if (!L.item_ok[L.frames[J.frame].item]) return;
+    const uint32_t strip = blockIdx.x - FL.cta_first[job];
+    fused_tile<HM, VM, NM>(L, FL, job, strip / J.strips_x, (strip % J.strips_x) * NM, S);
 }
 
 }  // namespace
@@ -178,14 +214,22 @@ int fused_variant(uint32_t hmax, uint32_t vmax) {
 }
 
 uint32_t fused_strips_x(int variant, uint32_t mcu_cols) {
-    const uint32_t nm = variant == 0 ? FusedShape<1, 1>::NM : FusedShape<2, 1>::NM;
+    const uint32_t nm = variant == 0 ? fused_nm<1, 1>() : variant == 1 ? fused_nm<2, 1>() : fused_nm<2, 2>();
     return (mcu_cols + nm - 1) / nm;
 }
 
+template <int HM, int VM>
+static void launch_variant(const JpegLaunch &L, const FusedLaunch &FL, cudaStream_t s) {
+    if (!FL.n_ctas) return;
+    idct_rgb_kernel<HM, VM><<<FL.n_ctas, FusedShape<HM, VM, fused_nm<HM, VM>()>::THREADS, 0, s>>>(L, FL);
+}
+
+int fused_launches(const FusedLaunch &FL) { return FL.n_ctas ? 1 : 0; }
+
 void launch_jpeg_idct_rgb(const JpegLaunch &L, const FusedLaunch *FL, cudaStream_t s) {
-    if (FL[0].n_ctas) idct_rgb_kernel<1, 1><<<FL[0].n_ctas, FusedShape<1, 1>::THREADS, 0, s>>>(L, FL[0]);
-    if (FL[1].n_ctas) idct_rgb_kernel<2, 1><<<FL[1].n_ctas, FusedShape<2, 1>::THREADS, 0, s>>>(L, FL[1]);
-    if (FL[2].n_ctas) idct_rgb_kernel<2, 2><<<FL[2].n_ctas, FusedShape<2, 2>::THREADS, 0, s>>>(L, FL[2]);
+    launch_variant<1, 1>(L, FL[0], s);
+    launch_variant<2, 1>(L, FL[1], s);
+    launch_variant<2, 2>(L, FL[2], s);
 }
 
 }  // namespace mmr

@@ -646,18 +646,25 @@ __global__ void slice_resolve_kernel(JpegLaunch L) {
 
 int jpeg_slice_launches(const JpegLaunch &L) { return L.n_items_small ? 6 + kSyncPasses : 0; }
 
-void launch_jpeg_slices(const JpegLaunch &L, cudaStream_t s) {
-    if (!L.n_items_small || !L.n_slots) return;
+void launch_jpeg_slices(const JpegLaunch &L, cudaStream_t s, cudaEvent_t *marks) {
+    const bool run = L.n_items_small && L.n_slots;
     const uint32_t warps_per_cta = 4;
-    slice_plan_kernel<<<(L.n_frames + warps_per_cta - 1) / warps_per_cta, 32 * warps_per_cta, 0, s>>>(L);
     const uint32_t grid = (L.n_slots + kSliceThreads - 1) / kSliceThreads;
-    slice_spec_kernel<<<grid, kSliceThreads, 0, s>>>(L);
-    for (uint32_t p = 0; p < (uint32_t)kSyncPasses; p++) slice_sync_kernel<<<grid, kSliceThreads, 0, s>>>(L, p);
     const uint32_t ivgrid = (L.n_items_small + warps_per_cta - 1) / warps_per_cta;
-    slice_fix_kernel<<<ivgrid, 32 * warps_per_cta, 0, s>>>(L);
-    slice_prefix_kernel<<<ivgrid, 32 * warps_per_cta, 0, s>>>(L);
-    slice_decode_kernel<<<grid, kSliceThreads, 0, s>>>(L);
-    slice_resolve_kernel<<<(L.n_items_small + 127) / 128, 128, 0, s>>>(L);
+    if (run) {
+        slice_plan_kernel<<<(L.n_frames + warps_per_cta - 1) / warps_per_cta, 32 * warps_per_cta, 0, s>>>(L);
+        slice_spec_kernel<<<grid, kSliceThreads, 0, s>>>(L);
+    }
+    if (marks) cudaEventRecord(marks[0], s);
+    if (run) {
+        for (uint32_t p = 0; p < (uint32_t)kSyncPasses; p++) slice_sync_kernel<<<grid, kSliceThreads, 0, s>>>(L, p);
+        slice_fix_kernel<<<ivgrid, 32 * warps_per_cta, 0, s>>>(L);
+        slice_prefix_kernel<<<ivgrid, 32 * warps_per_cta, 0, s>>>(L);
+    }
+    if (marks) cudaEventRecord(marks[1], s);
+    if (run) slice_decode_kernel<<<grid, kSliceThreads, 0, s>>>(L);
+    if (marks) cudaEventRecord(marks[2], s);
+    if (run) slice_resolve_kernel<<<(L.n_items_small + 127) / 128, 128, 0, s>>>(L);
 }
 
 }  // namespace mmr

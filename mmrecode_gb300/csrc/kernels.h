@@ -53,11 +53,12 @@ struct JpegLaunch {
 };
 
 constexpr int kSyncPasses = 2;
-constexpr uint32_t kSliceBitsDefault = 2048;
 
 void launch_jpeg_scan(const JpegLaunch &L, cudaStream_t s);
 void launch_jpeg_entropy(const JpegLaunch &L, cudaStream_t s);   // frames with > 4 components
-void launch_jpeg_slices(const JpegLaunch &L, cudaStream_t s);    // frames with <= 4 components
+// frames with <= 4 components; marks (optional, 3 events) are recorded after the
+// speculative pass, after the sync passes + prefix, and after the final decode
+void launch_jpeg_slices(const JpegLaunch &L, cudaStream_t s, cudaEvent_t *marks = nullptr);
 int jpeg_slice_launches(const JpegLaunch &L);
 void launch_jpeg_idct(const JpegLaunch &L, cudaStream_t s);
 uint32_t idct_ctas(uint32_t blocks);
@@ -81,6 +82,7 @@ struct FusedLaunch {
 int fused_variant(uint32_t hmax, uint32_t vmax);  // 0: 1x1, 1: 2x1, 2: 2x2, -1: not fused
 uint32_t fused_strips_x(int variant, uint32_t mcu_cols);
 void launch_jpeg_idct_rgb(const JpegLaunch &L, const FusedLaunch *FL, cudaStream_t s);  // FL[3]
+int fused_launches(const FusedLaunch &FL);
 
 struct DvLaunch {
     const DvFrame *frames;
