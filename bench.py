@@ -206,6 +206,163 @@ def reference_arm(args):
     return 0
 
 
+SERVE_SEED = 20261204
+SERVE_LEVELS = (0.1, 0.5, 0.8, 1.0)
+
+
+def serving_sweep(local: int, seconds: float, frames_per_stream: int = 3):
+    """C5: 64 streams -- 48 MJPEG (16 each at 1280x720, 1920x1080, 3840x2160; 4:2:2,
+    q85, restart interval one MCU row) and 16 DV25 NTSC -- served from a
+    device-resident pool of packets and frame slots under a 40 GB budget.
+    Peak = closed-loop throughput with 96 requests outstanding; then Poisson
+    arrivals (random stream each) at 10..100% of peak, `seconds` per level;
+    latency = submit -> completion, measured by the server."""
+    import ctypes
+    import random
+    import threading
+
+    import torch
+
+    import mmrecode_gb300 as m
+    from mmrecode_gb300 import _lib, synth
+
+    streams = []
+    sizes = [(1280, 720), (1920, 1080), (3840, 2160)]
+    for k in range(48):
+        w, h = sizes[k % 3]
+        streams.append((m.CODEC_MJPEG, synth.mjpeg_stream(SERVE_SEED + k, frames_per_stream, w, h, "422", 85,
+                                                          (w + 15) // 16, annex_k=True)))
+    for k in range(16):
+        streams.append((m.CODEC_DV, synth.dv_stream(SERVE_SEED + 100 + k, frames_per_stream)))
+    # device pool: every packet resident, SLOTS output frames per stream
+    SLOTS = 8
+    offs, o = [], 0
+    for codec, pk in streams:
+        row = []
+        for p in pk:
+            row.append(o)
+            o += (len(p) + 255) // 256 * 256
+        offs.append(row)
+    host_in = torch.empty(o, dtype=torch.uint8, pin_memory=True)
+    hv = host_in.numpy()
+    for (codec, pk), row in zip(streams, offs):
+        for p, off in zip(pk, row):
+            hv[off:off + len(p)] = memoryview(p)
+    dev_in = host_in.to(f"cuda:{local}")
+    out_sizes = [m.probe(codec, pk[0]).planar_bytes for codec, pk in streams]
+    out_offs, o = [], 0
+    for sz in out_sizes:
+        out_offs.append(o)
+        o += SLOTS * ((sz + 255) // 256 * 256)
+    dev_out = torch.empty(o, dtype=torch.uint8, device=f"cuda:{local}")
+    templates = []
+    for s_i, (codec, pk) in enumerate(streams):
+        row = []
+        for f_i, p in enumerate(pk):
+            it = _lib.GpuItem()
+            it.struct_size = ctypes.sizeof(_lib.GpuItem)
+            it.data = host_in.data_ptr() + offs[s_i][f_i]
+            it.device_data = dev_in.data_ptr() + offs[s_i][f_i]
+            it.len = len(p)
+            it.codec = codec
+            it.output = m.OUTPUT_PLANAR
+            it.flags = m.ITEM_OUT_DEVICE
+            it.out_capacity = out_sizes[s_i]
+            row.append(it)
+        templates.append(row)
+    cursor = [0] * len(streams)
+
+    def make(s_i):
+        f = cursor[s_i]
+        cursor[s_i] += 1
+        t = templates[s_i][f % len(templates[s_i])]
+        it = _lib.GpuItem()
+        ctypes.memmove(ctypes.addressof(it), ctypes.addressof(t), ctypes.sizeof(_lib.GpuItem))
+        slot_bytes = (out_sizes[s_i] + 255) // 256 * 256
+        it.out = dev_out.data_ptr() + out_offs[s_i] + (f % SLOTS) * slot_bytes
+        return it
+
+    srv = m.Server(local, engines=4, max_batch=16, memory_budget=40 << 30)
+    rng = random.Random(SERVE_SEED)
+    failures = 0
+
+    def collect(q, done):
+        nonlocal failures
+        res = _lib.GpuItem()
+        res.struct_size = ctypes.sizeof(_lib.GpuItem)
+        while True:
+            t = q.get()
+            if t is None:
+                break
+            srv.wait_item(t, res)
+            failures += res.status != 0
+        done.set()
+
+    import queue as _q
+
+    def closed_loop(duration, outstanding=96):
+        q, done = _q.Queue(), threading.Event()
+        th = threading.Thread(target=collect, args=(q, done))
+        th.start()
+        pending = []
+        res = _lib.GpuItem()
+        res.struct_size = ctypes.sizeof(_lib.GpuItem)
+        srv.stats(reset=True)
+        t0 = time.perf_counter()
+        count = 0
+        while time.perf_counter() - t0 < duration:
+            while len(pending) < outstanding:
+                it = make(rng.randrange(len(streams)))
+                pending.append((srv.submit_item(it), it))
+            t, it = pending.pop(0)
+            srv.wait_item(t, res)
+            count += 1
+        for t, it in pending:
+            srv.wait_item(t, res)
+            count += 1
+        dt = time.perf_counter() - t0
+        q.put(None)
+        th.join()
+        return count / dt
+
+    def open_loop(rate, duration):
+        nonlocal failures
+        arrivals, t = [], 0.0
+        while True:
+            t += rng.expovariate(rate)
+            if t >= duration:
+                break
+            arrivals.append(t)
+        n = len(arrivals)
+        arr = (_lib.GpuItem * n)()
+        for i in range(n):
+            it = make(rng.randrange(len(streams)))
+            ctypes.memmove(ctypes.addressof(arr[i]), ctypes.addressof(it), ctypes.sizeof(_lib.GpuItem))
+        srv.stats(reset=True)
+        lat, lag_ms = srv.replay(arr, arrivals)
+        st = srv.stats()
+        failures += sum(1 for i in range(n) if arr[i].status != 0)
+        lat.sort()
+        pct = lambda q: lat[min(n - 1, int(q * n))] if n else 0.0
+        return {"offered_fps": n / duration, "achieved_fps": st["frames_per_s"], "completed": n,
+                "p50_ms": pct(0.5), "p99_ms": pct(0.99), "max_ms": lat[-1] if n else 0.0,
+                "max_submit_lag_ms": lag_ms, "batches": st["batches"]}
+
+    closed_loop(0.5)  # warm-up: arenas grow to their working size
+    peak = closed_loop(seconds)
+    levels = []
+    for lv in SERVE_LEVELS:
+        r = open_loop(lv * peak, seconds)
+        r["load"] = lv
+        levels.append(r)
+    st = srv.stats()
+    srv.close()
+    return {"workload": "c5-64streams-48mjpeg(720p/1080p/2160p 422 q85 ri1row)+16dv25-planar-device-pool",
+            "engines": 4, "max_batch": 16, "memory_budget_bytes": 40 << 30,
+            "peak_fps_closed_loop": peak, "levels": levels, "failed_requests": failures,
+            "peak_budget_bytes": st["peak_budget_bytes"]}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -214,6 +371,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the oracle CPU-baseline sample")
     ap.add_argument("--plain-frames", type=int, default=60)
+    ap.add_argument("--serve-seconds", type=float, default=2.0, help="seconds per serving load level (0: skip)")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
@@ -249,7 +407,8 @@ def main():
     dev_in = host_in.to(f"cuda:{local}")
     dev_out = torch.empty(n * rgb_bytes, dtype=torch.uint8, device=f"cuda:{local}")
     host_out = torch.empty(n * rgb_bytes, dtype=torch.uint8, pin_memory=True)
-    ctx = m.Context(local)
+    ctx = m.Context(local)               # engines decoding parts of a batch concurrently
+    ctx1 = m.Context(local, engines=1)   # one engine: kernels never overlap, for per-kernel timing
 
     def items(device_resident: bool):
         arr = (_lib.GpuItem * n)()
@@ -266,7 +425,7 @@ def main():
             it.out_capacity = rgb_bytes
         return arr
 
-    def run(arr, steps, warmup, sample_clocks=False):
+    def run(arr, steps, warmup, sample_clocks=False, ctx=ctx):
         for _ in range(warmup):
             ctx.decode_raw(arr)
         _barrier(world)
@@ -301,6 +460,9 @@ def main():
     edt = _max_over_ranks(world, edt)
     e2e = total_frames / edt
 
+    # per-kernel stage times: one engine, device-resident, nothing overlapping
+    _, _, stages, _ = run(resident, 3, 2, ctx=ctx1)
+
     # plain GPU form: one frame per call, host buffers
     lat = []
     for i in range(min(args.plain_frames, n) + 3):
@@ -308,7 +470,7 @@ def main():
         ctypes.memmove(ctypes.addressof(one), ctypes.addressof(hostbuf[i % n]), ctypes.sizeof(_lib.GpuItem))
         torch.cuda.synchronize()
         t = time.perf_counter()
-        ctx.decode_raw(one)
+        ctx1.decode_raw(one)
         lat.append(time.perf_counter() - t)
         assert one[0].status == 0
     lat = lat[3:]
@@ -350,6 +512,11 @@ def main():
     roofline = roof(dominant)
     roofline_transform = roof("idct_rgb_kernel")
 
+    serving, served80 = None, None
+    if rank == 0 and args.serve_seconds > 0:
+        serving = serving_sweep(local, args.serve_seconds)
+        served80 = next((lv for lv in serving["levels"] if lv["load"] == 0.8), None)
+
     cpu = None
     bit_exact = None
     if pool is not None:
@@ -388,7 +555,10 @@ def main():
             "plain_gpu": {"value": plain_fps, "unit": "frames/s", "p50_ms": pct(lat_ms, 0.5), "p99_ms": pct(lat_ms, 0.99),
                           "frames": len(lat)},
             "batched_over_plain": value / plain_fps,
-            "latency_ms": {"batched_p50": ms_per_step, "batched_p99": ms_per_step},
+            "latency_ms": {"batched_p50": ms_per_step, "batched_p99": ms_per_step,
+                           "served_p50_at_80pct": served80["p50_ms"] if served80 else None,
+                           "served_p99_at_80pct": served80["p99_ms"] if served80 else None},
+            "serving": serving,
             "stage_ms": stage_times,
             "idct_exact_sample_fraction": exact_frac,
             "roofline": roofline,

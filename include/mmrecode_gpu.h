@@ -35,11 +35,14 @@ typedef struct mmr_gpu_context mmr_gpu_context;
 
 typedef struct mmr_gpu_config {
     size_t struct_size;
-    int32_t device; /* CUDA device ordinal */
-    uint32_t flags; /* reserved, 0 */
+    int32_t device;   /* CUDA device ordinal */
+    uint32_t flags;   /* reserved, 0 */
+    uint32_t engines; /* batches decoded concurrently, each on its own CUDA stream with its own
+                         device arenas; 0 = 3. A large batch is split over them so that planning,
+                         uploads, kernels and read-backs of its parts overlap. */
 } mmr_gpu_config;
 
-/* Creates a decode context (one CUDA stream and its device arenas) on a device. */
+/* Creates a decode context on a device. */
 MMR_API mmr_status mmr_gpu_context_create(const mmr_gpu_config *config, mmr_gpu_context **out_context);
 
 /* Destroys a context; NULL is ignored. */
@@ -160,6 +163,76 @@ MMR_API mmr_status mmr_dv_encode_ex(const mmr_video_frame_view *frame, uint32_t 
  */
 MMR_API mmr_status mmr_dv_decode_static(const uint8_t *data, size_t len, uint8_t *out, size_t out_capacity,
                                         mmr_gpu_frame_info *info);
+
+/*
+ * Serving: requests from many streams, admitted against a device-memory budget
+ * and batched continuously. No counterpart in the reference library (whose
+ * decoders run one packet per call on the calling thread).
+ *
+ * Each engine takes the oldest queued requests that fit its share of the
+ * budget (memory_budget / engines, estimated from the packet headers) and at
+ * most max_batch of them, decodes them as one batch and takes the next ones, so
+ * requests arriving while others are on the GPU join the next free batch.
+ * A request whose estimate alone exceeds an engine's share is refused with
+ * MMR_STATUS_INVALID_ARGUMENT.
+ */
+typedef struct mmr_gpu_server mmr_gpu_server;
+
+typedef struct mmr_gpu_server_config {
+    size_t struct_size;
+    int32_t device;
+    uint32_t engines;       /* batches in flight; 0 = 3 */
+    uint32_t max_batch;     /* packets per batch; 0 = 64 */
+    uint32_t pad;
+    uint64_t memory_budget; /* device bytes for all batches in flight; 0 = no cap */
+} mmr_gpu_server_config;
+
+typedef struct mmr_gpu_server_stats {
+    size_t struct_size;
+    uint64_t submitted, completed, failed, rejected, batches, in_flight, queued;
+    double p50_ms, p99_ms, max_ms, mean_ms; /* submit -> completion, requests completed in the window */
+    double frames_per_s, window_s;          /* completions over the window (since creation or reset) */
+    uint64_t peak_budget_bytes;             /* largest estimated footprint of the batches in flight */
+} mmr_gpu_server_stats;
+
+MMR_API mmr_status mmr_gpu_server_create(const mmr_gpu_server_config *config, mmr_gpu_server **out_server);
+
+/* Completes every submitted request, then destroys the server; NULL is ignored. */
+MMR_API void mmr_gpu_server_destroy(mmr_gpu_server *server);
+
+/*
+ * Queues one packet and returns at once with a ticket. The item's fields are
+ * read now (data, len, codec, output, flags, out, out_capacity, as for
+ * mmr_gpu_decode_batch); the packet bytes and the output buffer must stay valid
+ * until mmr_gpu_server_wait has returned the ticket.
+ */
+MMR_API mmr_status mmr_gpu_server_submit(mmr_gpu_server *server, const mmr_gpu_item *item, uint64_t *ticket);
+
+/*
+ * Waits for a ticket (timeout_ns < 0: without limit). On completion fills the
+ * result fields of *result (status, format, ..., message; its struct_size must
+ * be set) and *latency_ms (submit to completion), forgets the ticket and returns
+ * MMR_STATUS_OK; on timeout returns MMR_STATUS_INVALID_STATE and the ticket stays
+ * valid. Unknown tickets are MMR_STATUS_INVALID_ARGUMENT.
+ */
+MMR_API mmr_status mmr_gpu_server_wait(mmr_gpu_server *server, uint64_t ticket, int64_t timeout_ns,
+                                       mmr_gpu_item *result, double *latency_ms);
+
+/* Counters and latency percentiles; reset != 0 starts a new window. */
+MMR_API mmr_status mmr_gpu_server_stats_get(mmr_gpu_server *server, int reset, mmr_gpu_server_stats *stats);
+
+/*
+ * Open-loop load replay: submits items[i] arrival_ns[i] nanoseconds after the
+ * call starts (offsets non-decreasing) from a native thread, and returns when
+ * every item has completed, with its result in items[i], its submit-to-completion
+ * latency in latency_ms[i] and the largest delay of a submission past its
+ * arrival time in *max_lag_ns (NULL allowed).
+ */
+MMR_API mmr_status mmr_gpu_server_replay(mmr_gpu_server *server, mmr_gpu_item *items, size_t count,
+                                         const int64_t *arrival_ns, double *latency_ms, int64_t *max_lag_ns);
+
+/* mmr_gpu_set_slice_bits for a server's engines. */
+MMR_API mmr_status mmr_gpu_server_set_slice_bits(mmr_gpu_server *server, uint32_t bits);
 
 #ifdef __cplusplus
 }

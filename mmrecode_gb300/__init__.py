@@ -11,6 +11,8 @@ Mirrors the reference's decode interface for this path:
   With ``batch > 1`` packets queue until a batch is full (or ``flush``) and
   decode together on the GPU.
 * ``Context``: many packets per GPU pass (``mmr_gpu_decode_batch``).
+* ``Server``: requests from many streams, admitted against a device-memory budget
+  and batched continuously (``mmr_gpu_server_*``), with p50/p99 latency.
 
 All decoding runs in CUDA kernels inside libmmrecode_gpu.so; there is no CPU
 decode path.
@@ -215,11 +217,12 @@ class BatchResult:
 
 
 class Context:
-    """One GPU decode context (a CUDA stream with its device arenas)."""
+    """A GPU decode context: engines (CUDA stream + device arenas each) that decode batches."""
 
-    def __init__(self, device: int = 0):
+    def __init__(self, device: int = 0, engines: int = 0):
+        """``engines``: batches decoded concurrently (own CUDA stream and arenas each); 0 = 3."""
         lib = _lib.load()
-        cfg = _lib.GpuConfig(ctypes.sizeof(_lib.GpuConfig), device, 0)
+        cfg = _lib.GpuConfig(ctypes.sizeof(_lib.GpuConfig), device, 0, engines)
         h = ctypes.c_void_p()
         st = lib.mmr_gpu_context_create(ctypes.byref(cfg), ctypes.byref(h))
         if st != STATUS_OK:
@@ -310,6 +313,131 @@ class Context:
             payload = ctypes.string_at(outs[i], it.out_bytes) if it.status == STATUS_OK else None
             res.append((r, payload))
         return res
+
+
+def _result(it) -> BatchResult:
+    return BatchResult(it.status, it.message.decode("utf-8", "replace"), it.format, it.range, it.width, it.height,
+                       it.plane_count, tuple(it.plane_offset), tuple(it.plane_width), tuple(it.plane_height),
+                       it.out_bytes, it.concealed_segments)
+
+
+class Server:
+    """Continuous-batching decode server (``mmr_gpu_server_*``).
+
+    ``submit`` queues one packet and returns a ticket at once; the packet bytes and
+    the output buffer are kept alive here until ``wait`` returns that ticket."""
+
+    def __init__(self, device: int = 0, engines: int = 0, max_batch: int = 0, memory_budget: int = 0):
+        lib = _lib.load()
+        cfg = _lib.ServerConfig(ctypes.sizeof(_lib.ServerConfig), device, engines, max_batch, 0, memory_budget)
+        h = ctypes.c_void_p()
+        st = lib.mmr_gpu_server_create(ctypes.byref(cfg), ctypes.byref(h))
+        if st != STATUS_OK:
+            raise MmrError(st, _lib.last_error())
+        self._h = h
+        self._keep = {}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.load().mmr_gpu_server_destroy(self._h)
+            self._h = None
+            self._keep.clear()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def submit(self, packet: bytes, codec: int = CODEC_MJPEG, output: int = OUTPUT_PLANAR, conceal: bool = False,
+               out_device_ptr: int = 0, out_capacity: int = 0) -> int:
+        """Queues a packet; output goes to a host buffer sized from the headers, or to
+        ``out_device_ptr`` (device memory of ``out_capacity`` bytes) when given."""
+        data = bytes(packet)
+        src = (ctypes.c_uint8 * max(len(data), 1)).from_buffer_copy(data or b"\0")
+        it = _lib.GpuItem()
+        it.struct_size = ctypes.sizeof(_lib.GpuItem)
+        it.data = ctypes.addressof(src)
+        it.len = len(data)
+        it.codec = codec
+        it.output = output
+        it.flags = (ITEM_CONCEAL if conceal else 0) | (ITEM_OUT_DEVICE if out_device_ptr else 0)
+        dst = None
+        if out_device_ptr:
+            it.out = out_device_ptr
+            it.out_capacity = out_capacity
+        else:
+            try:
+                info = probe(codec, data)
+                need = info.rgb_bytes if output == OUTPUT_RGB24 else info.planar_bytes
+            except MmrError:
+                need = 0
+            dst = (ctypes.c_uint8 * max(need, 1))()
+            it.out = ctypes.addressof(dst)
+            it.out_capacity = need
+        t = ctypes.c_uint64()
+        st = _lib.load().mmr_gpu_server_submit(self._h, ctypes.byref(it), ctypes.byref(t))
+        if st != STATUS_OK:
+            raise MmrError(st, _lib.last_error())
+        self._keep[t.value] = (src, dst)
+        return t.value
+
+    def submit_item(self, item) -> int:
+        """Queues a prebuilt ``_lib.GpuItem`` (its buffers are the caller's to keep alive)."""
+        t = ctypes.c_uint64()
+        st = _lib.load().mmr_gpu_server_submit(self._h, ctypes.byref(item), ctypes.byref(t))
+        if st != STATUS_OK:
+            raise MmrError(st, _lib.last_error())
+        return t.value
+
+    def wait_item(self, ticket: int, result, timeout_s: float | None = None) -> float:
+        """Waits for a ticket from ``submit_item``; fills ``result`` (a ``_lib.GpuItem``); returns the latency in ms."""
+        lat = ctypes.c_double()
+        ns = -1 if timeout_s is None else int(timeout_s * 1e9)
+        st = _lib.load().mmr_gpu_server_wait(self._h, ticket, ns, ctypes.byref(result), ctypes.byref(lat))
+        if st != STATUS_OK:
+            raise MmrError(st, _lib.last_error())
+        return lat.value
+
+    def wait(self, ticket: int, timeout_s: float | None = None):
+        """(BatchResult, payload bytes or None, latency ms); raises MmrError(INVALID_STATE) on timeout."""
+        it = _lib.GpuItem()
+        it.struct_size = ctypes.sizeof(_lib.GpuItem)
+        lat = ctypes.c_double()
+        ns = -1 if timeout_s is None else int(timeout_s * 1e9)
+        st = _lib.load().mmr_gpu_server_wait(self._h, ticket, ns, ctypes.byref(it), ctypes.byref(lat))
+        if st != STATUS_OK:
+            raise MmrError(st, _lib.last_error())
+        src, dst = self._keep.pop(ticket)
+        r = _result(it)
+        payload = ctypes.string_at(dst, it.out_bytes) if (dst is not None and it.status == STATUS_OK) else None
+        return r, payload, lat.value
+
+    def replay(self, items, arrival_s) -> tuple:
+        """Open-loop replay of a ``(_lib.GpuItem * n)`` array at the given arrival
+        offsets (seconds, non-decreasing), natively; returns (latencies ms, max
+        submission lag ms). Results land in ``items``."""
+        n = len(items)
+        arr = (ctypes.c_int64 * n)(*[int(t * 1e9) for t in arrival_s])
+        lat = (ctypes.c_double * n)()
+        lag = ctypes.c_int64()
+        st = _lib.load().mmr_gpu_server_replay(self._h, items, n, arr, lat, ctypes.byref(lag))
+        if st != STATUS_OK:
+            raise MmrError(st, _lib.last_error())
+        return list(lat), lag.value / 1e6
+
+    def stats(self, reset: bool = False) -> dict:
+        s = _lib.ServerStats()
+        s.struct_size = ctypes.sizeof(_lib.ServerStats)
+        st = _lib.load().mmr_gpu_server_stats_get(self._h, 1 if reset else 0, ctypes.byref(s))
+        if st != STATUS_OK:
+            raise MmrError(st, _lib.last_error())
+        return {name: getattr(s, name) for name, _ in _lib.ServerStats._fields_ if name != "struct_size"}
+
+    def set_slice_bits(self, bits: int) -> None:
+        st = _lib.load().mmr_gpu_server_set_slice_bits(self._h, bits)
+        if st != STATUS_OK:
+            raise MmrError(st, _lib.last_error())
 
 
 def frame_from_batch(r: BatchResult, payload: bytes) -> VideoFrame:

@@ -43,7 +43,20 @@ class Buffer(ctypes.Structure):
 
 
 class GpuConfig(ctypes.Structure):
-    _fields_ = [("struct_size", ctypes.c_size_t), ("device", ctypes.c_int32), ("flags", ctypes.c_uint32)]
+    _fields_ = [("struct_size", ctypes.c_size_t), ("device", ctypes.c_int32), ("flags", ctypes.c_uint32),
+                ("engines", ctypes.c_uint32)]
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_size_t), ("device", ctypes.c_int32), ("engines", ctypes.c_uint32),
+                ("max_batch", ctypes.c_uint32), ("pad", ctypes.c_uint32), ("memory_budget", ctypes.c_uint64)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_size_t)] + [(n, ctypes.c_uint64) for n in (
+        "submitted", "completed", "failed", "rejected", "batches", "in_flight", "queued")] + [
+        (n, ctypes.c_double) for n in ("p50_ms", "p99_ms", "max_ms", "mean_ms", "frames_per_s", "window_s")] + [
+        ("peak_budget_bytes", ctypes.c_uint64)]
 
 
 class FrameInfo(ctypes.Structure):
@@ -112,6 +125,17 @@ SIGNATURES = {
     "mmr_dv_encode_ex": ([ctypes.POINTER(VideoFrameView), ctypes.c_uint32, ctypes.POINTER(Buffer)], ctypes.c_int32),
     "mmr_dv_decode_static": ([ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
                               ctypes.POINTER(FrameInfo)], ctypes.c_int32),
+    "mmr_gpu_server_create": ([ctypes.POINTER(ServerConfig), ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int32),
+    "mmr_gpu_server_destroy": ([ctypes.c_void_p], None),
+    "mmr_gpu_server_submit": ([ctypes.c_void_p, ctypes.POINTER(GpuItem), ctypes.POINTER(ctypes.c_uint64)],
+                              ctypes.c_int32),
+    "mmr_gpu_server_wait": ([ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int64, ctypes.POINTER(GpuItem),
+                            ctypes.POINTER(ctypes.c_double)], ctypes.c_int32),
+    "mmr_gpu_server_stats_get": ([ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ServerStats)], ctypes.c_int32),
+    "mmr_gpu_server_set_slice_bits": ([ctypes.c_void_p, ctypes.c_uint32], ctypes.c_int32),
+    "mmr_gpu_server_replay": ([ctypes.c_void_p, ctypes.POINTER(GpuItem), ctypes.c_size_t,
+                              ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_double),
+                              ctypes.POINTER(ctypes.c_int64)], ctypes.c_int32),
 }
 
 _lib = None

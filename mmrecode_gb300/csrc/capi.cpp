@@ -15,6 +15,7 @@
 #include "encode.h"
 #include "engine.h"
 #include "last_error.h"
+#include "runtime.h"
 
 using mmr::Engine;
 using mmr::Item;
@@ -246,11 +247,58 @@ void set_last_error(int32_t status, const char *message) {
 }  // namespace mmr
 
 struct mmr_gpu_context {
-    Engine *engine;
+    mmr::EnginePool *pool;
     double last_ms;
     uint32_t last_launches;
     mmr::EngineTimes times;
 };
+
+struct mmr_gpu_server {
+    mmr::Server *server;
+};
+
+namespace {
+
+bool to_item(const mmr_gpu_item &g, Item &it, const char **err) {
+    if (g.struct_size != sizeof(mmr_gpu_item)) {
+        *err = "item struct_size mismatch";
+        return false;
+    }
+    if (g.len > 0 && !g.data) {
+        *err = "item data is null while length is nonzero";
+        return false;
+    }
+    it.data = static_cast<const uint8_t *>(g.data);
+    it.dev_data = static_cast<const uint8_t *>(g.device_data);
+    it.len = g.len;
+    it.codec = g.codec;
+    it.output = g.output;
+    it.flags = (g.flags & MMR_ITEM_CONCEAL) ? mmr::kFlagConceal : 0;
+    it.out = static_cast<uint8_t *>(g.out);
+    it.out_capacity = g.out_capacity;
+    it.out_on_device = (g.flags & MMR_ITEM_OUT_DEVICE) != 0;
+    return true;
+}
+
+void from_item(const Item &it, mmr_gpu_item &g) {
+    g.status = it.status;
+    g.format = it.format;
+    g.range = it.range;
+    g.width = it.width;
+    g.height = it.height;
+    g.plane_count = it.plane_count;
+    for (int c = 0; c < 3; c++) {
+        g.plane_offset[c] = it.plane_offset[c];
+        g.plane_width[c] = it.plane_width[c];
+        g.plane_height[c] = it.plane_height[c];
+    }
+    g.out_bytes = it.out_bytes;
+    g.concealed_segments = (uint32_t)it.concealed.size();
+    std::string m = it.status == MMR_STATUS_OK ? std::string() : with_prefix(it.status, it.message);
+    snprintf(g.message, sizeof g.message, "%s", m.c_str());
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -357,10 +405,11 @@ MMR_API void mmr_buffer_free(mmr_buffer *buffer) {
 MMR_API mmr_status mmr_gpu_context_create(const mmr_gpu_config *config, mmr_gpu_context **out_context) {
     if (!out_context) return invalid_argument("out_context is null");
     *out_context = nullptr;
-    int device = 0;
+    int device = 0, engines = 3;
     if (config) {
         if (config->struct_size != sizeof(mmr_gpu_config)) return invalid_argument("config struct_size mismatch");
         device = config->device;
+        if (config->engines) engines = (int)std::min<uint32_t>(config->engines, 16);
     }
     int count = 0;
     if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) {
@@ -368,7 +417,7 @@ MMR_API mmr_status mmr_gpu_context_create(const mmr_gpu_config *config, mmr_gpu_
         return finish(MMR_STATUS_INTERNAL_ERROR, "no usable CUDA device for the GPU decoder");
     }
     try {
-        mmr_gpu_context *c = new mmr_gpu_context{new Engine(device), 0.0, 0, mmr::EngineTimes()};
+        mmr_gpu_context *c = new mmr_gpu_context{new mmr::EnginePool(device, engines), 0.0, 0, mmr::EngineTimes()};
         *out_context = c;
         return finish(MMR_STATUS_OK, "");
     } catch (const std::exception &e) {
@@ -378,7 +427,7 @@ MMR_API mmr_status mmr_gpu_context_create(const mmr_gpu_config *config, mmr_gpu_
 
 MMR_API void mmr_gpu_context_destroy(mmr_gpu_context *context) {
     if (!context) return;
-    delete context->engine;
+    delete context->pool;
     delete context;
 }
 
@@ -409,44 +458,15 @@ MMR_API mmr_status mmr_gpu_decode_batch(mmr_gpu_context *context, mmr_gpu_item *
     if (count && !items) return invalid_argument("items is null");
     try {
         std::vector<Item> v(count);
-        for (size_t i = 0; i < count; i++) {
-            const mmr_gpu_item &g = items[i];
-            if (g.struct_size != sizeof(mmr_gpu_item)) return invalid_argument("item struct_size mismatch");
-            if (g.len > 0 && !g.data) return invalid_argument("item data is null while length is nonzero");
-            v[i].data = g.data;
-            v[i].dev_data = g.device_data;
-            v[i].len = g.len;
-            v[i].codec = g.codec;
-            v[i].output = g.output;
-            v[i].flags = (g.flags & MMR_ITEM_CONCEAL) ? mmr::kFlagConceal : 0;
-            v[i].out = g.out;
-            v[i].out_capacity = g.out_capacity;
-            v[i].out_on_device = (g.flags & MMR_ITEM_OUT_DEVICE) != 0;
-        }
+        const char *err = nullptr;
+        for (size_t i = 0; i < count; i++)
+            if (!to_item(items[i], v[i], &err)) return invalid_argument(err);
         mmr::EngineTimes t;
-        int32_t st = context->engine->decode(v.data(), count, &t);
+        int32_t st = context->pool->decode(v.data(), count, &t);
         context->last_ms = t.device_ms;
-        context->last_launches = context->engine->last_launches();
+        context->last_launches = context->pool->last_launches();
         context->times = t;
-        for (size_t i = 0; i < count; i++) {
-            mmr_gpu_item &g = items[i];
-            const Item &it = v[i];
-            g.status = it.status;
-            g.format = it.format;
-            g.range = it.range;
-            g.width = it.width;
-            g.height = it.height;
-            g.plane_count = it.plane_count;
-            for (int c = 0; c < 3; c++) {
-                g.plane_offset[c] = it.plane_offset[c];
-                g.plane_width[c] = it.plane_width[c];
-                g.plane_height[c] = it.plane_height[c];
-            }
-            g.out_bytes = it.out_bytes;
-            g.concealed_segments = (uint32_t)it.concealed.size();
-            std::string m = it.status == MMR_STATUS_OK ? std::string() : with_prefix(it.status, it.message);
-            snprintf(g.message, sizeof g.message, "%s", m.c_str());
-        }
+        for (size_t i = 0; i < count; i++) from_item(v[i], items[i]);
         if (st != mmr::kOk) return finish(MMR_STATUS_INTERNAL_ERROR, "CUDA device failure during batch decode");
         return finish(MMR_STATUS_OK, "");
     } catch (...) {
@@ -462,7 +482,7 @@ MMR_API uint32_t mmr_gpu_last_batch_launches(const mmr_gpu_context *context) {
 
 MMR_API mmr_status mmr_gpu_set_slice_bits(mmr_gpu_context *context, uint32_t bits) {
     if (!context) return invalid_argument("context is null");
-    if (!context->engine->set_slice_bits(bits)) return invalid_argument("slice bits must be 0 or a multiple of 32 in 128..1048576");
+    if (!context->pool->set_slice_bits(bits)) return invalid_argument("slice bits must be 0 or a multiple of 32 in 128..1048576");
     return finish(MMR_STATUS_OK, "");
 }
 
@@ -515,6 +535,114 @@ MMR_API mmr_status mmr_dv_encode_ex(const mmr_video_frame_view *frame, uint32_t 
     } catch (...) {
         return finish(MMR_STATUS_INTERNAL_ERROR, "panic contained at MMRecode C API boundary");
     }
+}
+
+MMR_API mmr_status mmr_gpu_server_create(const mmr_gpu_server_config *config, mmr_gpu_server **out_server) {
+    if (!out_server) return invalid_argument("out_server is null");
+    *out_server = nullptr;
+    if (!config) return invalid_argument("config is null");
+    if (config->struct_size != sizeof(mmr_gpu_server_config)) return invalid_argument("config struct_size mismatch");
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || config->device < 0 || config->device >= count) {
+        cudaGetLastError();
+        return finish(MMR_STATUS_INTERNAL_ERROR, "no usable CUDA device for the GPU decoder");
+    }
+    try {
+        mmr::ServerConfig c;
+        c.device = config->device;
+        c.engines = config->engines ? (int)std::min<uint32_t>(config->engines, 16) : 3;
+        c.max_batch = config->max_batch ? config->max_batch : 64;
+        c.memory_budget = config->memory_budget;
+        *out_server = new mmr_gpu_server{new mmr::Server(c)};
+        return finish(MMR_STATUS_OK, "");
+    } catch (const std::exception &e) {
+        return finish(MMR_STATUS_INTERNAL_ERROR, std::string("could not initialise the GPU server: ") + e.what());
+    }
+}
+
+MMR_API void mmr_gpu_server_destroy(mmr_gpu_server *server) {
+    if (!server) return;
+    delete server->server;
+    delete server;
+}
+
+MMR_API mmr_status mmr_gpu_server_submit(mmr_gpu_server *server, const mmr_gpu_item *item, uint64_t *ticket) {
+    if (!server || !item || !ticket) return invalid_argument("server, item or ticket is null");
+    try {
+        Item it;
+        const char *err = nullptr;
+        if (!to_item(*item, it, &err)) return invalid_argument(err);
+        if (server->server->submit(it, ticket) != mmr::kOk)
+            return invalid_argument("request exceeds the server's device-memory budget per engine");
+        return finish(MMR_STATUS_OK, "");
+    } catch (...) {
+        return finish(MMR_STATUS_INTERNAL_ERROR, "panic contained at MMRecode C API boundary");
+    }
+}
+
+MMR_API mmr_status mmr_gpu_server_wait(mmr_gpu_server *server, uint64_t ticket, int64_t timeout_ns,
+                                       mmr_gpu_item *result, double *latency_ms) {
+    if (!server || !result) return invalid_argument("server or result is null");
+    if (result->struct_size != sizeof(mmr_gpu_item)) return invalid_argument("result struct_size mismatch");
+    try {
+        Item it;
+        double lat = 0;
+        if (!server->server->wait(ticket, timeout_ns, &it, &lat)) {
+            if (!server->server->known(ticket)) return invalid_argument("unknown ticket");
+            return finish(MMR_STATUS_INVALID_STATE, "request not complete before the timeout");
+        }
+        from_item(it, *result);
+        if (latency_ms) *latency_ms = lat;
+        return finish(MMR_STATUS_OK, "");
+    } catch (...) {
+        return finish(MMR_STATUS_INTERNAL_ERROR, "panic contained at MMRecode C API boundary");
+    }
+}
+
+MMR_API mmr_status mmr_gpu_server_stats_get(mmr_gpu_server *server, int reset, mmr_gpu_server_stats *stats) {
+    if (!server || !stats) return invalid_argument("server or stats is null");
+    if (stats->struct_size != sizeof(mmr_gpu_server_stats)) return invalid_argument("stats struct_size mismatch");
+    const mmr::ServerStats s = server->server->stats(reset != 0);
+    stats->submitted = s.submitted;
+    stats->completed = s.completed;
+    stats->failed = s.failed;
+    stats->rejected = s.rejected;
+    stats->batches = s.batches;
+    stats->in_flight = s.in_flight;
+    stats->queued = s.queued;
+    stats->p50_ms = s.p50_ms;
+    stats->p99_ms = s.p99_ms;
+    stats->max_ms = s.max_ms;
+    stats->mean_ms = s.mean_ms;
+    stats->frames_per_s = s.frames_per_s;
+    stats->window_s = s.window_s;
+    stats->peak_budget_bytes = s.peak_budget_bytes;
+    return finish(MMR_STATUS_OK, "");
+}
+
+MMR_API mmr_status mmr_gpu_server_replay(mmr_gpu_server *server, mmr_gpu_item *items, size_t count,
+                                         const int64_t *arrival_ns, double *latency_ms, int64_t *max_lag_ns) {
+    if (!server) return invalid_argument("server is null");
+    if (count && (!items || !arrival_ns || !latency_ms)) return invalid_argument("items, arrival_ns or latency_ms is null");
+    try {
+        std::vector<Item> v(count);
+        const char *err = nullptr;
+        for (size_t i = 0; i < count; i++) {
+            if (!to_item(items[i], v[i], &err)) return invalid_argument(err);
+            if (i && arrival_ns[i] < arrival_ns[i - 1]) return invalid_argument("arrival times must not decrease");
+        }
+        server->server->replay(v.data(), count, arrival_ns, latency_ms, max_lag_ns);
+        for (size_t i = 0; i < count; i++) from_item(v[i], items[i]);
+        return finish(MMR_STATUS_OK, "");
+    } catch (...) {
+        return finish(MMR_STATUS_INTERNAL_ERROR, "panic contained at MMRecode C API boundary");
+    }
+}
+
+MMR_API mmr_status mmr_gpu_server_set_slice_bits(mmr_gpu_server *server, uint32_t bits) {
+    if (!server) return invalid_argument("server is null");
+    if (!server->server->set_slice_bits(bits)) return invalid_argument("slice bits must be 0 or a multiple of 32 in 128..1048576");
+    return finish(MMR_STATUS_OK, "");
 }
 
 }  // extern "C"

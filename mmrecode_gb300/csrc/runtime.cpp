@@ -1,0 +1,297 @@
+// Host runtime: engine pool for large batches and the continuous-batching server.
+#include "runtime.h"
+
+#include <algorithm>
+#include <chrono>
+
+namespace mmr {
+
+void accumulate_times(EngineTimes &a, const EngineTimes &t) {
+    a.upload_ms += t.upload_ms;
+    a.scan_ms += t.scan_ms;
+    a.entropy_ms += t.entropy_ms;
+    a.idct_ms += t.idct_ms;
+    a.dv_ms += t.dv_ms;
+    a.rgb_ms += t.rgb_ms;
+    a.download_ms += t.download_ms;
+    a.slice_spec_ms += t.slice_spec_ms;
+    a.slice_sync_ms += t.slice_sync_ms;
+    a.slice_decode_ms += t.slice_decode_ms;
+    a.input_bytes += t.input_bytes;
+    a.output_bytes += t.output_bytes;
+    a.jpeg_blocks += t.jpeg_blocks;
+    a.dv_blocks += t.dv_blocks;
+    a.rgb_pixels += t.rgb_pixels;
+    a.idct_exact_samples += t.idct_exact_samples;
+}
+
+// ------------------------------------------------------------------ pool ---
+
+EnginePool::EnginePool(int device, int engines) {
+    engines = std::max(1, engines);
+    for (int k = 0; k < engines; k++) engines_.emplace_back(new Engine(device));
+    for (int k = 0; k < engines; k++) threads_.emplace_back(&EnginePool::worker, this, k);
+}
+
+EnginePool::~EnginePool() {
+    {
+        std::lock_guard<std::mutex> g(mu_);
+        stop_ = true;
+    }
+    work_cv_.notify_all();
+    for (auto &t : threads_) t.join();
+}
+
+bool EnginePool::set_slice_bits(uint32_t bits) {
+    bool ok = true;
+    for (auto &e : engines_) ok &= e->set_slice_bits(bits);
+    return ok;
+}
+
+void EnginePool::worker(int k) {
+    for (;;) {
+        std::unique_lock<std::mutex> lk(mu_);
+        work_cv_.wait(lk, [&] { return stop_ || next_ < chunks_.size(); });
+        if (stop_) return;
+        const size_t i = next_++;
+        Chunk &c = chunks_[i];
+        lk.unlock();
+        c.status = engines_[k]->decode(c.items, c.n, &c.times);
+        c.launches = engines_[k]->last_launches();
+        lk.lock();
+        if (++done_ == chunks_.size()) done_cv_.notify_all();
+    }
+}
+
+int32_t EnginePool::decode(Item *items, size_t n, EngineTimes *times) {
+    std::lock_guard<std::mutex> call(call_mu_);
+    const auto t0 = std::chrono::steady_clock::now();
+    const size_t k = engines_.size();
+    int32_t status;
+    EngineTimes sum;
+    if (k == 1 || n < 2 * kMinChunk) {
+        // small batch: the calling thread decodes on the first engine
+        status = engines_[0]->decode(items, n, &sum);
+        launches_ = engines_[0]->last_launches();
+    } else {
+        // two chunks per engine: each engine plans its next chunk while its last
+        // one is on the GPU next to the other engines' chunks
+        const size_t parts = std::min(2 * k, n / kMinChunk);
+        std::unique_lock<std::mutex> lk(mu_);
+        chunks_.clear();
+        for (size_t p = 0, first = 0; p < parts; p++) {
+            const size_t cnt = n / parts + (p < n % parts ? 1 : 0);
+            chunks_.push_back({items + first, cnt, EngineTimes(), 0, kOk});
+            first += cnt;
+        }
+        next_ = done_ = 0;
+        work_cv_.notify_all();
+        done_cv_.wait(lk, [&] { return done_ == chunks_.size(); });
+        status = kOk;
+        launches_ = 0;
+        for (const Chunk &c : chunks_) {
+            accumulate_times(sum, c.times);
+            launches_ += c.launches;
+            if (c.status != kOk) status = c.status;
+        }
+    }
+    sum.device_ms = (float)std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (times) *times = sum;
+    return status;
+}
+
+// ---------------------------------------------------------------- server ---
+
+uint64_t Server::estimate_bytes(const Item &it) {
+    const Probe p = probe_packet(it.codec, it.data, it.len);
+    const uint64_t planar = p.status == kOk ? p.planar_bytes : 0;
+    const uint64_t out = p.status == kOk ? (it.output == kOutRgb24 ? p.rgb_bytes : planar) : 0;
+    uint64_t b = 4 * (uint64_t)it.len + (planar * 5) / 2 + planar + 65536;  // tokens, slices, coefficients, scratch
+    if (!it.out_on_device) b += out;  // staged output
+    return b;
+}
+
+Server::Server(const ServerConfig &cfg) : cfg_(cfg) {
+    cfg_.engines = std::max(1, cfg_.engines);
+    cfg_.max_batch = std::max<size_t>(1, cfg_.max_batch);
+    share_ = cfg_.memory_budget ? cfg_.memory_budget / cfg_.engines : 0;
+    window_start_ = std::chrono::steady_clock::now();
+    for (int k = 0; k < cfg_.engines; k++) engines_.emplace_back(new Engine(cfg_.device));
+    for (int k = 0; k < cfg_.engines; k++) threads_.emplace_back(&Server::worker, this, k);
+}
+
+Server::~Server() {
+    {
+        std::unique_lock<std::mutex> lk(mu_);
+        // finish what was submitted
+        done_cv_.wait(lk, [&] { return queue_.empty() && in_flight_ == 0; });
+        stop_ = true;
+    }
+    work_cv_.notify_all();
+    for (auto &t : threads_) t.join();
+}
+
+bool Server::set_slice_bits(uint32_t bits) {
+    std::lock_guard<std::mutex> g(mu_);
+    bool ok = true;
+    for (auto &e : engines_) ok &= e->set_slice_bits(bits);
+    return ok;
+}
+
+int32_t Server::submit(const Item &item, uint64_t *ticket) {
+    auto r = std::make_shared<Request>();
+    r->item = item;
+    r->est_bytes = estimate_bytes(item);
+    if (share_ && r->est_bytes > share_) {
+        std::lock_guard<std::mutex> g(mu_);
+        totals_.rejected++;
+        return kInvalidArgument;
+    }
+    r->submitted = std::chrono::steady_clock::now();
+    {
+        std::lock_guard<std::mutex> g(mu_);
+        r->ticket = next_ticket_++;
+        live_[r->ticket] = r;
+        queue_.push_back(r);
+        totals_.submitted++;
+    }
+    work_cv_.notify_one();
+    *ticket = r->ticket;
+    return kOk;
+}
+
+void Server::worker(int k) {
+    Engine &engine = *engines_[k];
+    std::vector<std::shared_ptr<Request>> batch;
+    std::vector<Item> items;
+    for (;;) {
+        batch.clear();
+        uint64_t bytes = 0;
+        {
+            std::unique_lock<std::mutex> lk(mu_);
+            work_cv_.wait(lk, [&] { return stop_ || !queue_.empty(); });
+            if (stop_ && queue_.empty()) return;
+            // the oldest requests that fit this engine's share of the budget
+            while (!queue_.empty() && batch.size() < cfg_.max_batch) {
+                const auto &r = queue_.front();
+                if (!batch.empty() && share_ && bytes + r->est_bytes > share_) break;
+                bytes += r->est_bytes;
+                batch.push_back(r);
+                queue_.pop_front();
+            }
+            in_flight_ += batch.size();
+            in_flight_bytes_ += bytes;
+            totals_.peak_budget_bytes = std::max(totals_.peak_budget_bytes, in_flight_bytes_);
+            totals_.batches++;
+            if (!queue_.empty()) work_cv_.notify_one();  // more work for an idle engine
+        }
+        items.resize(batch.size());
+        for (size_t i = 0; i < batch.size(); i++) items[i] = batch[i]->item;
+        engine.decode(items.data(), items.size(), nullptr);
+        const auto now = std::chrono::steady_clock::now();
+        {
+            std::lock_guard<std::mutex> g(mu_);
+            for (size_t i = 0; i < batch.size(); i++) {
+                Request &r = *batch[i];
+                r.item = items[i];
+                r.latency_ms = std::chrono::duration<double, std::milli>(now - r.submitted).count();
+                r.done = true;
+                lat_.push_back(r.latency_ms);
+                totals_.completed++;
+                if (r.item.status != kOk) totals_.failed++;
+            }
+            in_flight_ -= batch.size();
+            in_flight_bytes_ -= bytes;
+        }
+        done_cv_.notify_all();
+    }
+}
+
+bool Server::wait(uint64_t ticket, int64_t timeout_ns, Item *out, double *latency_ms) {
+    std::unique_lock<std::mutex> lk(mu_);
+    auto it = live_.find(ticket);
+    if (it == live_.end()) return false;
+    std::shared_ptr<Request> r = it->second;
+    auto ready = [&] { return r->done; };
+    if (timeout_ns < 0) done_cv_.wait(lk, ready);
+    else if (!done_cv_.wait_for(lk, std::chrono::nanoseconds(timeout_ns), ready)) return false;
+    if (out) *out = r->item;
+    if (latency_ms) *latency_ms = r->latency_ms;
+    live_.erase(ticket);
+    return true;
+}
+
+void Server::replay(Item *items, size_t n, const int64_t *arrival_ns, double *latency_ms, int64_t *max_lag_ns) {
+    std::vector<uint64_t> tickets(n, 0);
+    std::atomic<size_t> submitted{0};
+    std::mutex m;
+    std::condition_variable cv;
+    std::thread collector([&] {
+        for (size_t i = 0; i < n; i++) {
+            {
+                std::unique_lock<std::mutex> lk(m);
+                cv.wait(lk, [&] { return submitted.load() > i; });
+            }
+            if (tickets[i] == 0) {
+                latency_ms[i] = 0;
+                continue;
+            }
+            wait(tickets[i], -1, &items[i], &latency_ms[i]);
+        }
+    });
+    const auto t0 = std::chrono::steady_clock::now();
+    int64_t lag = 0;
+    for (size_t i = 0; i < n; i++) {
+        const auto at = t0 + std::chrono::nanoseconds(arrival_ns[i]);
+        std::this_thread::sleep_until(at);
+        lag = std::max<int64_t>(lag, std::chrono::duration_cast<std::chrono::nanoseconds>(
+                                         std::chrono::steady_clock::now() - at).count());
+        uint64_t t = 0;
+        if (submit(items[i], &t) != kOk) {
+            items[i].status = kInvalidArgument;
+            items[i].message = "request exceeds the server's device-memory budget per engine";
+        }
+        {
+            std::lock_guard<std::mutex> g(m);
+            tickets[i] = t;
+            submitted.store(i + 1);
+        }
+        cv.notify_one();
+    }
+    collector.join();
+    if (max_lag_ns) *max_lag_ns = lag;
+}
+
+bool Server::known(uint64_t ticket) {
+    std::lock_guard<std::mutex> g(mu_);
+    return live_.count(ticket) != 0;
+}
+
+ServerStats Server::stats(bool reset) {
+    std::lock_guard<std::mutex> g(mu_);
+    ServerStats s = totals_;
+    s.in_flight = in_flight_;
+    s.queued = queue_.size();
+    const auto now = std::chrono::steady_clock::now();
+    s.window_s = std::chrono::duration<double>(now - window_start_).count();
+    if (!lat_.empty()) {
+        std::vector<double> v(lat_);
+        std::sort(v.begin(), v.end());
+        auto pct = [&](double q) { return v[std::min(v.size() - 1, (size_t)(q * v.size()))]; };
+        s.p50_ms = pct(0.50);
+        s.p99_ms = pct(0.99);
+        s.max_ms = v.back();
+        double sum = 0;
+        for (double x : v) sum += x;
+        s.mean_ms = sum / v.size();
+        s.frames_per_s = s.window_s > 0 ? v.size() / s.window_s : 0;
+    }
+    if (reset) {
+        lat_.clear();
+        window_start_ = now;
+        totals_.peak_budget_bytes = in_flight_bytes_;
+    }
+    return s;
+}
+
+}  // namespace mmr
