@@ -218,7 +218,8 @@ MMR_API mmr_status mmr_gpu_server_submit(mmr_gpu_server *server, const mmr_gpu_i
 MMR_API mmr_status mmr_gpu_server_wait(mmr_gpu_server *server, uint64_t ticket, int64_t timeout_ns,
                                        mmr_gpu_item *result, double *latency_ms);
 
-/* Counters and latency percentiles; reset != 0 starts a new window. */
+/* Counters and latency percentiles of the window (since creation or the last reset);
+   reset != 0 starts a new window after reading this one. */
 MMR_API mmr_status mmr_gpu_server_stats_get(mmr_gpu_server *server, int reset, mmr_gpu_server_stats *stats);
 
 /*

@@ -286,9 +286,10 @@ ServerStats Server::stats(bool reset) {
         s.mean_ms = sum / v.size();
         s.frames_per_s = s.window_s > 0 ? v.size() / s.window_s : 0;
     }
-    if (reset) {
+    if (reset) {  // counters and latencies start again
         lat_.clear();
         window_start_ = now;
+        totals_ = ServerStats();
         totals_.peak_budget_bytes = in_flight_bytes_;
     }
     return s;

@@ -109,7 +109,8 @@ def test_unknown_ticket_and_timeout():
         assert r.status == 0 and payload
         st = srv.stats(reset=True)
         assert st["completed"] == 1
-        assert srv.stats()["p50_ms"] == 0  # new window
+        st = srv.stats()
+        assert st["p50_ms"] == 0 and st["completed"] == 0  # new window
 
 
 def test_open_loop_replay_returns_every_result():
