@@ -164,9 +164,14 @@ def _profile_figures():
     return out
 
 
+def workload_seed(rank: int) -> int:
+    """Each replica decodes its own frames."""
+    return SEED + rank
+
+
 def make_workload(rank: int):
     from mmrecode_gb300 import synth
-    return synth.mjpeg_stream(SEED + rank, FRAMES, W, H, SUB, Q, RI, annex_k=True)
+    return synth.mjpeg_stream(workload_seed(rank), FRAMES, W, H, SUB, Q, RI, annex_k=True)
 
 
 def reference_arm(args):
