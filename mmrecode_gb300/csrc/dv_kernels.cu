@@ -7,9 +7,10 @@
 //              unused bits -- block region, macroblock pool, segment pool
 //              (dv/src/decoder.rs:152-317); writes dequantised coefficients.
 //   resolve    first failing segment per frame (sequential semantics).
-//   idct       one thread per sample: the reference's binary64 8-8 direct sum
-//              or 2-4-8 field transform (decoder.rs:520-602) in its exact
-//              operation order, then placement (decoder.rs:395-505).
+//   idct       one thread per sample: fp32 separable 8-8 / 2-4-8 transform with
+//              a proven error bound; samples within it of a rounding boundary
+//              get the reference's binary64 sum in its exact operation order
+//              (decoder.rs:520-602); then placement (decoder.rs:395-505).
 #include <cuda_runtime.h>
 
 #include "kernels.h"
@@ -319,15 +320,75 @@ __device__ __forceinline__ void mb_coords(bool pal, uint32_t seqs, uint32_t sequ
 
 constexpr int kIdctThreads = 256;  // 4 blocks x 64 samples
 
+__constant__ float c_cos16f[128] = {
+#include "cos_table.inc"
+};
+
+constexpr double kFrac = 0.7071067811865476;  // FRAC_1_SQRT_2
+
+// The reference's binary64 8-8 direct sum for sample (y, x) (decoder.rs:520-548):
+// terms ((((cu*cv)*c)*cos_u)*cos_v) accumulated in (v, u) order, then / 4.0. Zero
+// coefficients are skipped: their term is +-0.0, which leaves any sum that is not
+// -0.0 unchanged, and these sums are never -0.0.
+__device__ __noinline__ double exact_88(const int32_t *c, int y, int x) {
+    const double kk00 = __dmul_rn(kFrac, kFrac);
+    double sum = 0.0;
+    for (int v = 0; v < 8; v++) {
+        for (int u = 0; u < 8; u++) {
+            const int32_t cv = c[v * 8 + u];
+            if (cv == 0) continue;
+            const double k = (u == 0 && v == 0) ? kk00 : (u == 0 || v == 0) ? kFrac : 1.0;
+            double t = __dmul_rn(k, (double)cv);
+            t = __dmul_rn(t, c_cos16[(2 * x + 1) * u]);
+            t = __dmul_rn(t, c_cos16[(2 * y + 1) * v]);
+            sum = __dadd_rn(sum, t);
+        }
+    }
+    return sum / 4.0;
+}
+
+// The reference's binary64 2-4-8 transform for sample (y, x) (decoder.rs:555-602):
+// butterfly of row pairs, horizontal pass per row (/ 2.0), four-term field pass (/ 2.0).
+__device__ __noinline__ double exact_248(const int32_t *c, int y, int x) {
+    const int field = y & 1, yy = y >> 1;
+    double sum = 0.0;
+    for (int v = 0; v < 4; v++) {
+        const int row = v * 2 + field, pair = row >> 1;
+        double hs = 0.0;
+        for (int u = 0; u < 8; u++) {
+            const double first = (double)c[pair * 16 + u], second = (double)c[pair * 16 + 8 + u];
+            const double b = (row & 1) ? __dsub_rn(first, second) : __dadd_rn(first, second);
+            if (b != 0.0) hs = __dadd_rn(hs, __dmul_rn(__dmul_rn(u == 0 ? kFrac : 1.0, b), c_cos16[(2 * x + 1) * u]));
+        }
+        const double h = hs / 2.0;
+        if (h != 0.0) sum = __dadd_rn(sum, __dmul_rn(__dmul_rn(v == 0 ? kFrac : 1.0, h), c_cos16[2 * (2 * yy + 1) * v]));
+    }
+    return sum / 2.0;
+}
+
+// Both transforms are first evaluated in fp32 as separable sums (8 + 8 terms for
+// 8-8; butterfly, 8 + 4 terms for 2-4-8), each factor cu * cos the fp32 product
+// of the fp32 roundings (3u, u = 2^-24) and each pass an FMA chain. Against the
+// exact real value of the reference's terms (its doubles: FRAC_1_SQRT_2, the cos
+// table, the integer c) the fp32 sum is off by at most (3u + 8u) + (3u + 8u) = 22u B
+// for 8-8 and 11u + 3u + 4u = 18u B for 2-4-8; the binary64 sequence by < 70 *
+// 2^-53 B. B = sum |terms| <= C1 = sum |c| for 8-8 (|cos| <= 1, cu cv <= 1) and
+// <= C1 / 2 per 2-4-8 field (a butterfly output is at most |c1| + |c2|); after the
+// final / 4.0 or / 2.0, |value32 - value64| <= 5.5u C1 < delta = 2^-21 C1 + 2^-30
+// (= 8u C1 + 2^-30, margin 1.45). If no half-integer lies within delta of value32
+// both round (half away from zero) and clamp alike; the rest are recomputed in
+// the reference order.
 __global__ void __launch_bounds__(kIdctThreads) dv_idct_kernel(DvLaunch L) {
     __shared__ int32_t s_c[4][64];
-    __shared__ double s_h[4][64];
+    __shared__ float s_h[4][64];
+    __shared__ float s_c1[4][2];
     int lb = threadIdx.x >> 6, px = threadIdx.x & 63;
     uint64_t gb = (uint64_t)blockIdx.x * 4 + lb;
     bool valid = gb < L.n_blocks;
     uint32_t f = 0, local_blk = 0;
     const DvFrame *F = nullptr;
     bool failed = false, mode = false;
+    int32_t cval = 0;
     if (valid) {
         // frame from block index: blocks of frame f are [blk_off, blk_off + sequences*27*30)
         uint32_t lo = 0, hi = L.n_frames;
@@ -343,69 +404,65 @@ __global__ void __launch_bounds__(kIdctThreads) dv_idct_kernel(DvLaunch L) {
         if (valid) {
             failed = L.seg_err[F->seg_first + local_blk / 30] != 0;
             mode = L.modes[gb] != 0;
-            s_c[lb][px] = failed ? 0 : (int32_t)L.coef[gb * 64 + px];
+            cval = failed ? 0 : (int32_t)L.coef[gb * 64 + px];
         }
     }
-    __syncthreads();
-    int y = px >> 3, x = px & 7;
-    const double kFrac = 0.7071067811865476;  // FRAC_1_SQRT_2
-    double value = 0.0;
-    if (valid && !failed && mode) {
-        // inverse_248 (decoder.rs:555-602): butterfly, horizontal pass per row, field pass
-        int row = y;
-        int pair = row >> 1;
-        double sum = 0.0;
+    s_c[lb][px] = cval;
+    // C1 of the block: 64 threads = two warps
+    float a = fabsf((float)cval);
 #pragma unroll
-        for (int u = 0; u < 8; u++) {
-            double first = (double)s_c[lb][pair * 16 + u];
-            double second = (double)s_c[lb][pair * 16 + 8 + u];
-            double b = (row & 1) ? __dsub_rn(first, second) : __dadd_rn(first, second);
-            if (b != 0.0) {
-                double cu = u == 0 ? kFrac : 1.0;
-                sum = __dadd_rn(sum, __dmul_rn(__dmul_rn(cu, b), c_cos16[(2 * x + 1) * u]));
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    if ((px & 31) == 0) s_c1[lb][px >> 5] = a;
+    __syncthreads();
+    const int y = px >> 3, x = px & 7;
+    // pass 1: h[row][x]
+    if (valid && !failed) {
+        const int row = y;
+        float h = 0.0f;
+        if (mode) {
+            const int pair = row >> 1;
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const float first = (float)s_c[lb][pair * 16 + u], second = (float)s_c[lb][pair * 16 + 8 + u];
+                const float b = (row & 1) ? first - second : first + second;  // exact: |c| < 2^23
+                h = fmaf((u == 0 ? (float)kFrac : 1.0f) * c_cos16f[(2 * x + 1) * u], b, h);
             }
+            h *= 0.5f;
+        } else {
+#pragma unroll
+            for (int u = 0; u < 8; u++)
+                h = fmaf((u == 0 ? (float)kFrac : 1.0f) * c_cos16f[(2 * x + 1) * u], (float)s_c[lb][row * 8 + u], h);
         }
-        s_h[lb][row * 8 + x] = sum / 2.0;
+        s_h[lb][row * 8 + x] = h;
     }
     __syncthreads();
     if (!valid) return;
+    uint8_t sample = 0;
     if (!failed) {
+        float value;
         if (mode) {
-            int field = y & 1, yy = y >> 1;  // output row y = 2*yy + field
-            double sum = 0.0;
+            const int field = y & 1, yy = y >> 1;
+            float s = 0.0f;
 #pragma unroll
-            for (int v = 0; v < 4; v++) {
-                double h = s_h[lb][(v * 2 + field) * 8 + x];
-                if (h != 0.0) {
-                    double cv = v == 0 ? kFrac : 1.0;
-                    sum = __dadd_rn(sum, __dmul_rn(__dmul_rn(cv, h), c_cos16[2 * (2 * yy + 1) * v]));
-                }
-            }
-            value = sum / 2.0;
+            for (int v = 0; v < 4; v++)
+                s = fmaf((v == 0 ? (float)kFrac : 1.0f) * c_cos16f[2 * (2 * yy + 1) * v], s_h[lb][(v * 2 + field) * 8 + x], s);
+            value = s * 0.5f;
         } else {
-            // inverse_88 (decoder.rs:520-548): direct 64-term sum in (v, u) order
-            const double kk00 = __dmul_rn(kFrac, kFrac);
-            double sum = 0.0;
-            for (int v = 0; v < 8; v++) {
-                for (int u = 0; u < 8; u++) {
-                    int32_t c = s_c[lb][v * 8 + u];
-                    if (c == 0) continue;
-                    double k = (u == 0 && v == 0) ? kk00 : (u == 0 || v == 0) ? kFrac : 1.0;
-                    double t = __dmul_rn(k, (double)c);
-                    t = __dmul_rn(t, c_cos16[(2 * x + 1) * u]);
-                    t = __dmul_rn(t, c_cos16[(2 * y + 1) * v]);
-                    sum = __dadd_rn(sum, t);
-                }
-            }
-            value = sum / 4.0;
+            float s = 0.0f;
+#pragma unroll
+            for (int v = 0; v < 8; v++)
+                s = fmaf((v == 0 ? (float)kFrac : 1.0f) * c_cos16f[(2 * y + 1) * v], s_h[lb][v * 8 + x], s);
+            value = s * 0.25f;
         }
-    }
-    uint8_t sample;
-    if (failed) {
-        sample = 0;  // set below per plane (limited-range black)
-    } else {
-        double r = fmin(fmax(round(value), 0.0), 255.0);
-        sample = (uint8_t)r;
+        const float c1 = s_c1[lb][0] + s_c1[lb][1];
+        const float near = 0.5f - (c1 * 0x1p-21f + 0x1p-30f);
+        const float r = rintf(value);
+        if (fabsf(value - r) < near) {
+            sample = (uint8_t)fminf(fmaxf(r, 0.0f), 255.0f);
+        } else {
+            const double e = mode ? exact_248(s_c[lb], y, x) : exact_88(s_c[lb], y, x);
+            sample = (uint8_t)fmin(fmax(round(e), 0.0), 255.0);
+        }
     }
     // placement (decoder.rs:432-505)
     uint32_t seg = local_blk / 30, j = local_blk % 30;
