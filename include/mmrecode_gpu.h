@@ -117,7 +117,35 @@ typedef struct mmr_gpu_batch_stats {
     uint32_t launches;
     /* inside entropy_ms: speculative slice decode, slice synchronisation + block prefix, final decode */
     double slice_spec_ms, slice_sync_ms, slice_decode_ms;
+    uint32_t graph_replays; /* parts of the batch whose launches replayed a captured CUDA graph */
 } mmr_gpu_batch_stats;
+
+/*
+ * Autotuner: for each tuning class of MJPEG frame in the sample (restart layout:
+ * none / intervals of <= 8 MCUs / longer; log2 of the compressed bits per
+ * interval), decodes up to 64 of its frames at every candidate slice size
+ * (1024, 2048, 4096, 8192 bits) and keeps the fastest entropy stage for that
+ * class in this context. The items are decoded (outputs written) several times.
+ * report (capacity entries, may be NULL) receives one entry per class; *count
+ * the number of classes.
+ */
+typedef struct mmr_gpu_tune_entry {
+    uint32_t frame_class; /* (layout << 8) | log2(bits per interval) */
+    uint32_t slice_bits;  /* chosen */
+    uint32_t frames;      /* sample frames of the class */
+    uint32_t pad;
+    double entropy_ms[4]; /* per candidate: 1024, 2048, 4096, 8192 bits */
+} mmr_gpu_tune_entry;
+
+MMR_API mmr_status mmr_gpu_autotune(mmr_gpu_context *context, mmr_gpu_item *items, size_t count,
+                                    mmr_gpu_tune_entry *report, size_t capacity, size_t *report_count);
+
+/*
+ * CUDA-graph replay (default on): a batch whose packets stay on the device and
+ * whose plan, buffers and pointers equal one of an engine's recent batches is
+ * captured on its second occurrence and replayed as one graph launch afterwards.
+ */
+MMR_API mmr_status mmr_gpu_set_graphs(mmr_gpu_context *context, int enable);
 
 MMR_API mmr_status mmr_gpu_last_batch_stats(const mmr_gpu_context *context, mmr_gpu_batch_stats *stats);
 

@@ -251,6 +251,25 @@ class Context:
     def last_batch_launches(self) -> int:
         return _lib.load().mmr_gpu_last_batch_launches(self._h)
 
+    def autotune(self, items) -> list:
+        """Tunes the slice size per frame class on a ``(_lib.GpuItem * n)`` sample (decoded
+        several times); returns one dict per class."""
+        cap = 64
+        rep = (_lib.TuneEntry * cap)()
+        cnt = ctypes.c_size_t()
+        st = _lib.load().mmr_gpu_autotune(self._h, items, len(items), rep, cap, ctypes.byref(cnt))
+        if st != STATUS_OK:
+            raise MmrError(st, _lib.last_error())
+        return [{"frame_class": rep[k].frame_class, "slice_bits": rep[k].slice_bits, "frames": rep[k].frames,
+                 "entropy_ms": dict(zip((1024, 2048, 4096, 8192), list(rep[k].entropy_ms)))}
+                for k in range(min(cnt.value, cap))]
+
+    def set_graphs(self, enable: bool) -> None:
+        """CUDA-graph replay of repeated device-resident batches (default on)."""
+        st = _lib.load().mmr_gpu_set_graphs(self._h, 1 if enable else 0)
+        if st != STATUS_OK:
+            raise MmrError(st, _lib.last_error())
+
     def set_slice_bits(self, bits: int) -> None:
         """Bits per entropy-decoder slice for later batches (0: automatic). Output never depends on it."""
         st = _lib.load().mmr_gpu_set_slice_bits(self._h, bits)

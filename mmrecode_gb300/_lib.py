@@ -84,7 +84,13 @@ class BatchStats(ctypes.Structure):
         (n, ctypes.c_uint64) for n in ("input_bytes", "output_bytes", "jpeg_blocks", "dv_blocks", "rgb_pixels",
                                       "idct_exact_samples")] + [
         ("launches", ctypes.c_uint32)] + [
-        (n, ctypes.c_double) for n in ("slice_spec_ms", "slice_sync_ms", "slice_decode_ms")]
+        (n, ctypes.c_double) for n in ("slice_spec_ms", "slice_sync_ms", "slice_decode_ms")] + [
+        ("graph_replays", ctypes.c_uint32)]
+
+
+class TuneEntry(ctypes.Structure):
+    _fields_ = [("frame_class", ctypes.c_uint32), ("slice_bits", ctypes.c_uint32), ("frames", ctypes.c_uint32),
+                ("pad", ctypes.c_uint32), ("entropy_ms", ctypes.c_double * 4)]
 
 
 class JpegEncodeOptions(ctypes.Structure):
@@ -119,6 +125,9 @@ SIGNATURES = {
     "mmr_gpu_last_batch_ms": ([ctypes.c_void_p], ctypes.c_double),
     "mmr_gpu_last_batch_launches": ([ctypes.c_void_p], ctypes.c_uint32),
     "mmr_gpu_set_slice_bits": ([ctypes.c_void_p, ctypes.c_uint32], ctypes.c_int32),
+    "mmr_gpu_set_graphs": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int32),
+    "mmr_gpu_autotune": ([ctypes.c_void_p, ctypes.POINTER(GpuItem), ctypes.c_size_t, ctypes.POINTER(TuneEntry),
+                         ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int32),
     "mmr_gpu_last_batch_stats": ([ctypes.c_void_p, ctypes.POINTER(BatchStats)], ctypes.c_int32),
     "mmr_mjpeg_encode_ex": ([ctypes.POINTER(VideoFrameView), ctypes.POINTER(JpegEncodeOptions), ctypes.POINTER(Buffer)],
                             ctypes.c_int32),

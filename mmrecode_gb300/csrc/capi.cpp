@@ -480,6 +480,36 @@ MMR_API uint32_t mmr_gpu_last_batch_launches(const mmr_gpu_context *context) {
     return context ? context->last_launches : 0;
 }
 
+MMR_API mmr_status mmr_gpu_autotune(mmr_gpu_context *context, mmr_gpu_item *items, size_t count,
+                                    mmr_gpu_tune_entry *report, size_t capacity, size_t *report_count) {
+    if (!context) return invalid_argument("context is null");
+    if (count && !items) return invalid_argument("items is null");
+    try {
+        std::vector<Item> v(count);
+        const char *err = nullptr;
+        for (size_t i = 0; i < count; i++)
+            if (!to_item(items[i], v[i], &err)) return invalid_argument(err);
+        const std::vector<mmr::TuneResult> r = context->pool->autotune(v.data(), count);
+        for (size_t k = 0; k < r.size() && report && k < capacity; k++) {
+            report[k].frame_class = r[k].frame_class;
+            report[k].slice_bits = r[k].slice_bits;
+            report[k].frames = r[k].frames;
+            report[k].pad = 0;
+            for (int c = 0; c < 4; c++) report[k].entropy_ms[c] = r[k].ms[c];
+        }
+        if (report_count) *report_count = r.size();
+        return finish(MMR_STATUS_OK, "");
+    } catch (...) {
+        return finish(MMR_STATUS_INTERNAL_ERROR, "panic contained at MMRecode C API boundary");
+    }
+}
+
+MMR_API mmr_status mmr_gpu_set_graphs(mmr_gpu_context *context, int enable) {
+    if (!context) return invalid_argument("context is null");
+    context->pool->set_graphs(enable != 0);
+    return finish(MMR_STATUS_OK, "");
+}
+
 MMR_API mmr_status mmr_gpu_set_slice_bits(mmr_gpu_context *context, uint32_t bits) {
     if (!context) return invalid_argument("context is null");
     if (!context->pool->set_slice_bits(bits)) return invalid_argument("slice bits must be 0 or a multiple of 32 in 128..1048576");
@@ -508,6 +538,7 @@ MMR_API mmr_status mmr_gpu_last_batch_stats(const mmr_gpu_context *context, mmr_
     stats->slice_spec_ms = t.slice_spec_ms;
     stats->slice_sync_ms = t.slice_sync_ms;
     stats->slice_decode_ms = t.slice_decode_ms;
+    stats->graph_replays = t.graph_replays;
     return finish(MMR_STATUS_OK, "");
 }
 

@@ -108,6 +108,16 @@ struct JPlan {
     uint32_t fmt = 0;        // predicted from the header (color model may change in the tail)
 };
 
+// Tuning class of a planned MJPEG frame: restart layout (none, short, long
+// intervals) and log2 of its compressed bits per interval.
+uint32_t tune_class_of(const JPlan &p, size_t len) {
+    const uint32_t layout = p.ri >= p.total_mcus ? 0 : p.ri <= 8 ? 1 : 2;
+    uint64_t bits = 8 * (uint64_t)len / std::max<uint32_t>(1, p.n_intervals);
+    uint32_t lg = 0;
+    while ((bits >>= 1) != 0) lg++;
+    return layout << 8 | lg;
+}
+
 // Huffman LUT source: counts + symbols bytes (as in the DHT payload).
 struct LutSource {
     std::vector<uint8_t> key;  // 16 counts then symbols
@@ -608,6 +618,13 @@ std::string render_message(const Diag &d, const uint8_t *in, size_t len, uint32_
 
 // ---------------------------------------------------------------- probe ---
 
+uint32_t jpeg_tune_class(const uint8_t *data, size_t len) {
+    JPlan p;
+    plan_jpeg(data, len, p);
+    if (!p.decode || p.ncomp > 4) return 0xffffffffu;
+    return tune_class_of(p, len);
+}
+
 Probe probe_packet(uint32_t codec, const uint8_t *data, size_t len) {
     Probe pr;
     if (codec == kCodecDv) {
@@ -672,6 +689,17 @@ struct Engine::Impl {
     // stage boundaries: start, uploads, scan, entropy, idct, dv, rgb, end
     cudaEvent_t ev[8] = {};
     cudaEvent_t marks[3] = {};  // inside the entropy stage
+    // launch sequences of recent batches, as CUDA graphs once they repeat
+    struct GraphEntry {
+        std::vector<uintptr_t> key;
+        std::vector<uint8_t> blob;
+        cudaGraphExec_t exec = nullptr;
+        uint32_t launches = 0;
+        uint64_t last_use = 0;
+    };
+    std::vector<GraphEntry> graphs;
+    uint64_t graph_clock = 0;
+    static constexpr size_t kGraphCache = 8;
 };
 
 Engine::Engine(int device) : device_(device), slice_bits_(0), impl_(new Impl) {
@@ -691,11 +719,17 @@ Engine::~Engine() {
         if (e) cudaEventDestroy(e);
     for (auto &e : impl_->marks)
         if (e) cudaEventDestroy(e);
+    for (auto &g : impl_->graphs)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
     delete impl_;
     if (stream_) cudaStreamDestroy(stream_);
 }
 
 namespace {
+
+cudaError_t record_event(cudaEvent_t e, cudaStream_t s, bool capturing) {
+    return capturing ? cudaEventRecordWithFlags(e, s, cudaEventRecordExternal) : cudaEventRecord(e, s);
+}
 
 void set_result(Item &it, const Diag &d, const uint8_t *in, size_t len, uint32_t ds, uint32_t term) {
     it.diag = d;
@@ -892,7 +926,11 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
                 F.rst_off = rst_total;
                 rst_total += p.n_intervals;
                 if (p.ncomp <= 4) {
-                    const uint32_t slice_bits = slice_bits_ ? slice_bits_ : auto_bits;
+                    uint32_t slice_bits = slice_bits_ ? slice_bits_ : auto_bits;
+                    if (!slice_bits_) {
+                        auto t = tuned_.find(tune_class_of(p, it.len));
+                        if (t != tuned_.end()) slice_bits = t->second;
+                    }
                     F.slice_bits = slice_bits;
                     F.slot_first = (uint32_t)n_slots;
                     F.slot_count = (uint32_t)((8 * (uint64_t)it.len + slice_bits - 1) / slice_bits + p.n_intervals);
@@ -1126,9 +1164,19 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
         memcpy(I.h_blob.ptr, blob.bytes.data(), blob.bytes.size());
         uint8_t *db = I.d_blob.as<uint8_t>();
 
+        // read-back layout (states, item flags, DV segment errors, exact-sample count)
+        size_t back_j = jstates.size() * sizeof(JState), back_d = dstates.size() * sizeof(DvState);
+        size_t back_ok = n * 4, back_seg = seg_first.back();
+        size_t o_b1 = 0, o_b2 = align_up(back_j, 16), o_b3 = align_up(o_b2 + back_d, 16),
+               o_b4 = align_up(o_b3 + back_ok, 16), o_b5 = align_up(o_b4 + back_seg, 16);
+        I.h_back.ensure(std::max<size_t>(o_b5 + 4, 256));
+        uint8_t *hb = reinterpret_cast<uint8_t *>(I.h_back.ptr);
+
         // ------------------------------------------------------- launches
         cudaStream_t s = stream_;
-        MMR_CUDA(cudaEventRecord(I.ev[0], s));
+        bool capturing = false;  // timing events become external graph nodes under capture
+        auto enqueue = [&]() {
+        MMR_CUDA(record_event(I.ev[0], s, capturing));
         MMR_CUDA(cudaMemcpyAsync(db, I.h_blob.ptr, blob.bytes.size(), cudaMemcpyHostToDevice, s));
         for (size_t i = 0; i < n; i++) {
             bool planned = items[i].status == kOk && (items[i].codec == kCodecMjpeg || items[i].codec == kCodecDv);
@@ -1136,7 +1184,7 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
                 MMR_CUDA(cudaMemcpyAsync(d_in + in_off[i], items[i].data, items[i].len, cudaMemcpyHostToDevice, s));
         }
         if (dv_blocks) MMR_CUDA(cudaMemsetAsync(I.d_dvcoef.ptr, 0, dv_blocks * 128, s));
-        MMR_CUDA(cudaEventRecord(I.ev[1], s));
+        MMR_CUDA(record_event(I.ev[1], s, capturing));
 
         JpegLaunch JL;
         memset(&JL, 0, sizeof(JL));
@@ -1181,10 +1229,10 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
         JL.sync_dirty = reinterpret_cast<uint32_t *>(db + o_dirty);
         if (!jframes.empty()) {
             launch_jpeg_scan(JL, s);
-            MMR_CUDA(cudaEventRecord(I.ev[2], s));
-            launch_jpeg_slices(JL, s, I.marks);
+            MMR_CUDA(record_event(I.ev[2], s, capturing));
+            launch_jpeg_slices(JL, s, I.marks, capturing);
             launch_jpeg_entropy(JL, s);
-            MMR_CUDA(cudaEventRecord(I.ev[3], s));
+            MMR_CUDA(record_event(I.ev[3], s, capturing));
             launch_jpeg_idct(JL, s);
             FusedLaunch FL[3];
             for (int v = 0; v < 3; v++) {
@@ -1198,10 +1246,10 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
             launches_ += (JL.n_tiles ? 3 : 0) + (JL.n_slots ? jpeg_slice_launches(JL) : 0) +
                          (n_items > JL.n_items_small ? 1 : 0) + 1 + (JL.n_idct_ctas ? 2 : 0);
         } else {
-            MMR_CUDA(cudaEventRecord(I.ev[2], s));
-            MMR_CUDA(cudaEventRecord(I.ev[3], s));
+            MMR_CUDA(record_event(I.ev[2], s, capturing));
+            MMR_CUDA(record_event(I.ev[3], s, capturing));
         }
-        MMR_CUDA(cudaEventRecord(I.ev[4], s));
+        MMR_CUDA(record_event(I.ev[4], s, capturing));
         DvLaunch DL;
         memset(&DL, 0, sizeof(DL));
         DL.frames = reinterpret_cast<const DvFrame *>(db + o_dframes);
@@ -1223,7 +1271,7 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
             launch_dv_idct(DL, s);
             launches_ += 4;
         }
-        MMR_CUDA(cudaEventRecord(I.ev[5], s));
+        MMR_CUDA(record_event(I.ev[5], s, capturing));
         RgbLaunch RL;
         RL.jobs = reinterpret_cast<const RgbJob *>(db + o_rgbjobs);
         RL.cta_first = reinterpret_cast<const uint32_t *>(db + o_rgbcta);
@@ -1234,16 +1282,10 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
             launch_rgb(RL, s);
             launches_ += 1;
         }
-        MMR_CUDA(cudaEventRecord(I.ev[6], s));
+        MMR_CUDA(record_event(I.ev[6], s, capturing));
         MMR_CUDA(cudaGetLastError());
 
         // ------------------------------------------------------- read-back
-        size_t back_j = jstates.size() * sizeof(JState), back_d = dstates.size() * sizeof(DvState);
-        size_t back_ok = n * 4, back_seg = seg_first.back();
-        size_t o_b1 = 0, o_b2 = align_up(back_j, 16), o_b3 = align_up(o_b2 + back_d, 16),
-               o_b4 = align_up(o_b3 + back_ok, 16), o_b5 = align_up(o_b4 + back_seg, 16);
-        I.h_back.ensure(std::max<size_t>(o_b5 + 4, 256));
-        uint8_t *hb = reinterpret_cast<uint8_t *>(I.h_back.ptr);
         if (back_j) MMR_CUDA(cudaMemcpyAsync(hb + o_b1, db + o_jstates, back_j, cudaMemcpyDeviceToHost, s));
         if (back_d) MMR_CUDA(cudaMemcpyAsync(hb + o_b2, db + o_dstates, back_d, cudaMemcpyDeviceToHost, s));
         if (back_ok) MMR_CUDA(cudaMemcpyAsync(hb + o_b3, db + o_itemok, back_ok, cudaMemcpyDeviceToHost, s));
@@ -1262,7 +1304,87 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
                 MMR_CUDA(cudaMemcpyAsync(it.out, src, it.out_bytes, cudaMemcpyDeviceToHost, s));
             }
         }
-        MMR_CUDA(cudaEventRecord(I.ev[7], s));
+        MMR_CUDA(record_event(I.ev[7], s, capturing));
+        };
+        // A batch identical to the previous one (same plan image, buffers and
+        // caller pointers) is captured into a CUDA graph on its second occurrence
+        // and replayed from then on.
+        std::vector<uintptr_t> key;
+        // only batches whose payloads stay on the device (host copies may be pageable)
+        bool device_resident = true;
+        for (size_t i = 0; i < n; i++)
+            device_resident &= items[i].status != kOk || ((items[i].dev_data || !items[i].len) &&
+                                                          (items[i].out_on_device || !items[i].out_bytes));
+        const bool use_graphs = graphs_ && device_resident;
+        if (use_graphs) {
+            key = {n, (uintptr_t)I.h_blob.ptr, (uintptr_t)I.h_back.ptr, blob.bytes.size()};
+            for (const DevBuf *b : {&I.d_in, &I.d_tok, &I.d_blob, &I.d_tile_tok, &I.d_tile_rst, &I.d_rsts,
+                                    &I.d_results, &I.d_coef, &I.d_dc, &I.d_planes, &I.d_out, &I.d_dvcoef, &I.d_modes,
+                                    &I.d_flags, &I.d_segerr, &I.d_vlc, &I.d_fix, &I.d_slot_item, &I.d_ivs, &I.d_sync,
+                                    &I.d_spec, &I.d_prefix, &I.d_events, &I.d_ivkey})
+                key.push_back((uintptr_t)b->ptr);
+            for (size_t i = 0; i < n; i++) {
+                const Item &it = items[i];
+                for (uintptr_t v : {(uintptr_t)it.data, (uintptr_t)it.dev_data, (uintptr_t)it.len, (uintptr_t)it.out,
+                                    (uintptr_t)it.out_on_device, (uintptr_t)it.out_bytes, (uintptr_t)it.status,
+                                    (uintptr_t)it.plane_out[0], (uintptr_t)it.plane_out[1], (uintptr_t)it.plane_out[2]})
+                    key.push_back(v);
+            }
+        }
+        Impl::GraphEntry *hit = nullptr;
+        if (use_graphs) {
+            for (auto &g : I.graphs)
+                if (g.key == key && g.blob == blob.bytes) hit = &g;
+            if (hit) hit->last_use = ++I.graph_clock;
+        }
+        graph_replayed_ = false;
+        if (hit && hit->exec) {
+            MMR_CUDA(cudaGraphLaunch(hit->exec, s));
+            launches_ = hit->launches;
+            graph_replayed_ = true;
+        } else if (hit) {  // second occurrence: capture
+            cudaGraph_t g = nullptr;
+            cudaGraphExec_t exec = nullptr;
+            bool captured = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+            if (captured) {
+                capturing = true;
+                try {
+                    enqueue();
+                } catch (const CudaError &) {
+                    captured = false;
+                }
+                capturing = false;
+                captured &= cudaStreamEndCapture(s, &g) == cudaSuccess && g;
+                captured = captured && cudaGraphInstantiate(&exec, g, 0) == cudaSuccess;
+                if (g) cudaGraphDestroy(g);
+            }
+            if (captured) {
+                hit->exec = exec;
+                hit->launches = launches_;
+                MMR_CUDA(cudaGraphLaunch(exec, s));
+                graph_replayed_ = true;
+            } else {  // capture refused: run directly from now on
+                cudaGetLastError();
+                graphs_ = false;
+                launches_ = 0;
+                enqueue();
+            }
+        } else {
+            enqueue();
+            if (use_graphs) {  // remember it; evict the least recently used entry
+                if (I.graphs.size() >= Impl::kGraphCache) {
+                    auto lru = std::min_element(I.graphs.begin(), I.graphs.end(),
+                                                [](const auto &a, const auto &b) { return a.last_use < b.last_use; });
+                    if (lru->exec) cudaGraphExecDestroy(lru->exec);
+                    I.graphs.erase(lru);
+                }
+                Impl::GraphEntry e;
+                e.key = std::move(key);
+                e.blob = blob.bytes;
+                e.last_use = ++I.graph_clock;
+                I.graphs.push_back(std::move(e));
+            }
+        }
         MMR_CUDA(cudaStreamSynchronize(s));
         if (times) {
             float *dst[8] = {nullptr, &times->upload_ms, &times->scan_ms, &times->entropy_ms, &times->idct_ms,
@@ -1277,6 +1399,7 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
                 times->slice_spec_ms = times->slice_sync_ms = times->slice_decode_ms = 0;
             }
             times->jpeg_blocks = blocks;
+            times->graph_replays = graph_replayed_ ? 1 : 0;
             times->idct_exact_samples = *reinterpret_cast<const uint32_t *>(hb + o_b5);
             times->dv_blocks = dv_blocks;
             times->rgb_pixels = rgbfirst.back();

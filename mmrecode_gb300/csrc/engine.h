@@ -5,6 +5,7 @@
 
 #include <cuda_runtime.h>
 
+#include <map>
 #include <string>
 #include <utility>
 #include <vector>
@@ -55,6 +56,10 @@ struct Probe {
 
 Probe probe_packet(uint32_t codec, const uint8_t *data, size_t len);
 
+// Tuning class of an MJPEG packet (restart layout, log2 compressed bits per
+// interval), UINT32_MAX when its headers fail or it has more than 4 components.
+uint32_t jpeg_tune_class(const uint8_t *data, size_t len);
+
 // Renders a diagnostic as the reference's message. `data` is the packet, used
 // to turn token counts into byte offsets for entropy-stage errors.
 std::string render_message(const Diag &d, const uint8_t *data, size_t len, uint32_t data_start, uint32_t term);
@@ -74,6 +79,7 @@ struct EngineTimes {
     float slice_spec_ms = 0, slice_sync_ms = 0, slice_decode_ms = 0;
     uint64_t input_bytes = 0, output_bytes = 0, jpeg_blocks = 0, dv_blocks = 0, rgb_pixels = 0;
     uint64_t idct_exact_samples = 0;  // MJPEG samples recomputed in exact binary64 order
+    uint32_t graph_replays = 0;       // batches whose launches replayed a captured CUDA graph
 };
 
 class Engine {
@@ -91,6 +97,9 @@ public:
     cudaStream_t stream() const { return stream_; }
     // Number of this engine's kernel launches in the last decode() call.
     uint32_t last_launches() const { return launches_; }
+    // Replay repeated identical batches from a captured CUDA graph (default on).
+    void set_graphs(bool on) { graphs_ = on; }
+    bool last_batch_from_graph() const { return graph_replayed_; }
     // Bits per slice of the chunked entropy decoder (a multiple of 32 in
     // 128..2^20); 0 selects the automatic per-frame choice.
     uint32_t slice_bits() const { return slice_bits_; }
@@ -99,6 +108,8 @@ public:
         slice_bits_ = bits;
         return true;
     }
+    // Slice bits per tuning class, used when no fixed size is set.
+    void set_tuned(const std::map<uint32_t, uint32_t> &t) { tuned_ = t; }
 
     struct Impl;
 
@@ -107,6 +118,9 @@ private:
     cudaStream_t stream_ = nullptr;
     uint32_t launches_ = 0;
     uint32_t slice_bits_;
+    bool graphs_ = true;
+    std::map<uint32_t, uint32_t> tuned_;
+    bool graph_replayed_ = false;
     Impl *impl_;
 };
 

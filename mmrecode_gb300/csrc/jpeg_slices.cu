@@ -646,7 +646,10 @@ __global__ void slice_resolve_kernel(JpegLaunch L) {
 
 int jpeg_slice_launches(const JpegLaunch &L) { return L.n_items_small ? 6 + kSyncPasses : 0; }
 
-void launch_jpeg_slices(const JpegLaunch &L, cudaStream_t s, cudaEvent_t *marks) {
+void launch_jpeg_slices(const JpegLaunch &L, cudaStream_t s, cudaEvent_t *marks, bool capturing) {
+    auto mark = [&](int k) {
+        if (marks) capturing ? cudaEventRecordWithFlags(marks[k], s, cudaEventRecordExternal) : cudaEventRecord(marks[k], s);
+    };
     const bool run = L.n_items_small && L.n_slots;
     const uint32_t warps_per_cta = 4;
     const uint32_t grid = (L.n_slots + kSliceThreads - 1) / kSliceThreads;
@@ -655,15 +658,15 @@ void launch_jpeg_slices(const JpegLaunch &L, cudaStream_t s, cudaEvent_t *marks)
         slice_plan_kernel<<<(L.n_frames + warps_per_cta - 1) / warps_per_cta, 32 * warps_per_cta, 0, s>>>(L);
         slice_spec_kernel<<<grid, kSliceThreads, 0, s>>>(L);
     }
-    if (marks) cudaEventRecord(marks[0], s);
+    mark(0);
     if (run) {
         for (uint32_t p = 0; p < (uint32_t)kSyncPasses; p++) slice_sync_kernel<<<grid, kSliceThreads, 0, s>>>(L, p);
         slice_fix_kernel<<<ivgrid, 32 * warps_per_cta, 0, s>>>(L);
         slice_prefix_kernel<<<ivgrid, 32 * warps_per_cta, 0, s>>>(L);
     }
-    if (marks) cudaEventRecord(marks[1], s);
+    mark(1);
     if (run) slice_decode_kernel<<<grid, kSliceThreads, 0, s>>>(L);
-    if (marks) cudaEventRecord(marks[2], s);
+    mark(2);
     if (run) slice_resolve_kernel<<<(L.n_items_small + 127) / 128, 128, 0, s>>>(L);
 }
 

@@ -58,7 +58,8 @@ void launch_jpeg_scan(const JpegLaunch &L, cudaStream_t s);
 void launch_jpeg_entropy(const JpegLaunch &L, cudaStream_t s);   // frames with > 4 components
 // frames with <= 4 components; marks (optional, 3 events) are recorded after the
 // speculative pass, after the sync passes + prefix, and after the final decode
-void launch_jpeg_slices(const JpegLaunch &L, cudaStream_t s, cudaEvent_t *marks = nullptr);
+// (as external event nodes when the stream is being captured into a graph)
+void launch_jpeg_slices(const JpegLaunch &L, cudaStream_t s, cudaEvent_t *marks = nullptr, bool capturing = false);
 int jpeg_slice_launches(const JpegLaunch &L);
 void launch_jpeg_idct(const JpegLaunch &L, cudaStream_t s);
 uint32_t idct_ctas(uint32_t blocks);

@@ -23,6 +23,7 @@ void accumulate_times(EngineTimes &a, const EngineTimes &t) {
     a.dv_blocks += t.dv_blocks;
     a.rgb_pixels += t.rgb_pixels;
     a.idct_exact_samples += t.idct_exact_samples;
+    a.graph_replays += t.graph_replays;
 }
 
 // ------------------------------------------------------------------ pool ---
@@ -40,6 +41,10 @@ EnginePool::~EnginePool() {
     }
     work_cv_.notify_all();
     for (auto &t : threads_) t.join();
+}
+
+void EnginePool::set_graphs(bool on) {
+    for (auto &e : engines_) e->set_graphs(on);
 }
 
 bool EnginePool::set_slice_bits(uint32_t bits) {
@@ -61,6 +66,44 @@ void EnginePool::worker(int k) {
         lk.lock();
         if (++done_ == chunks_.size()) done_cv_.notify_all();
     }
+}
+
+std::vector<TuneResult> EnginePool::autotune(Item *items, size_t n) {
+    std::lock_guard<std::mutex> call(call_mu_);
+    std::map<uint32_t, std::vector<Item>> classes;
+    for (size_t i = 0; i < n; i++) {
+        if (items[i].codec != kCodecMjpeg) continue;
+        const uint32_t c = jpeg_tune_class(items[i].data, items[i].len);
+        if (c != 0xffffffffu && classes[c].size() < 64) classes[c].push_back(items[i]);
+    }
+    Engine &e = *engines_[0];
+    const uint32_t keep_bits = e.slice_bits();
+    std::vector<TuneResult> out;
+    for (auto &kv : classes) {
+        TuneResult r;
+        r.frame_class = kv.first;
+        r.frames = (uint32_t)kv.second.size();
+        double best = 1e30;
+        for (int k = 0; k < 4; k++) {
+            e.set_slice_bits(kTuneCandidates[k]);
+            double m = 1e30;
+            for (int rep = 0; rep < 3; rep++) {  // the first run sizes the arenas
+                EngineTimes t;
+                e.decode(kv.second.data(), kv.second.size(), &t);
+                if (rep) m = std::min(m, (double)t.entropy_ms);
+            }
+            r.ms[k] = m;
+            if (m < best) {
+                best = m;
+                r.slice_bits = kTuneCandidates[k];
+            }
+        }
+        tuned_[kv.first] = r.slice_bits;
+        out.push_back(r);
+    }
+    e.set_slice_bits(keep_bits);
+    for (auto &en : engines_) en->set_tuned(tuned_);
+    return out;
 }
 
 int32_t EnginePool::decode(Item *items, size_t n, EngineTimes *times) {

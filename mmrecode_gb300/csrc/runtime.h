@@ -10,6 +10,7 @@
 #include <condition_variable>
 #include <cstdint>
 #include <deque>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <thread>
@@ -22,6 +23,16 @@ namespace mmr {
 
 // Sum of per-chunk stage times (device work) and counters of one pooled decode.
 void accumulate_times(EngineTimes &into, const EngineTimes &t);
+
+// One tuned class: the slice size chosen for it and the entropy-stage time of
+// every candidate on the sample (ms, best of the repetitions).
+struct TuneResult {
+    uint32_t frame_class = 0;
+    uint32_t slice_bits = 0;
+    uint32_t frames = 0;
+    double ms[4] = {0, 0, 0, 0};
+};
+constexpr uint32_t kTuneCandidates[4] = {1024, 2048, 4096, 8192};
 
 class EnginePool {
 public:
@@ -36,6 +47,12 @@ public:
     int32_t decode(Item *items, size_t n, EngineTimes *times);
     uint32_t last_launches() const { return launches_; }
     bool set_slice_bits(uint32_t bits);
+    void set_graphs(bool on);
+    // Measures the entropy stage of the sample's MJPEG frames, class by class, at
+    // every candidate slice size on one engine and keeps the fastest per class for
+    // all engines (classes not in the sample keep the automatic choice). Decodes
+    // the items (outputs included) several times.
+    std::vector<TuneResult> autotune(Item *items, size_t n);
     int size() const { return (int)engines_.size(); }
     Engine &engine(int k) { return *engines_[k]; }
     static constexpr size_t kMinChunk = 16;
@@ -58,6 +75,7 @@ private:
     size_t next_ = 0, done_ = 0;
     bool stop_ = false;
     uint32_t launches_ = 0;
+    std::map<uint32_t, uint32_t> tuned_;
 };
 
 struct ServerConfig {

@@ -106,3 +106,32 @@ def test_corruption_at_slice_boundaries(ctx):
             d[p] = val
             packets.append(bytes(d))
     check(ctx, packets, "boundary")
+
+
+def test_autotune_picks_a_size_per_class_and_output_is_unchanged():
+    import ctypes
+    from mmrecode_gb300 import _lib
+    packets = (synth.mjpeg_stream(311, 6, 640, 480, "420", 75, 0) +
+               synth.mjpeg_stream(312, 6, 480, 272, "422", 90, 30) +
+               synth.mjpeg_stream(313, 6, 320, 240, "444", 60, 4))
+    keep, arr = [], (_lib.GpuItem * len(packets))()
+    for i, p in enumerate(packets):
+        src = (ctypes.c_uint8 * len(p)).from_buffer_copy(p)
+        need = m.probe(m.CODEC_MJPEG, p).planar_bytes
+        dst = (ctypes.c_uint8 * need)()
+        keep.append((src, dst))
+        it = arr[i]
+        it.struct_size = ctypes.sizeof(_lib.GpuItem)
+        it.data, it.len, it.codec, it.output = ctypes.addressof(src), len(p), m.CODEC_MJPEG, m.OUTPUT_PLANAR
+        it.out, it.out_capacity = ctypes.addressof(dst), need
+    with m.Context(engines=2) as ctx:
+        report = ctx.autotune(arr)
+        assert len(report) == 3  # three restart layouts
+        for r in report:
+            assert r["slice_bits"] in (1024, 2048, 4096, 8192) and r["frames"] == 6
+            assert r["entropy_ms"][r["slice_bits"]] == min(r["entropy_ms"].values())
+        results = ctx.decode_batch(packets, m.CODEC_MJPEG, m.OUTPUT_PLANAR)
+    for p, (r, payload) in zip(packets, results):
+        ref = oracle.jpeg_decode(p)
+        assert r.status == 0
+        assert payload == b"".join(d for (_, _, d) in ref.frame.planes)
