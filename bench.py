@@ -368,6 +368,69 @@ def serving_sweep(local: int, seconds: float, frames_per_stream: int = 3):
             "peak_budget_bytes": st["peak_budget_bytes"]}
 
 
+MIXED_SEED = 20261205
+
+
+def mixed_sweep(local: int, steps: int = 5, warmup: int = 3):
+    """C4: 512 MJPEG frames, sizes in steps of 16 over 320x240..3840x2160, 4:2:0 /
+    4:2:2 / 4:4:4, q 50..95, restart interval none / one MCU row / 4 MCUs, planar
+    output, device-resident; slice size autotuned per frame class, then timed with
+    the repeated batch replayed from captured CUDA graphs."""
+    import ctypes
+
+    import torch
+
+    import mmrecode_gb300 as m
+    from mmrecode_gb300 import _lib, synth
+
+    packets, _ = synth.mixed_mjpeg_stream(MIXED_SEED, 512)
+    offs, o = [], 0
+    for p in packets:
+        offs.append(o)
+        o += (len(p) + 255) // 256 * 256
+    host = torch.empty(o, dtype=torch.uint8, pin_memory=True)
+    for p, off in zip(packets, offs):
+        host.numpy()[off:off + len(p)] = memoryview(p)
+    dev = host.to(f"cuda:{local}")
+    need = [m.probe(m.CODEC_MJPEG, p).planar_bytes for p in packets]
+    ooffs, o = [], 0
+    for nb in need:
+        ooffs.append(o)
+        o += (nb + 255) // 256 * 256
+    dev_out = torch.empty(o, dtype=torch.uint8, device=f"cuda:{local}")
+    arr = (_lib.GpuItem * len(packets))()
+    for i, p in enumerate(packets):
+        it = arr[i]
+        it.struct_size = ctypes.sizeof(_lib.GpuItem)
+        it.data = host.data_ptr() + offs[i]
+        it.device_data = dev.data_ptr() + offs[i]
+        it.len = len(p)
+        it.codec = m.CODEC_MJPEG
+        it.output = m.OUTPUT_PLANAR
+        it.flags = m.ITEM_OUT_DEVICE
+        it.out = dev_out.data_ptr() + ooffs[i]
+        it.out_capacity = need[i]
+    ctx = m.Context(local)
+    tuned = ctx.autotune(arr)
+    for _ in range(warmup):
+        ctx.decode_raw(arr)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    replays = 0
+    for _ in range(steps):
+        ctx.decode_raw(arr)
+        replays += ctx.stats()["graph_replays"]
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    ok = all(arr[i].status == 0 for i in range(len(packets)))
+    ctx.close()
+    return {"workload": "c4-512-mixed-mjpeg(320x240..3840x2160, 420/422/444, q50-95, ri none/row/4)-planar",
+            "frames_per_step": len(packets), "compressed_bytes": sum(len(p) for p in packets),
+            "fps": len(packets) * steps / dt, "ms_per_step": 1000 * dt / steps, "graph_replays": replays,
+            "all_ok": ok, "tuned": [{"frame_class": t["frame_class"], "slice_bits": t["slice_bits"],
+                                      "frames": t["frames"]} for t in tuned]}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -377,6 +440,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the oracle CPU-baseline sample")
     ap.add_argument("--plain-frames", type=int, default=60)
     ap.add_argument("--serve-seconds", type=float, default=2.0, help="seconds per serving load level (0: skip)")
+    ap.add_argument("--mixed", type=int, default=1, help="run the 512-frame mixed batch (0: skip)")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
@@ -517,6 +581,7 @@ def main():
     roofline = roof(dominant)
     roofline_transform = roof("idct_rgb_kernel")
 
+    mixed = mixed_sweep(local) if rank == 0 and args.mixed else None
     serving, served80 = None, None
     if rank == 0 and args.serve_seconds > 0:
         serving = serving_sweep(local, args.serve_seconds)
@@ -564,6 +629,7 @@ def main():
                            "served_p50_at_80pct": served80["p50_ms"] if served80 else None,
                            "served_p99_at_80pct": served80["p99_ms"] if served80 else None},
             "serving": serving,
+            "mixed_autotuned_graphs": mixed,
             "stage_ms": stage_times,
             "idct_exact_sample_fraction": exact_frac,
             "roofline": roofline,
