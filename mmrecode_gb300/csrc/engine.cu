@@ -1156,7 +1156,7 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
 
         uint32_t zero_counters[2] = {0, 0};
         size_t o_fixcount = blob.add(zero_counters, 8);
-        uint32_t zero_dirty[kSyncPasses] = {};
+        uint32_t zero_dirty[2 * kSyncPasses] = {};  // changed-exit counts, then work counters
         size_t o_dirty = blob.add(zero_dirty, sizeof(zero_dirty));
         size_t blob_size = std::max<size_t>(blob.bytes.size(), 256);
         I.d_blob.ensure(blob_size);

@@ -9,8 +9,9 @@
 // symbol boundary with the same state, and from there both are identical.
 //
 //   slice_plan     per frame: interval token ranges, slice counts, slot -> interval map
-//   slice_spec     every slice decoded from a guessed state (the first slice from the
-//                  true one) up to its end; keeps the state at 1/4, 1/2 and 3/4 of it
+//   slice_spec     every slice decoded from a guessed state 512 bits before it (the
+//                  first slice from the true one) up to its end; keeps the state 64,
+//                  256, 1024 and 2048 bits into the slice
 //   slice_sync     (twice) each slice whose start no longer equals its predecessor's
 //                  exit state re-decodes from that state until it meets one of its own
 //                  checkpoints (then the rest is known) or its end
@@ -31,6 +32,8 @@
 // by the owner of the block they occur in, so the earliest reported event is the
 // one the serial decoder stops at.
 #include <cuda_runtime.h>
+
+#include <algorithm>
 
 #include "entropy_core.h"
 #include "kernels.h"
@@ -65,6 +68,12 @@ __device__ __forceinline__ BlockTabs block_tabs(const JpegLaunch &L, const JFram
     t.dc = L.luts + R.dc_lut;
     t.ac = L.luts + R.ac_lut;
     return t;
+}
+
+// Bit offset of checkpoint q from the nominal slice start (UINT32_MAX past the slice).
+__device__ __forceinline__ uint32_t mark_of(uint32_t q, uint32_t S) {
+    const uint32_t m = q == 0 ? 64u : 64u << (2 * q < 6 ? 2 * q : 5);  // 64, 256, 1024, 2048
+    return q < (uint32_t)kSliceCheckpoints && m < S ? m : 0xffffffffu;
 }
 
 __device__ __forceinline__ void add_dc(int32_t (&dc)[4], uint32_t comp, int32_t v) {
@@ -180,7 +189,15 @@ __global__ void __launch_bounds__(kSliceThreads) slice_spec_kernel(JpegLaunch L)
     }
     const JFrame &F = *s.F;
     const uint32_t S = F.slice_bits;
-    const unsigned long long p0 = (unsigned long long)s.j * S;
+    const unsigned long long nominal = (unsigned long long)s.j * S;
+    // a guessed decode starts up to kSpecLead bits early; positions below are from p0
+    const uint32_t lead = guess ? (uint32_t)min((unsigned long long)kSpecLead, nominal) : 0;
+    const unsigned long long p0 = nominal - lead;
+    const uint32_t end = S + lead;
+    auto mark_at = [&](uint32_t qq) {
+        const uint32_t m = mark_of(qq, S);
+        return m == 0xffffffffu ? m : m + lead;
+    };
     const unsigned long long lbits = (unsigned long long)(s.v.barrier - s.v.start) * 8;
     const uint32_t lim = clamp_u32(lbits - p0);  // bits before the barrier, from p0
     const uint64_t tokbit = (uint64_t)s.v.start * 8;
@@ -194,17 +211,16 @@ __global__ void __launch_bounds__(kSliceThreads) slice_spec_kernel(JpegLaunch L)
     int32_t dcv = 0;  // DC difference of the block in progress (0 before its DC symbol)
     SliceSpec *sp = L.spec + slot;
     uint32_t q = 0, recorded = 0;
-    const uint32_t step = S / (kSliceCheckpoints + 1);
-    uint32_t next_mark = guess ? step : 0xffffffffu;
+    uint32_t next_mark = guess ? mark_at(0) : 0xffffffffu;
     unsigned long long exit_state = kStErr;
     for (;;) {
         const uint32_t pr = r.used;
-        if (pr >= S) {
+        if (pr >= end) {
             exit_state = pack_state(p0 + pr, si, k);
             break;
         }
         if (pr >= next_mark) {
-            while (q < (uint32_t)kSliceCheckpoints && pr >= (q + 1) * step) {
+            while (pr >= mark_at(q)) {
                 SlicePoint cp;
                 cp.state = pack_state(p0 + pr, si, k);
                 cp.blocks = blocks;
@@ -215,7 +231,7 @@ __global__ void __launch_bounds__(kSliceThreads) slice_spec_kernel(JpegLaunch L)
                 recorded |= 1u << q;
                 q++;
             }
-            next_mark = q < (uint32_t)kSliceCheckpoints ? (q + 1) * step : 0xffffffffu;
+            next_mark = mark_at(q);
         }
         const int k0 = k;
         blocks += k0 == 0;
@@ -300,10 +316,9 @@ __device__ bool resync_slice(const JpegLaunch &L, uint32_t slot, const SliceRef 
     int32_t dc[4] = {0, 0, 0, 0};
     int32_t dcv = 0;
     const SliceSpec *sp = L.spec + slot;
-    const uint32_t step = S / (kSliceCheckpoints + 1);
     uint32_t q = 0;
-    while (q < (uint32_t)kSliceCheckpoints && (q + 1) * step <= rel) q++;  // marks already behind
-    uint32_t next_mark = q < (uint32_t)kSliceCheckpoints ? (q + 1) * step : 0xffffffffu;
+    while (mark_of(q, S) <= rel) q++;  // marks already behind
+    uint32_t next_mark = mark_of(q, S);
     unsigned long long exit_state = kStErr;
     for (;;) {
         const uint32_t pr = r.used;
@@ -314,7 +329,7 @@ __device__ bool resync_slice(const JpegLaunch &L, uint32_t slot, const SliceRef 
         }
         if (pn >= next_mark) {
             bool matched = false;
-            while (q < (uint32_t)kSliceCheckpoints && pn >= (q + 1) * step) {
+            while (pn >= mark_of(q, S)) {
                 const unsigned long long cs = sp->cp[q].state;
                 if (cs != kStErr && cs == pack_state(p0 + pr, si, k)) {
                     // the rest of the slice is the speculative decode's: take its tail
@@ -331,7 +346,7 @@ __device__ bool resync_slice(const JpegLaunch &L, uint32_t slot, const SliceRef 
                 q++;
             }
             if (matched) break;
-            next_mark = q < (uint32_t)kSliceCheckpoints ? (q + 1) * step : 0xffffffffu;
+            next_mark = mark_of(q, S);
         }
         const int k0 = k;
         blocks += k0 == 0;
@@ -356,18 +371,25 @@ __device__ bool resync_slice(const JpegLaunch &L, uint32_t slot, const SliceRef 
     return exit_state != old_exit;
 }
 
+// Persistent threads take slots from a counter: re-decode lengths vary a lot
+// (most slices meet their first checkpoint, a few run to their end), so a lane
+// that is done takes the next slot instead of idling beside the slow ones.
 __global__ void __launch_bounds__(kSliceThreads) slice_sync_kernel(JpegLaunch L, uint32_t pass) {
-    const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
-    SliceRef s;
-    if (!slice_ref(L, slot, s) || s.j == 0) return;
-    const unsigned long long prev = *(volatile const unsigned long long *)&L.sync[slot - 1].exit;
-    const unsigned long long cur = L.sync[slot].start;
-    if (prev == cur) return;
-    if (s.last) {
-        L.sync[slot].start = prev;
-        return;
+    uint32_t *next = L.sync_dirty + kSyncPasses + pass;
+    for (;;) {
+        const uint32_t slot = atomicAdd(next, 1u);
+        if (slot >= L.n_slots) return;
+        SliceRef s;
+        if (!slice_ref(L, slot, s) || s.j == 0) continue;
+        const unsigned long long prev = *(volatile const unsigned long long *)&L.sync[slot - 1].exit;
+        const unsigned long long cur = L.sync[slot].start;
+        if (prev == cur) continue;
+        if (s.last) {
+            L.sync[slot].start = prev;
+            continue;
+        }
+        if (resync_slice(L, slot, s, prev)) atomicAdd(&L.sync_dirty[pass], 1u);
     }
-    if (resync_slice(L, slot, s, prev)) atomicAdd(&L.sync_dirty[pass], 1u);
 }
 
 // One warp per interval; runs only when the last sync pass still changed an exit state.
@@ -660,7 +682,8 @@ void launch_jpeg_slices(const JpegLaunch &L, cudaStream_t s, cudaEvent_t *marks,
     }
     mark(0);
     if (run) {
-        for (uint32_t p = 0; p < (uint32_t)kSyncPasses; p++) slice_sync_kernel<<<grid, kSliceThreads, 0, s>>>(L, p);
+        const uint32_t sync_grid = std::min<uint32_t>(grid, 152 * 8);
+        for (uint32_t p = 0; p < (uint32_t)kSyncPasses; p++) slice_sync_kernel<<<sync_grid, kSliceThreads, 0, s>>>(L, p);
         slice_fix_kernel<<<ivgrid, 32 * warps_per_cta, 0, s>>>(L);
         slice_prefix_kernel<<<ivgrid, 32 * warps_per_cta, 0, s>>>(L);
     }

@@ -49,7 +49,8 @@ struct JpegLaunch {
     SlicePrefix *prefix;         // per slot
     SliceEvent *events;          // per slot
     unsigned long long *iv_key;  // per item: (position << 26 | slice) of its first event
-    uint32_t *sync_dirty;        // per sync pass: slices whose exit state changed (zeroed per batch)
+    uint32_t *sync_dirty;        // per sync pass: slices whose exit state changed, then per pass the
+                                 // next slot to take (2 x kSyncPasses, zeroed per batch)
 };
 
 constexpr int kSyncPasses = 2;

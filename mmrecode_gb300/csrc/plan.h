@@ -121,7 +121,13 @@ struct SlicePoint {
     uint32_t pad;
 };
 
-constexpr int kSliceCheckpoints = 3;  // at 1/4, 1/2 and 3/4 of the slice
+// Checkpoints 64, 256, 1024 and 2048 bits into a slice (those inside it). The
+// speculative decode of a slice starts kSpecLead bits before the slice: the
+// synchronisation distance of Huffman-coded JPEG data is a few hundred bits, so
+// it has usually met the true decode by the first checkpoint, and a re-decode
+// from the predecessor's exit matches there after a few symbols.
+constexpr int kSliceCheckpoints = 4;
+constexpr uint32_t kSpecLead = 512;
 
 struct SliceSpec {
     SlicePoint exit;                      // end of the speculative decode
