@@ -529,6 +529,22 @@ def main():
     edt = _max_over_ranks(world, edt)
     e2e = total_frames / edt
 
+    # the host link this run had: one device-to-host copy of a step's outputs and
+    # one host-to-device copy of its inputs, timed with CUDA events
+    def link_gbs(dst, src, nbytes):
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        best = 0.0
+        for _ in range(3):
+            ev0.record()
+            dst[:nbytes].copy_(src[:nbytes], non_blocking=True)
+            ev1.record()
+            ev1.synchronize()
+            best = max(best, nbytes / (ev0.elapsed_time(ev1) * 1e6))
+        return best
+
+    d2h_gbs = link_gbs(host_out, dev_out, n * rgb_bytes)
+    h2d_gbs = link_gbs(dev_in, host_in, in_bytes)
+
     # per-kernel stage times: one engine, device-resident, nothing overlapping
     _, _, stages, _ = run(resident, 3, 2, ctx=ctx1)
 
@@ -620,7 +636,11 @@ def main():
                        "compressed_bytes_per_step": in_bytes, "l2": "inputs/outputs per step exceed L2; no flush",
                        "parallelism": f"replicas x{world}"},
             "e2e": {"value": e2e, "unit": "frames/s", "h2d_bytes_per_step": in_bytes,
-                    "d2h_bytes_per_step": n * rgb_bytes},
+                    "d2h_bytes_per_step": n * rgb_bytes,
+                    # the link alone: copy-engine bandwidths of this run and the frame rate
+                    # the device-to-host copy of the outputs caps e2e at
+                    "link_d2h_GBps": d2h_gbs, "link_h2d_GBps": h2d_gbs,
+                    "link_cap_frames_per_s": d2h_gbs * 1e9 / rgb_bytes},
             "compressed_MBps": value * in_bytes / n / 1e6,
             "plain_gpu": {"value": plain_fps, "unit": "frames/s", "p50_ms": pct(lat_ms, 0.5), "p99_ms": pct(lat_ms, 0.99),
                           "frames": len(lat)},

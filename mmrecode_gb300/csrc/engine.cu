@@ -702,9 +702,17 @@ struct Engine::Impl {
     static constexpr size_t kGraphCache = 8;
 };
 
-Engine::Engine(int device) : device_(device), slice_bits_(0), impl_(new Impl) {
+Engine::Engine(int device, int levels) : device_(device), slice_bits_(0), impl_(new Impl) {
     MMR_CUDA(cudaSetDevice(device));
-    MMR_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    int least = 0, greatest = 0;
+    MMR_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    levels = std::max(1, std::min(levels, least - greatest + 1));
+    for (int l = 0; l < levels; l++) {
+        cudaStream_t st = nullptr;
+        MMR_CUDA(cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, levels > 1 ? greatest + l : 0));
+        streams_.push_back(st);
+    }
+    stream_ = streams_[0];
     for (auto &e : impl_->ev) MMR_CUDA(cudaEventCreate(&e));
     for (auto &e : impl_->marks) MMR_CUDA(cudaEventCreate(&e));
     impl_->vlc = build_dv_vlc();
@@ -714,7 +722,7 @@ Engine::Engine(int device) : device_(device), slice_bits_(0), impl_(new Impl) {
 
 Engine::~Engine() {
     cudaSetDevice(device_);
-    if (stream_) cudaStreamSynchronize(stream_);
+    for (cudaStream_t st : streams_) cudaStreamSynchronize(st);
     for (auto &e : impl_->ev)
         if (e) cudaEventDestroy(e);
     for (auto &e : impl_->marks)
@@ -722,7 +730,7 @@ Engine::~Engine() {
     for (auto &g : impl_->graphs)
         if (g.exec) cudaGraphExecDestroy(g.exec);
     delete impl_;
-    if (stream_) cudaStreamDestroy(stream_);
+    for (cudaStream_t st : streams_) cudaStreamDestroy(st);
 }
 
 namespace {

@@ -5,6 +5,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <map>
 #include <string>
 #include <utility>
@@ -84,7 +85,9 @@ struct EngineTimes {
 
 class Engine {
 public:
-    explicit Engine(int device);
+    // `levels`: streams at that many CUDA priorities, highest first (1: one
+    // stream at the default priority); set_level picks the next batch's.
+    explicit Engine(int device, int levels = 1);
     ~Engine();
     Engine(const Engine &) = delete;
     Engine &operator=(const Engine &) = delete;
@@ -95,6 +98,11 @@ public:
 
     int device() const { return device_; }
     cudaStream_t stream() const { return stream_; }
+    // Runs the following batches on the stream of priority level `l` (0 = highest,
+    // clamped to the levels the engine has). Kernels of a higher level go first
+    // when engines share the GPU.
+    void set_level(int l) { stream_ = streams_[std::min<size_t>(std::max(l, 0), streams_.size() - 1)]; }
+    int levels() const { return (int)streams_.size(); }
     // Number of this engine's kernel launches in the last decode() call.
     uint32_t last_launches() const { return launches_; }
     // Replay repeated identical batches from a captured CUDA graph (default on).
@@ -115,7 +123,8 @@ public:
 
 private:
     int device_;
-    cudaStream_t stream_ = nullptr;
+    cudaStream_t stream_ = nullptr;      // the current level's stream
+    std::vector<cudaStream_t> streams_;  // one per priority level
     uint32_t launches_ = 0;
     uint32_t slice_bits_;
     bool graphs_ = true;

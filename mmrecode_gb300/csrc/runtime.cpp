@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <stdexcept>
 
 namespace mmr {
 
@@ -28,9 +29,16 @@ void accumulate_times(EngineTimes &a, const EngineTimes &t) {
 
 // ------------------------------------------------------------------ pool ---
 
-EnginePool::EnginePool(int device, int engines) {
+EnginePool::EnginePool(int device, int engines) : device_(device) {
     engines = std::max(1, engines);
-    for (int k = 0; k < engines; k++) engines_.emplace_back(new Engine(device));
+    for (int k = 0; k < engines; k++) {
+        // chunk i of a batch runs at priority level i: chunks complete in order
+        engines_.emplace_back(new Engine(device, engines > 1 ? 2 * engines : 1));
+        cudaStream_t d = nullptr;
+        if (cudaStreamCreateWithFlags(&d, cudaStreamNonBlocking) != cudaSuccess)
+            throw std::runtime_error("cannot create a download stream");
+        down_.push_back(d);
+    }
     for (int k = 0; k < engines; k++) threads_.emplace_back(&EnginePool::worker, this, k);
 }
 
@@ -41,6 +49,54 @@ EnginePool::~EnginePool() {
     }
     work_cv_.notify_all();
     for (auto &t : threads_) t.join();
+    cudaSetDevice(device_);
+    for (cudaStream_t d : down_) {
+        cudaStreamSynchronize(d);
+        cudaStreamDestroy(d);
+    }
+    if (stage_ptr_) cudaFree(stage_ptr_);
+}
+
+bool EnginePool::stage(const Item *items, size_t n) {
+    staged_.assign(items, items + n);
+    redirected_.assign(n, 0);
+    orig_ = items;
+    std::vector<size_t> in_off(n), out_off(n);
+    size_t total = 0;
+    bool any = false;
+    for (size_t i = 0; i < n; i++) {
+        const Item &it = items[i];
+        // single-buffer host payloads (planes written to separate pointers stay on the engine's path)
+        if (it.dev_data || !it.data || !it.len || it.out_on_device || !it.out || !it.out_capacity || it.plane_out[0])
+            continue;
+        redirected_[i] = 1;
+        any = true;
+        in_off[i] = total;
+        total += (it.len + 255) / 256 * 256;
+        out_off[i] = total;
+        total += (it.out_capacity + 255) / 256 * 256;
+    }
+    if (!any) return false;
+    if (total > stage_cap_) {
+        const size_t want = std::max(total, stage_cap_ + stage_cap_ / 2);
+        if (stage_ptr_) cudaFree(stage_ptr_);
+        stage_ptr_ = nullptr;
+        stage_cap_ = 0;
+        if (cudaMalloc(&stage_ptr_, want) != cudaSuccess) {  // no room: the engines copy directly
+            cudaGetLastError();
+            stage_ptr_ = nullptr;
+            return false;
+        }
+        stage_cap_ = want;
+    }
+    uint8_t *base = static_cast<uint8_t *>(stage_ptr_);
+    for (size_t i = 0; i < n; i++) {
+        if (!redirected_[i]) continue;
+        staged_[i].dev_data = base + in_off[i];
+        staged_[i].out = base + out_off[i];
+        staged_[i].out_on_device = true;
+    }
+    return true;
 }
 
 void EnginePool::set_graphs(bool on) {
@@ -53,18 +109,56 @@ bool EnginePool::set_slice_bits(uint32_t bits) {
     return ok;
 }
 
+// Worker k decodes chunks k, k + K, k + 2K, ... of each batch: a repeated batch
+// meets the same engine chunk by chunk, so its graphs replay.
 void EnginePool::worker(int k) {
+    uint64_t seen = 0;
     for (;;) {
         std::unique_lock<std::mutex> lk(mu_);
-        work_cv_.wait(lk, [&] { return stop_ || next_ < chunks_.size(); });
+        work_cv_.wait(lk, [&] { return stop_ || gen_ != seen; });
         if (stop_) return;
-        const size_t i = next_++;
-        Chunk &c = chunks_[i];
+        seen = gen_;
+        const size_t n_chunks = chunks_.size();
+        const bool staging = !redirected_.empty();
         lk.unlock();
-        c.status = engines_[k]->decode(c.items, c.n, &c.times);
-        c.launches = engines_[k]->last_launches();
-        lk.lock();
-        if (++done_ == chunks_.size()) done_cv_.notify_all();
+        Engine &e = *engines_[k];
+        for (size_t i = k; i < n_chunks; i += engines_.size()) {
+            Chunk &c = chunks_[i];
+            e.set_level(staging ? (int)i : 0);  // staged chunks complete in order, for their downloads
+            c.status = kOk;
+            if (staging) {  // inputs up, ahead of the chunk's kernels on the same stream
+                for (size_t j = 0; j < c.n && c.status == kOk; j++)
+                    if (redirected_[c.first + j] &&
+                        cudaMemcpyAsync(const_cast<uint8_t *>(c.items[j].dev_data), c.items[j].data, c.items[j].len,
+                                        cudaMemcpyHostToDevice, e.stream()) != cudaSuccess)
+                        c.status = kInternal;
+            }
+            if (c.status == kOk) {
+                c.status = e.decode(c.items, c.n, &c.times);
+                c.launches = e.last_launches();
+            }
+            if (staging && c.status == kOk) {  // outputs down, while this engine takes its next chunk
+                for (size_t j = 0; j < c.n && c.status == kOk; j++) {
+                    const Item &it = c.items[j];
+                    if (redirected_[c.first + j] && it.status == kOk && it.out_bytes &&
+                        cudaMemcpyAsync(orig_[c.first + j].out, it.out, it.out_bytes, cudaMemcpyDeviceToHost,
+                                        down_[k]) != cudaSuccess)
+                        c.status = kInternal;
+                }
+            }
+            if (c.status != kOk) {
+                cudaGetLastError();
+                for (size_t j = 0; j < c.n; j++) {
+                    c.items[j].diag = make_diag(kDeviceError);
+                    c.items[j].status = kInternal;
+                    if (c.items[j].message.empty()) c.items[j].message = "CUDA device failure: staging copy";
+                    c.items[j].out_bytes = 0;
+                }
+            }
+            lk.lock();
+            if (++done_ == n_chunks) done_cv_.notify_all();
+            lk.unlock();
+        }
     }
 }
 
@@ -77,6 +171,7 @@ std::vector<TuneResult> EnginePool::autotune(Item *items, size_t n) {
         if (c != 0xffffffffu && classes[c].size() < 64) classes[c].push_back(items[i]);
     }
     Engine &e = *engines_[0];
+    e.set_level(0);
     const uint32_t keep_bits = e.slice_bits();
     std::vector<TuneResult> out;
     for (auto &kv : classes) {
@@ -114,23 +209,53 @@ int32_t EnginePool::decode(Item *items, size_t n, EngineTimes *times) {
     EngineTimes sum;
     if (k == 1 || n < 2 * kMinChunk) {
         // small batch: the calling thread decodes on the first engine
+        engines_[0]->set_level(0);
         status = engines_[0]->decode(items, n, &sum);
         launches_ = engines_[0]->last_launches();
     } else {
         // two chunks per engine: each engine plans its next chunk while its last
         // one is on the GPU next to the other engines' chunks
         const size_t parts = std::min(2 * k, n / kMinChunk);
+        Item *work = items;
+        if (cudaSetDevice(device_) == cudaSuccess && stage(items, n)) work = staged_.data();
+        else redirected_.clear();
         std::unique_lock<std::mutex> lk(mu_);
         chunks_.clear();
         for (size_t p = 0, first = 0; p < parts; p++) {
             const size_t cnt = n / parts + (p < n % parts ? 1 : 0);
-            chunks_.push_back({items + first, cnt, EngineTimes(), 0, kOk});
+            chunks_.push_back({work + first, cnt, EngineTimes(), 0, kOk, first});
             first += cnt;
         }
-        next_ = done_ = 0;
+        done_ = 0;
+        gen_++;
         work_cv_.notify_all();
         done_cv_.wait(lk, [&] { return done_ == chunks_.size(); });
+        lk.unlock();
         status = kOk;
+        if (work != items) {  // downloads done, results back into the caller's items
+            for (cudaStream_t d : down_)
+                if (cudaStreamSynchronize(d) != cudaSuccess) status = kInternal;
+            cudaGetLastError();
+            for (size_t i = 0; i < n; i++) {
+                Item &dst = items[i];
+                const Item &src = staged_[i];
+                const uint8_t *dev = dst.dev_data, *data = dst.data;
+                uint8_t *out = dst.out;
+                const bool on_device = dst.out_on_device;
+                dst = src;
+                dst.data = data;
+                dst.dev_data = dev;
+                dst.out = out;
+                dst.out_on_device = on_device;
+                if (status != kOk) {
+                    dst.diag = make_diag(kDeviceError);
+                    dst.status = kInternal;
+                    dst.message = "CUDA device failure: staging copy";
+                    dst.out_bytes = 0;
+                }
+            }
+            redirected_.clear();
+        }
         launches_ = 0;
         for (const Chunk &c : chunks_) {
             accumulate_times(sum, c.times);

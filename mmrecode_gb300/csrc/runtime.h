@@ -42,8 +42,14 @@ public:
     EnginePool &operator=(const EnginePool &) = delete;
 
     // Decodes the items; batches of at least 2 * min_chunk items are split into
-    // chunks decoded concurrently by all engines. times: stage times summed over
-    // chunks, device_ms = wall time of the call. Returns kOk or kInternal.
+    // chunks decoded concurrently by all engines. Payloads in host memory are
+    // staged through device buffers: a chunk's inputs go up on its engine's
+    // stream, the chunk decodes device-resident (and replays as a graph when it
+    // repeats), and its outputs come down on the engine's download stream while
+    // the engine takes its next chunk. Staged chunk i runs at stream priority
+    // level i, so concurrent chunks finish in order and their downloads spread
+    // over the batch instead of queueing at its end. times: stage times summed
+    // over chunks, device_ms = wall time of the call. Returns kOk or kInternal.
     int32_t decode(Item *items, size_t n, EngineTimes *times);
     uint32_t last_launches() const { return launches_; }
     bool set_slice_bits(uint32_t bits);
@@ -64,15 +70,28 @@ private:
         EngineTimes times;
         uint32_t launches;
         int32_t status;
+        size_t first;  // index of items[0] in the batch
     };
     void worker(int k);
+    // Redirects host payloads of the batch to device staging buffers (into
+    // staged_); false when nothing was redirected.
+    bool stage(const Item *items, size_t n);
     std::vector<std::unique_ptr<Engine>> engines_;
+    std::vector<cudaStream_t> down_;  // per engine: downloads of staged outputs
+    int device_ = 0;
+    // staging of the current batch: device copies of its inputs and outputs
+    void *stage_ptr_ = nullptr;
+    size_t stage_cap_ = 0;
+    std::vector<Item> staged_;
+    std::vector<uint8_t> redirected_;  // per item: payloads go through staging
+    const Item *orig_ = nullptr;       // the caller's items of the current batch
     std::vector<std::thread> threads_;
     std::mutex call_mu_;  // one decode call at a time
     std::mutex mu_;
     std::condition_variable work_cv_, done_cv_;
     std::vector<Chunk> chunks_;
-    size_t next_ = 0, done_ = 0;
+    size_t done_ = 0;
+    uint64_t gen_ = 0;  // batches handed to the workers
     bool stop_ = false;
     uint32_t launches_ = 0;
     std::map<uint32_t, uint32_t> tuned_;
