@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 
 #include "kernels.h"
+#include "rounding.h"
 #include "tables.h"
 
 namespace mmr {
@@ -456,9 +457,10 @@ __global__ void __launch_bounds__(kIdctThreads) dv_idct_kernel(DvLaunch L) {
         }
         const float c1 = s_c1[lb][0] + s_c1[lb][1];
         const float near = 0.5f - (c1 * 0x1p-21f + 0x1p-30f);
-        const float r = rintf(value);
-        if (fabsf(value - r) < near) {
-            sample = (uint8_t)fminf(fmaxf(r, 0.0f), 255.0f);
+        float r;
+        const int32_t v = round_nearest(value, r);
+        if (fabsf(value - r) < near && fabsf(value) < 0x1p22f) {
+            sample = (uint8_t)min(max(v, 0), 255);
         } else {
             const double e = mode ? exact_248(s_c[lb], y, x) : exact_88(s_c[lb], y, x);
             sample = (uint8_t)fmin(fmax(round(e), 0.0), 255.0);

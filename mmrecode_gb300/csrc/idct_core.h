@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "rounding.h"
 #include "tables.h"
 
 namespace mmr {
@@ -99,12 +100,17 @@ __device__ __forceinline__ float stage_rows(const int16_t *coef, const int32_t *
 // Sample of an fp32 transform value. Rounding it provably equals rounding the
 // binary64 value when no half-integer lies within delta of acc, i.e. when acc
 // is closer than 0.5 - delta to its nearest integer (with delta >= 0.5 nothing
-// is certain); the exact pass settles the rest, ties included, so rintf's
-// ties-to-even never decides a sample. Clamping after an agreed rounding agrees.
+// is certain); the exact pass settles the rest, ties included, so the rounding
+// mode's ties-to-even never decides a sample. Clamping after an agreed rounding
+// agrees.
+//
+// round_nearest (rounding.h) avoids conversion instructions; larger |acc| than
+// it handles is left to the exact pass.
 __device__ __forceinline__ uint32_t round_sample(float acc, float near, bool &unsure) {
-    const float r = rintf(acc);
-    unsure = !(fabsf(acc - r) < near);
-    return (uint32_t)fminf(fmaxf(r + 128.0f, 0.0f), 255.0f);
+    float r;
+    const int32_t v = round_nearest(acc, r) + 128;
+    unsure = !(fabsf(acc - r) < near && fabsf(acc) < 0x1p22f);
+    return (uint32_t)min(max(v, 0), 255);
 }
 
 // Transform of one staged block by its four threads; thread q produces output

@@ -23,6 +23,15 @@ namespace {
 
 constexpr int kFStride = 68;  // floats per staged block (16-byte rows, conflict-free over 8 blocks)
 
+// Four channel values saturated to 0..255 and packed, b0 in the low byte
+// (cvt.pack.sat: d = c << 16 | sat(a) << 8 | sat(b)).
+__device__ __forceinline__ uint32_t pack4_sat_u8(int32_t b0, int32_t b1, int32_t b2, int32_t b3) {
+    uint32_t hi, d;
+    asm("cvt.pack.sat.u8.s32.b32 %0, %1, %2, %3;" : "=r"(hi) : "r"(b3), "r"(b2), "r"(0));
+    asm("cvt.pack.sat.u8.s32.b32 %0, %1, %2, %3;" : "=r"(d) : "r"(b1), "r"(b0), "r"(hi));
+    return d;
+}
+
 template <int HM, int VM, int NM>
 struct FusedShape {
     static constexpr int BPM = HM * VM + 2;  // blocks per MCU
@@ -132,36 +141,40 @@ __device__ __forceinline__ void fused_tile(const JpegLaunch &L, const FusedLaunc
     }
     __syncthreads();
     // colour conversion (terminal_preview.rs:7308-7330, full range), four pixels per
-    // thread: one 32-bit luma load, three 32-bit RGB stores (pixels past the visible
-    // width are computed from padding and never copied out)
+    // thread: one 32-bit luma load, three 32-bit words of RGB. Rows whose bytes
+    // start 4-aligned (width a multiple of 4, aligned output) are stored straight
+    // from registers, consecutive threads writing consecutive words; others go
+    // through a shared-memory tile and a byte-exact copy. Pixels past the visible
+    // width are computed from padding and never stored.
     const uint32_t x0 = mx0 * HM * 8, y0 = my * VM * 8;
     const uint32_t vis_w = min((uint32_t)(nm * HM * 8), J.width - x0);
     const uint32_t vis_h = min((uint32_t)Sh::YH, J.height - y0);
+    const bool direct = ((reinterpret_cast<uintptr_t>(J.out) | J.width) & 3) == 0;
     for (uint32_t p = threadIdx.x; p < vis_h * (Sh::YW / 4); p += blockDim.x) {
         const uint32_t ly = p / (Sh::YW / 4), lx = (p - ly * (Sh::YW / 4)) * 4;
         if (lx >= vis_w) continue;
         const uint32_t yq = *reinterpret_cast<const uint32_t *>(S.y + ly * Sh::YW + lx);
         const uint8_t *cbr = S.c[0] + (ly / VM) * Sh::CW + lx / HM;
         const uint8_t *crr = S.c[1] + (ly / VM) * Sh::CW + lx / HM;
-        uint32_t bytes[3] = {0, 0, 0};
+        int32_t ch[12];
 #pragma unroll
         for (int k = 0; k < 4; k++) {
             const int32_t Y = (int32_t)((yq >> (8 * k)) & 0xff);
             const int32_t u = (int32_t)cbr[k / HM] - 128, w = (int32_t)crr[k / HM] - 128;
-            const int32_t r = Y + ((359 * w + 128) >> 8);
-            const int32_t gg = Y - ((88 * u + 183 * w + 128) >> 8);
-            const int32_t b = Y + ((454 * u + 128) >> 8);
-            const uint32_t rgb[3] = {(uint32_t)(r < 0 ? 0 : r > 255 ? 255 : r),
-                                     (uint32_t)(gg < 0 ? 0 : gg > 255 ? 255 : gg),
-                                     (uint32_t)(b < 0 ? 0 : b > 255 ? 255 : b)};
-#pragma unroll
-            for (int c = 0; c < 3; c++) bytes[(3 * k + c) >> 2] |= rgb[c] << (8 * ((3 * k + c) & 3));
+            ch[3 * k + 0] = Y + ((359 * w + 128) >> 8);
+            ch[3 * k + 1] = Y - ((88 * u + 183 * w + 128) >> 8);
+            ch[3 * k + 2] = Y + ((454 * u + 128) >> 8);
         }
-        uint32_t *o = reinterpret_cast<uint32_t *>(S.rgb + ly * Sh::RW + lx * 3);
-        o[0] = bytes[0];
-        o[1] = bytes[1];
-        o[2] = bytes[2];
+        uint32_t word[3];
+#pragma unroll
+        for (int j = 0; j < 3; j++) word[j] = pack4_sat_u8(ch[4 * j], ch[4 * j + 1], ch[4 * j + 2], ch[4 * j + 3]);
+        uint32_t *o = direct ? reinterpret_cast<uint32_t *>(J.out + ((uint64_t)(y0 + ly) * J.width + x0 + lx) * 3)
+                             : reinterpret_cast<uint32_t *>(S.rgb + ly * Sh::RW + lx * 3);
+        o[0] = word[0];
+        o[1] = word[1];
+        o[2] = word[2];
     }
+    if (direct) return;  // uniform over the CTA
     __syncthreads();
     // rows out: 16-byte stores when the row is aligned, bytes otherwise
     const uint32_t row_bytes = vis_w * 3;
