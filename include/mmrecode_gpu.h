@@ -118,6 +118,9 @@ typedef struct mmr_gpu_batch_stats {
     /* inside entropy_ms: speculative slice decode, slice synchronisation + block prefix, final decode */
     double slice_spec_ms, slice_sync_ms, slice_decode_ms;
     uint32_t graph_replays; /* parts of the batch whose launches replayed a captured CUDA graph */
+    /* slices of the chunked entropy decoder, and those whose levels the final decode
+       pass redid instead of taking the speculative decode's */
+    uint64_t slices, slices_redone;
 } mmr_gpu_batch_stats;
 
 /*

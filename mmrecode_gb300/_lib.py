@@ -85,7 +85,7 @@ class BatchStats(ctypes.Structure):
                                       "idct_exact_samples")] + [
         ("launches", ctypes.c_uint32)] + [
         (n, ctypes.c_double) for n in ("slice_spec_ms", "slice_sync_ms", "slice_decode_ms")] + [
-        ("graph_replays", ctypes.c_uint32)]
+        ("graph_replays", ctypes.c_uint32), ("slices", ctypes.c_uint64), ("slices_redone", ctypes.c_uint64)]
 
 
 class TuneEntry(ctypes.Structure):

@@ -539,6 +539,8 @@ MMR_API mmr_status mmr_gpu_last_batch_stats(const mmr_gpu_context *context, mmr_
     stats->slice_sync_ms = t.slice_sync_ms;
     stats->slice_decode_ms = t.slice_decode_ms;
     stats->graph_replays = t.graph_replays;
+    stats->slices = t.slices;
+    stats->slices_redone = t.slices_redone;
     return finish(MMR_STATUS_OK, "");
 }
 

@@ -683,7 +683,8 @@ Probe probe_packet(uint32_t codec, const uint8_t *data, size_t len) {
 
 struct Engine::Impl {
     DevBuf d_in, d_tok, d_blob, d_tile_tok, d_tile_rst, d_rsts, d_results, d_coef, d_dc, d_planes, d_out, d_dvcoef,
-        d_modes, d_flags, d_segerr, d_vlc, d_fix, d_slot_item, d_ivs, d_sync, d_spec, d_prefix, d_events, d_ivkey;
+        d_modes, d_flags, d_segerr, d_vlc, d_fix, d_slot_item, d_ivs, d_sync, d_spec, d_prefix, d_events, d_ivkey,
+        d_own, d_match, d_redo, d_scratch, d_scratch_dc, d_blkmap;
     PinBuf h_blob, h_back;
     std::vector<uint32_t> vlc;
     // stage boundaries: start, uploads, scan, entropy, idct, dv, rgb, end
@@ -1120,6 +1121,16 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
         I.d_events.ensure(std::max<size_t>(n_slots * sizeof(SliceEvent), 256));
         I.d_ivs.ensure(std::max<size_t>(items_small.size() * sizeof(IvInfo), 256));
         I.d_ivkey.ensure(std::max<size_t>(items_small.size() * 8, 256));
+        // levels the speculative decode stores: every block once, plus the unused
+        // tail of each slot's last chunk
+        const uint64_t scratch_blocks = blocks + n_slots * kOwnChunkBlocks;
+        if (scratch_blocks > 0xffffffffull) throw std::runtime_error("batch too large for the chunked entropy decoder");
+        I.d_own.ensure(std::max<size_t>(n_slots * sizeof(SliceOwn), 256));
+        I.d_match.ensure(std::max<size_t>(n_slots * sizeof(SliceMatch), 256));
+        I.d_redo.ensure(std::max<size_t>(n_slots * 4, 256));
+        I.d_scratch.ensure(std::max<size_t>(scratch_blocks * 128, 256));
+        I.d_scratch_dc.ensure(std::max<size_t>(scratch_blocks * 2, 256));
+        I.d_blkmap.ensure(std::max<size_t>(blocks * 4, 256));
 
         uint8_t *d_in = I.d_in.as<uint8_t>();
         auto in_ptr = [&](size_t i) -> const uint8_t * { return items[i].dev_data ? items[i].dev_data : d_in + in_off[i]; };
@@ -1162,10 +1173,12 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
             o_fcta[v] = blob.add_vec(fcta[v]);
         }
 
-        uint32_t zero_counters[2] = {0, 0};
-        size_t o_fixcount = blob.add(zero_counters, 8);
+        uint32_t zero_counters[4] = {0, 0, 0, 0};  // fixup entries, exact samples, slices redone, slices
+        size_t o_fixcount = blob.add(zero_counters, sizeof(zero_counters));
         uint32_t zero_dirty[2 * kSyncPasses] = {};  // changed-exit counts, then work counters
         size_t o_dirty = blob.add(zero_dirty, sizeof(zero_dirty));
+        uint32_t zero_scratch[4] = {};  // scratch allocation counter
+        size_t o_scratch_next = blob.add(zero_scratch, sizeof(zero_scratch));
         size_t blob_size = std::max<size_t>(blob.bytes.size(), 256);
         I.d_blob.ensure(blob_size);
         I.h_blob.ensure(blob_size);
@@ -1177,7 +1190,7 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
         size_t back_ok = n * 4, back_seg = seg_first.back();
         size_t o_b1 = 0, o_b2 = align_up(back_j, 16), o_b3 = align_up(o_b2 + back_d, 16),
                o_b4 = align_up(o_b3 + back_ok, 16), o_b5 = align_up(o_b4 + back_seg, 16);
-        I.h_back.ensure(std::max<size_t>(o_b5 + 4, 256));
+        I.h_back.ensure(std::max<size_t>(o_b5 + 12, 256));
         uint8_t *hb = reinterpret_cast<uint8_t *>(I.h_back.ptr);
 
         // ------------------------------------------------------- launches
@@ -1235,7 +1248,17 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
         JL.events = I.d_events.as<SliceEvent>();
         JL.iv_key = I.d_ivkey.as<unsigned long long>();
         JL.sync_dirty = reinterpret_cast<uint32_t *>(db + o_dirty);
+        JL.own = I.d_own.as<SliceOwn>();
+        JL.match = I.d_match.as<SliceMatch>();
+        JL.redo = I.d_redo.as<uint32_t>();
+        JL.scratch = I.d_scratch.as<int16_t>();
+        JL.scratch_dc = I.d_scratch_dc.as<int16_t>();
+        JL.scratch_blocks = (uint32_t)scratch_blocks;
+        JL.scratch_next = reinterpret_cast<unsigned long long *>(db + o_scratch_next);
+        JL.blk_map = I.d_blkmap.as<uint32_t>();
         if (!jframes.empty()) {
+            if (n_slots) MMR_CUDA(cudaMemsetAsync(I.d_redo.ptr, 0, n_slots * 4, s));
+            if (blocks) MMR_CUDA(cudaMemsetAsync(I.d_blkmap.ptr, 0xff, blocks * 4, s));
             launch_jpeg_scan(JL, s);
             MMR_CUDA(record_event(I.ev[2], s, capturing));
             launch_jpeg_slices(JL, s, I.marks, capturing);
@@ -1298,7 +1321,7 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
         if (back_d) MMR_CUDA(cudaMemcpyAsync(hb + o_b2, db + o_dstates, back_d, cudaMemcpyDeviceToHost, s));
         if (back_ok) MMR_CUDA(cudaMemcpyAsync(hb + o_b3, db + o_itemok, back_ok, cudaMemcpyDeviceToHost, s));
         if (back_seg) MMR_CUDA(cudaMemcpyAsync(hb + o_b4, I.d_segerr.ptr, back_seg, cudaMemcpyDeviceToHost, s));
-        MMR_CUDA(cudaMemcpyAsync(hb + o_b5, db + o_fixcount + 4, 4, cudaMemcpyDeviceToHost, s));
+        MMR_CUDA(cudaMemcpyAsync(hb + o_b5, db + o_fixcount + 4, 12, cudaMemcpyDeviceToHost, s));
         for (size_t i = 0; i < n; i++) {
             Item &it = items[i];
             if (it.status != kOk || it.out_on_device || !it.out_bytes) continue;
@@ -1329,7 +1352,8 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
             for (const DevBuf *b : {&I.d_in, &I.d_tok, &I.d_blob, &I.d_tile_tok, &I.d_tile_rst, &I.d_rsts,
                                     &I.d_results, &I.d_coef, &I.d_dc, &I.d_planes, &I.d_out, &I.d_dvcoef, &I.d_modes,
                                     &I.d_flags, &I.d_segerr, &I.d_vlc, &I.d_fix, &I.d_slot_item, &I.d_ivs, &I.d_sync,
-                                    &I.d_spec, &I.d_prefix, &I.d_events, &I.d_ivkey})
+                                    &I.d_spec, &I.d_prefix, &I.d_events, &I.d_ivkey, &I.d_own, &I.d_match, &I.d_redo,
+                                    &I.d_scratch, &I.d_scratch_dc, &I.d_blkmap})
                 key.push_back((uintptr_t)b->ptr);
             for (size_t i = 0; i < n; i++) {
                 const Item &it = items[i];
@@ -1409,6 +1433,8 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
             times->jpeg_blocks = blocks;
             times->graph_replays = graph_replayed_ ? 1 : 0;
             times->idct_exact_samples = *reinterpret_cast<const uint32_t *>(hb + o_b5);
+            times->slices_redone = *reinterpret_cast<const uint32_t *>(hb + o_b5 + 4);
+            times->slices = *reinterpret_cast<const uint32_t *>(hb + o_b5 + 8);
             times->dv_blocks = dv_blocks;
             times->rgb_pixels = rgbfirst.back();
             times->input_bytes = 0;

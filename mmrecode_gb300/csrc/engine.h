@@ -81,6 +81,8 @@ struct EngineTimes {
     uint64_t input_bytes = 0, output_bytes = 0, jpeg_blocks = 0, dv_blocks = 0, rgb_pixels = 0;
     uint64_t idct_exact_samples = 0;  // MJPEG samples recomputed in exact binary64 order
     uint32_t graph_replays = 0;       // batches whose launches replayed a captured CUDA graph
+    uint64_t slices = 0;              // slices of the chunked entropy decoder
+    uint64_t slices_redone = 0;       // of which the final decode pass redid (the rest were placed)
 };
 
 class Engine {

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "kernels.h"
 #include "rounding.h"
 #include "tables.h"
 
@@ -69,13 +70,24 @@ __device__ __forceinline__ uint8_t exact_sample(const int32_t *c, int stride, in
     return exact_finish(t, y);
 }
 
-// Dequantises block g into fp32 rows q and q+4 of `blk` (the product of an
+// The 64 levels of block g: in the speculative decode's scratch arena when the
+// block map points there, else in the coefficient arena (any map value past the
+// arena, the reset value included, means in place).
+__device__ __forceinline__ const int16_t *block_levels(const JpegLaunch &L, uint64_t g) {
+    if (L.blk_map) {
+        const uint32_t v = L.blk_map[g];
+        if (v < L.scratch_blocks) return L.scratch + (uint64_t)v * 64;
+    }
+    return L.coef + g * 64;
+}
+
+// Dequantises block g (its levels at `levels`) into fp32 rows q and q+4 of `blk` (the product of an
 // int16 level and an 8-bit quantiser is exact in fp32; the DC is the decoder's
 // dequantised int32, rounded to fp32 like every c in the bound). Returns the
 // sum of |c| over the two rows.
-__device__ __forceinline__ float stage_rows(const int16_t *coef, const int32_t *dc, uint64_t g, uint32_t q,
+__device__ __forceinline__ float stage_rows(const int16_t *levels, const int32_t *dc, uint64_t g, uint32_t q,
                                             const float *Qf, float *blk) {
-    const int4 *src = reinterpret_cast<const int4 *>(coef + g * 64);
+    const int4 *src = reinterpret_cast<const int4 *>(levels);
     float l1 = 0.0f;
 #pragma unroll
     for (int h = 0; h < 2; h++) {

@@ -87,7 +87,7 @@ __device__ __forceinline__ void fused_tile(const JpegLaunch &L, const FusedLaunc
     }
     __syncthreads();  // q, n
     float *blk = S.f + lb * kFStride;
-    float l1 = valid ? stage_rows(L.coef, L.dc, g, q, S.q[comp], blk) : 0.0f;
+    float l1 = valid ? stage_rows(block_levels(L, g), L.dc, g, q, S.q[comp], blk) : 0.0f;
 #pragma unroll
     for (int o = 1; o < 4; o <<= 1) l1 += __shfl_xor_sync(0xffffffffu, l1, o);
     __syncwarp();
@@ -123,9 +123,10 @@ __device__ __forceinline__ void fused_tile(const JpegLaunch &L, const FusedLaunc
                 const uint32_t bc = bi < HM * VM ? 0 : bi - HM * VM + 1;
                 const uint64_t bg = S.blk[b];
                 const uint16_t *Q = L.quant + F.quant_off + comps[bc].q * 64;
+                const int16_t *lv = block_levels(L, bg);
                 int32_t crow[8];
 #pragma unroll
-                for (int u = 0; u < 8; u++) crow[u] = (int32_t)L.coef[bg * 64 + v * 8 + u] * (int32_t)Q[v * 8 + u];
+                for (int u = 0; u < 8; u++) crow[u] = (int32_t)lv[v * 8 + u] * (int32_t)Q[v * 8 + u];
                 if (v == 0) crow[0] = L.dc[bg];
                 const double tv = exact_row(crow, (int)x);
                 double t[8];

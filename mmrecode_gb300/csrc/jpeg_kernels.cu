@@ -488,7 +488,7 @@ __global__ void __launch_bounds__(kIdctThreads, 4) idct_kernel(JpegLaunch L) {
     const bool valid = local < nblk;
     const uint64_t g = R.first + local;
     float *blk = s_f + lb * kIdctStride;
-    float l1 = valid ? stage_rows(L.coef, L.dc, g, q, s_q, blk) : 0.0f;
+    float l1 = valid ? stage_rows(block_levels(L, g), L.dc, g, q, s_q, blk) : 0.0f;
 #pragma unroll
     for (int o = 1; o < 4; o <<= 1) l1 += __shfl_xor_sync(0xffffffffu, l1, o);
     __syncwarp();
@@ -545,7 +545,7 @@ __global__ void __launch_bounds__(256) idct_fixup_kernel(JpegLaunch L) {
         const JComp *C = &L.comps[F->comp_off + L.ranges[r].comp];
         const uint16_t *Q = L.quant + F->quant_off + C->q * 64;
         int32_t c[64];
-        const int4 *src = reinterpret_cast<const int4 *>(L.coef + g * 64);
+        const int4 *src = reinterpret_cast<const int4 *>(block_levels(L, g));
 #pragma unroll
         for (int k = 0; k < 8; k++) {
             int4 v = src[k];

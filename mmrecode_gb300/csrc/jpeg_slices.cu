@@ -171,7 +171,42 @@ __global__ void slice_plan_kernel(JpegLaunch L) {
 
 // ------------------------------------------------------ speculative pass ---
 
+// Stores the staged block as owned block n of the slot (allocating a scratch
+// chunk at each chunk's first block) and clears the stage; false when the slot's
+// chunks or the arena are exhausted.
+__device__ __forceinline__ bool store_owned(const JpegLaunch &L, uint32_t slot, uint32_t n, uint32_t &chunk_base,
+                                            int4 *stage4, int32_t dc_diff) {
+    const uint32_t c = n / kOwnChunkBlocks, i = n % kOwnChunkBlocks;
+    if (i == 0) {
+        if (c >= (uint32_t)kOwnChunks) return false;
+        const unsigned long long first = atomicAdd(L.scratch_next, (unsigned long long)kOwnChunkBlocks);
+        if (first + kOwnChunkBlocks > L.scratch_blocks) return false;
+        chunk_base = (uint32_t)first;
+        L.own[slot].chunk[c] = chunk_base;
+    }
+    int4 *dst = reinterpret_cast<int4 *>(L.scratch + (uint64_t)(chunk_base + i) * 64);
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+        dst[q] = stage4[q];
+        stage4[q] = make_int4(0, 0, 0, 0);
+    }
+    L.scratch_dc[chunk_base + i] = (int16_t)dc_diff;
+    return true;
+}
+
+// Besides the exit state, checkpoints and counts, the speculative decode stores
+// the levels of the blocks it owns along its own path (SliceOwn): blocks whose DC
+// symbol starts at or past the slice start and before the slice end, the last
+// one decoded to completion past the end.
 __global__ void __launch_bounds__(kSliceThreads) slice_spec_kernel(JpegLaunch L) {
+    __shared__ __align__(16) int16_t s_stage[kSliceThreads * kStride];
+    __shared__ uint8_t s_zz[64];
+    int16_t *stage = s_stage + threadIdx.x * kStride;
+    int4 *stage4 = reinterpret_cast<int4 *>(stage);
+#pragma unroll
+    for (int q = 0; q < 8; q++) stage4[q] = make_int4(0, 0, 0, 0);
+    if (threadIdx.x < 64) s_zz[threadIdx.x] = c_slice_zz[threadIdx.x];
+    __syncthreads();
     const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
     SliceRef s;
     if (!slice_ref(L, slot, s)) return;
@@ -183,8 +218,19 @@ __global__ void __launch_bounds__(kSliceThreads) slice_spec_kernel(JpegLaunch L)
     out.pad = 0;
 #pragma unroll
     for (int c = 0; c < 4; c++) out.dc[c] = 0;
-    if (s.last) {  // nothing reads the last slice's exit or counts
+    SliceOwn *own = L.own + slot;
+    {
+        SliceMatch m;  // a first slice starts true; the sync pass finds the others' point
+        m.q = guess ? kMatchNone : kMatchStart;
+        m.blocks = 0;
+#pragma unroll
+        for (int c = 0; c < 4; c++) m.dc[c] = 0;
+        L.match[slot] = m;
+    }
+    if (s.last) {  // nothing reads the last slice's exit or counts; the decode pass redoes it
         L.sync[slot] = out;
+        own->n = 0;
+        own->ok = 0;
         return;
     }
     const JFrame &F = *s.F;
@@ -213,18 +259,23 @@ __global__ void __launch_bounds__(kSliceThreads) slice_spec_kernel(JpegLaunch L)
     uint32_t q = 0, recorded = 0;
     uint32_t next_mark = guess ? mark_at(0) : 0xffffffffu;
     unsigned long long exit_state = kStErr;
+    bool entered = false;  // at or past the slice start
+    bool own_blk = false;  // the block in progress is owned
+    bool own_ok = true;    // the owned blocks so far are stored
+    uint32_t own_n = 0, chunk_base = 0;
     for (;;) {
         const uint32_t pr = r.used;
         if (pr >= end) {
             exit_state = pack_state(p0 + pr, si, k);
             break;
         }
+        entered |= pr >= lead;
         if (pr >= next_mark) {
             while (pr >= mark_at(q)) {
                 SlicePoint cp;
                 cp.state = pack_state(p0 + pr, si, k);
                 cp.blocks = blocks;
-                cp.pad = 0;
+                cp.own_next = own_n + (own_blk && k != 0 ? 1u : 0u);
 #pragma unroll
                 for (int c = 0; c < 4; c++) cp.dc[c] = dc[c] + (tb.comp == (uint32_t)c ? dcv : 0);
                 sp->cp[q] = cp;
@@ -235,13 +286,15 @@ __global__ void __launch_bounds__(kSliceThreads) slice_spec_kernel(JpegLaunch L)
         }
         const int k0 = k;
         blocks += k0 == 0;
+        own_blk = k0 == 0 ? entered : own_blk;
         int32_t val;
         uint16_t err;
         uint32_t eb;
         if (!decode_symbol(r, lim - pr, k0 == 0 ? tb.dc : tb.ac, L.symbols, k, val, err, eb)) {
             if (!guess || err == kBarrierErr) break;  // exit_state stays kStErr
             // A decode from a guessed state met an invalid symbol: start again one bit
-            // later; what came before cannot lead to the exit, so its checkpoints go.
+            // later; what came before cannot lead to the exit, so its checkpoints go,
+            // and the owned blocks start again too (this path was not the true one).
             for (uint32_t x = 0; x < (uint32_t)kSliceCheckpoints; x++)
                 if (recorded & (1u << x)) sp->cp[x].state = kStErr;
             recorded = 0;
@@ -252,17 +305,49 @@ __global__ void __launch_bounds__(kSliceThreads) slice_spec_kernel(JpegLaunch L)
             k = 1;
             si = 0;
             tb = block_tabs(L, F, si);
+            if (own_blk) {
+#pragma unroll
+                for (int x = 0; x < 8; x++) stage4[x] = make_int4(0, 0, 0, 0);
+            }
+            own_blk = false;
+            own_ok = true;
+            own_n = 0;
             bits_init(r, F.tok, tokbit + p0 + pr + 1, pr + 1);
             continue;
         }
+        if (own_blk && own_ok) stage[s_zz[k - 1]] = (int16_t)val;
         dcv = k0 == 0 ? val : dcv;
         if (k < 64) continue;
-        add_dc(dc, tb.comp, dcv);  // block complete
+        if (own_blk && own_ok) {  // block complete
+            own_ok = store_owned(L, slot, own_n, chunk_base, stage4, dcv);
+            own_n++;
+        }
+        own_blk = false;
+        add_dc(dc, tb.comp, dcv);
         dcv = 0;
         k = 0;
         si = si + 1 == F.sched_len ? 0 : si + 1;
         tb = block_tabs(L, F, si);
     }
+    // the owned block straddling the slice end is decoded to completion
+    if (exit_state != kStErr && own_blk && own_ok) {
+        while (k < 64) {
+            int32_t val;
+            uint16_t err;
+            uint32_t eb;
+            if (!decode_symbol(r, lim - r.used, tb.ac, L.symbols, k, val, err, eb)) {
+                own_ok = false;
+                break;
+            }
+            stage[s_zz[k - 1]] = (int16_t)val;
+        }
+        if (own_ok) {
+            own_ok = store_owned(L, slot, own_n, chunk_base, stage4, dcv);
+            own_n++;
+        }
+    }
+    own->n = own_n;
+    own->ok = own_ok && exit_state != kStErr;
     add_dc(dc, tb.comp, dcv);  // the block in progress is counted, with its DC if decoded
     if (guess) {
         for (uint32_t x = 0; x < (uint32_t)kSliceCheckpoints; x++)
@@ -270,7 +355,7 @@ __global__ void __launch_bounds__(kSliceThreads) slice_spec_kernel(JpegLaunch L)
         SlicePoint e;
         e.state = exit_state;
         e.blocks = blocks;
-        e.pad = 0;
+        e.own_next = own_n;
 #pragma unroll
         for (int c = 0; c < 4; c++) e.dc[c] = dc[c];
         sp->exit = e;
@@ -295,9 +380,15 @@ __device__ bool resync_slice(const JpegLaunch &L, uint32_t slot, const SliceRef 
 #pragma unroll
     for (int c = 0; c < 4; c++) out.dc[c] = 0;
     const unsigned long long old_exit = L.sync[slot].exit;
+    SliceMatch m;
+    m.q = kMatchNone;
+    m.blocks = 0;
+#pragma unroll
+    for (int c = 0; c < 4; c++) m.dc[c] = 0;
     if (from == kStErr) {
         out.exit = kStErr;
         L.sync[slot] = out;
+        L.match[slot] = m;
         return old_exit != kStErr;
     }
     const JFrame &F = *s.F;
@@ -337,6 +428,10 @@ __device__ bool resync_slice(const JpegLaunch &L, uint32_t slot, const SliceRef 
                     exit_state = e.state;
                     add_dc(dc, tb.comp, dcv);
                     dcv = 0;
+                    m.q = q;  // the true decode so far, where it meets the speculative one
+                    m.blocks = blocks;
+#pragma unroll
+                    for (int c = 0; c < 4; c++) m.dc[c] = dc[c];
                     blocks += e.blocks - cp.blocks;
 #pragma unroll
                     for (int c = 0; c < 4; c++) dc[c] += e.dc[c] - cp.dc[c];
@@ -368,6 +463,7 @@ __device__ bool resync_slice(const JpegLaunch &L, uint32_t slot, const SliceRef 
 #pragma unroll
     for (int c = 0; c < 4; c++) out.dc[c] = dc[c];
     L.sync[slot] = out;
+    L.match[slot] = m;
     return exit_state != old_exit;
 }
 
@@ -472,6 +568,92 @@ __global__ void slice_prefix_kernel(JpegLaunch L) {
     }
 }
 
+// ----------------------------------------------------------------- place ---
+
+// A thread per slice. The owned blocks that start after the point where the
+// slice's true decode met its speculative decode (SliceMatch) are final: their
+// DC predictors are settled as the final decode would (decoder.rs:507-515) and
+// the block map points at their levels. The final decode pass writes the blocks
+// before that point, and the whole slice when there is no such point, anything
+// failed, or it is the interval's last slice or owns the interval's last block
+// (their decode reports the interval's completion). A DC overflow among the
+// placed blocks also sends the whole slice there (reported with its position).
+// Returns true when the final decode pass has work in the slice.
+__device__ bool place_slice(const JpegLaunch &L, uint32_t slot, const SliceRef &s) {
+    const SliceSync y = L.sync[slot];
+    if (y.start == kStErr || y.start == kStGuess) return false;  // not reached: nothing to decode
+    const SlicePrefix P = L.prefix[slot];
+    const uint32_t B = s.v.blocks;
+    if (P.base >= B) return false;
+    const uint32_t nown = s.last ? B - P.base : min(y.blocks, B - P.base);
+    if (nown == 0) return false;
+    const SliceOwn *O = L.own + slot;
+    const SliceMatch M = L.match[slot];
+    uint32_t spec_first = 0;
+    bool usable = !s.last && P.base + nown < B && O->ok && M.q != kMatchNone && M.blocks <= nown;
+    if (usable && M.q != kMatchStart) spec_first = L.spec[slot].cp[M.q].own_next;
+    usable = usable && spec_first <= O->n && O->n - spec_first == nown - M.blocks;
+    if (usable && M.blocks < nown) {
+        const JFrame &F = *s.F;
+        const uint32_t sched_len = F.sched_len, mcu_cols = F.mcu_cols;
+        const uint32_t b0 = P.base + M.blocks;  // interval-relative block of the first placed one
+        const uint32_t mcu = L.items[s.item].y * F.ri + b0 / sched_len;
+        uint32_t mx = mcu % mcu_cols, my = mcu / mcu_cols, si = b0 % sched_len;
+        const JBlockRec *recs = L.brec + F.sched_off;
+        long long pred[4];
+#pragma unroll
+        for (int c = 0; c < 4; c++) pred[c] = P.dc[c] + M.dc[c];
+        for (uint32_t i = 0; i < nown - M.blocks; i++) {
+            const JBlockRec R = recs[si];
+            const uint64_t blk = F.blk_off + R.base_off + mx * R.mul_x + (uint64_t)my * R.mul_y;
+            const uint32_t own_i = spec_first + i;
+            const uint32_t sb = O->chunk[own_i / kOwnChunkBlocks] + own_i % kOwnChunkBlocks;
+            long long pc = 0;
+#pragma unroll
+            for (int c = 0; c < 4; c++)
+                if (R.comp == (uint32_t)c) pc = pred[c];
+            const long long pn = pc + L.scratch_dc[sb];
+            const long long d = pn * (long long)R.q0;
+            if (pn > INT32_MAX || pn < INT32_MIN || d > INT32_MAX || d < INT32_MIN) {
+                usable = false;
+                break;
+            }
+#pragma unroll
+            for (int c = 0; c < 4; c++)
+                if (R.comp == (uint32_t)c) pred[c] = pn;
+            L.dc[blk] = (int32_t)d;
+            L.blk_map[blk] = sb;
+            if (++si == sched_len) {
+                si = 0;
+                if (++mx == mcu_cols) {
+                    mx = 0;
+                    my++;
+                }
+            }
+        }
+    }
+    const uint32_t redo = usable ? M.blocks : 0xffffffffu;
+    L.redo[slot] = redo;
+    return redo != 0;
+}
+
+// Adds the lanes' flags to a counter, one atomic per warp.
+__device__ __forceinline__ void count_lanes(uint32_t *counter, bool flag) {
+    const uint32_t m = __ballot_sync(0xffffffffu, flag);
+    if ((threadIdx.x & 31) == 0 && m) atomicAdd(counter, (uint32_t)__popc(m));
+}
+
+__global__ void __launch_bounds__(kSliceThreads) slice_place_kernel(JpegLaunch L) {
+    const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+    SliceRef s;
+    const bool valid = slice_ref(L, slot, s);
+    count_lanes(L.fix_count + 3, valid);
+    bool redo = false;
+    if (valid) redo = place_slice(L, slot, s);
+    count_lanes(L.fix_count + 2, redo);
+}
+
+
 // ---------------------------------------------------------------- decode ---
 
 __device__ __forceinline__ void report(const JpegLaunch &L, const SliceRef &s, uint32_t slot, unsigned long long pos,
@@ -495,12 +677,14 @@ __global__ void __launch_bounds__(kSliceThreads) slice_decode_kernel(JpegLaunch 
     const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
     SliceRef s;
     if (!slice_ref(L, slot, s)) return;
+    const uint32_t redo = L.redo[slot];  // leading blocks to write; the rest are placed
+    if (!redo) return;
     const unsigned long long from = L.sync[slot].start;
     if (from == kStErr || from == kStGuess) return;
     const SlicePrefix P = L.prefix[slot];
     const uint32_t B = s.v.blocks;
     if (P.base >= B) return;
-    const uint32_t nown = s.last ? B - P.base : min(L.sync[slot].blocks, B - P.base);
+    const uint32_t nown = min(s.last ? B - P.base : min(L.sync[slot].blocks, B - P.base), redo);
     if (nown == 0) return;
     const JFrame &F = *s.F;
     const uint32_t iv = L.items[s.item].y;
@@ -609,6 +793,7 @@ __global__ void __launch_bounds__(kSliceThreads) slice_decode_kernel(JpegLaunch 
             stage4[q] = make_int4(0, 0, 0, 0);
         }
         L.dc[blk] = dq;
+        L.blk_map[blk] = kLevelsInPlace;  // (place may have mapped the first blocks before an overflow)
         if (b + 1 == B) {
             const unsigned long long endbit = p0 + r.used;
             report(L, s, slot, endbit, make_diag(kDiagNone, s.v.start + (uint32_t)((endbit + 7) / 8)), 1);
@@ -666,7 +851,7 @@ __global__ void slice_resolve_kernel(JpegLaunch L) {
 
 }  // namespace
 
-int jpeg_slice_launches(const JpegLaunch &L) { return L.n_items_small ? 6 + kSyncPasses : 0; }
+int jpeg_slice_launches(const JpegLaunch &L) { return L.n_items_small ? 7 + kSyncPasses : 0; }
 
 void launch_jpeg_slices(const JpegLaunch &L, cudaStream_t s, cudaEvent_t *marks, bool capturing) {
     auto mark = [&](int k) {
@@ -688,7 +873,10 @@ void launch_jpeg_slices(const JpegLaunch &L, cudaStream_t s, cudaEvent_t *marks,
         slice_prefix_kernel<<<ivgrid, 32 * warps_per_cta, 0, s>>>(L);
     }
     mark(1);
-    if (run) slice_decode_kernel<<<grid, kSliceThreads, 0, s>>>(L);
+    if (run) {
+        slice_place_kernel<<<grid, kSliceThreads, 0, s>>>(L);
+        slice_decode_kernel<<<grid, kSliceThreads, 0, s>>>(L);
+    }
     mark(2);
     if (run) slice_resolve_kernel<<<(L.n_items_small + 127) / 128, 128, 0, s>>>(L);
 }

@@ -51,6 +51,18 @@ struct JpegLaunch {
     unsigned long long *iv_key;  // per item: (position << 26 | slice) of its first event
     uint32_t *sync_dirty;        // per sync pass: slices whose exit state changed, then per pass the
                                  // next slot to take (2 x kSyncPasses, zeroed per batch)
+    // levels written by the speculative decode (SliceOwn): per slot what it owns,
+    // the scratch arena, its allocation counter (zeroed per batch), and per block
+    // where its levels are (scratch block, or kLevelsInPlace: the coefficient arena)
+    SliceOwn *own;
+    SliceMatch *match;           // per slot (written by the speculative and sync passes)
+    uint32_t *redo;              // per slot: leading owned blocks the final decode pass writes
+                                 // (0: none, UINT32_MAX: all; zeroed per batch)
+    int16_t *scratch;            // 64 levels per scratch block
+    int16_t *scratch_dc;         // DC difference per scratch block
+    uint32_t scratch_blocks;
+    unsigned long long *scratch_next;
+    uint32_t *blk_map;           // per block (all 0xff per batch); nullptr: levels in place
 };
 
 constexpr int kSyncPasses = 2;

@@ -113,12 +113,14 @@ struct SliceSync {
     uint32_t pad;
 };
 
-// A point of the speculative decode: its state and the counts accumulated before it.
+// A point of the speculative decode: its state and the counts accumulated before
+// it, and the index among its owned blocks (SliceOwn) of the first block that
+// starts at or after it.
 struct SlicePoint {
     unsigned long long state;
     uint32_t blocks;
     int32_t dc[4];
-    uint32_t pad;
+    uint32_t own_next;
 };
 
 // Checkpoints 64, 256, 1024 and 2048 bits into a slice (those inside it). The
@@ -132,6 +134,33 @@ constexpr uint32_t kSpecLead = 512;
 struct SliceSpec {
     SlicePoint exit;                      // end of the speculative decode
     SlicePoint cp[kSliceCheckpoints];     // state at the first symbol boundary past each mark
+};
+
+// The levels of the blocks a speculative decode owns along its own path (the
+// blocks whose DC symbol starts in [slice start, slice end), counted from its
+// last restart), written to a scratch arena in chunks of kOwnChunkBlocks while
+// the decode runs. Where the true decode of the slice meets the speculative one
+// (at the slice start for a slice's first slice, else at the checkpoint the sync
+// pass matched), every owned block that starts after that point is final; the
+// final decode pass writes only the blocks before it (all of them when there is
+// no such point, or anything went wrong).
+constexpr uint32_t kOwnChunkBlocks = 16;
+constexpr int kOwnChunks = 16;
+constexpr uint32_t kLevelsInPlace = 0xffffffffu;  // block map: levels in the coefficient arena
+
+struct SliceOwn {
+    uint32_t n;                 // owned blocks written
+    uint32_t ok;                // 1: all n are complete, error-free and stored
+    uint32_t chunk[kOwnChunks]; // first scratch block of each chunk
+};
+
+// Where the true decode of a slice met its speculative decode.
+constexpr uint32_t kMatchNone = 0xffffffffu;
+constexpr uint32_t kMatchStart = 4;  // a first slice: the speculative decode is the true one
+struct SliceMatch {
+    uint32_t q;        // checkpoint index, kMatchStart, or kMatchNone
+    uint32_t blocks;   // true blocks started before the point (counting the one in progress)
+    int32_t dc[4];     // their DC differences, per scan component
 };
 
 // Block index and DC predictors at a slice's start (interval-relative).

@@ -25,6 +25,8 @@ void accumulate_times(EngineTimes &a, const EngineTimes &t) {
     a.rgb_pixels += t.rgb_pixels;
     a.idct_exact_samples += t.idct_exact_samples;
     a.graph_replays += t.graph_replays;
+    a.slices += t.slices;
+    a.slices_redone += t.slices_redone;
 }
 
 // ------------------------------------------------------------------ pool ---
@@ -274,7 +276,10 @@ uint64_t Server::estimate_bytes(const Item &it) {
     const Probe p = probe_packet(it.codec, it.data, it.len);
     const uint64_t planar = p.status == kOk ? p.planar_bytes : 0;
     const uint64_t out = p.status == kOk ? (it.output == kOutRgb24 ? p.rgb_bytes : planar) : 0;
-    uint64_t b = 4 * (uint64_t)it.len + (planar * 5) / 2 + planar + 65536;  // tokens, slices, coefficients, scratch
+    // tokens and slice records (~8 B per compressed byte at the smallest automatic
+    // slice), coefficients in place and in the speculative decode's scratch
+    // (~4.5 B per sample), planes, fixed scratch
+    uint64_t b = 8 * (uint64_t)it.len + (planar * 9) / 2 + planar + 65536;
     if (!it.out_on_device) b += out;  // staged output
     return b;
 }
