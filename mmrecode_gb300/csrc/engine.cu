@@ -942,7 +942,7 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
                     }
                     F.slice_bits = slice_bits;
                     F.slot_first = (uint32_t)n_slots;
-                    F.slot_count = (uint32_t)((8 * (uint64_t)it.len + slice_bits - 1) / slice_bits + p.n_intervals);
+                    F.slot_count = (uint32_t)((8 * (uint64_t)it.len + slice_bits - 1) / slice_bits + 2 * (uint64_t)p.n_intervals);
                     n_slots += F.slot_count;
                 }
                 F.blk_off = blocks;

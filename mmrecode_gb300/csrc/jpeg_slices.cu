@@ -71,9 +71,11 @@ __device__ __forceinline__ BlockTabs block_tabs(const JpegLaunch &L, const JFram
 }
 
 // Bit offset of checkpoint q from the nominal slice start (UINT32_MAX past the slice).
+__constant__ uint32_t c_slice_marks[kSliceCheckpoints] = {64, 128, 256, 512, 768, 1024, 1536, 2048};
+
 __device__ __forceinline__ uint32_t mark_of(uint32_t q, uint32_t S) {
-    const uint32_t m = q == 0 ? 64u : 64u << (2 * q < 6 ? 2 * q : 5);  // 64, 256, 1024, 2048
-    return q < (uint32_t)kSliceCheckpoints && m < S ? m : 0xffffffffu;
+    const uint32_t m = q < (uint32_t)kSliceCheckpoints ? c_slice_marks[q] : 0xffffffffu;
+    return m < S ? m : 0xffffffffu;
 }
 
 __device__ __forceinline__ void add_dc(int32_t (&dc)[4], uint32_t comp, int32_t v) {
@@ -100,6 +102,15 @@ __device__ __forceinline__ bool slice_ref(const JpegLaunch &L, uint32_t slot, Sl
     return true;
 }
 
+// Nominal start (bits from the interval's start) and length of a slice that is
+// not its interval's last.
+__device__ __forceinline__ void slice_span(const SliceRef &s, uint32_t S, unsigned long long &start, uint32_t &len) {
+    start = (unsigned long long)s.j * S;
+    len = S;
+    if (s.v.tail && s.j + 2 == s.v.n_slices)  // the next is the split-off last slice
+        len = (uint32_t)((unsigned long long)(s.v.barrier - s.v.start) * 8 - s.v.tail - start);
+}
+
 __device__ __forceinline__ uint32_t clamp_u32(unsigned long long x) {
     return x > 0xffffffffull ? 0xffffffffu : (uint32_t)x;
 }
@@ -122,7 +133,7 @@ __global__ void slice_plan_kernel(JpegLaunch L) {
     uint32_t used = 0;
     for (uint32_t c = 0; c < n_int; c += 32) {
         const uint32_t iv = c + lane;
-        uint32_t n_s = 0, start = 0, barrier = 0, flags = 0, blocks = 0;
+        uint32_t n_s = 0, start = 0, barrier = 0, flags = 0, blocks = 0, tail = 0;
         if (iv < n_int) {
             bool dec = scan_ok;
             if (iv == 0) start = 0;
@@ -133,6 +144,10 @@ __global__ void slice_plan_kernel(JpegLaunch L) {
                 barrier = flags ? rst[iv].tok : n_tok;
                 const unsigned long long lbits = (unsigned long long)(barrier - start) * 8;
                 n_s = (uint32_t)max(1ull, (lbits + S - 1) / S);
+                if (lbits - (unsigned long long)(n_s - 1) * S > kSliceTail) {  // split the end off
+                    n_s++;
+                    tail = kSliceTail;
+                }
                 const uint32_t mcu0 = iv * F.ri, mcu1 = min(mcu0 + F.ri, F.total_mcus);
                 blocks = (mcu1 - mcu0) * F.sched_len;
             }
@@ -157,6 +172,8 @@ __global__ void slice_plan_kernel(JpegLaunch L) {
             v.n_slices = n_s;
             v.blocks = blocks;
             v.flags = flags;
+            v.tail = tail;
+            v.pad = 0;
             L.ivs[F.item_base + iv] = v;
             L.iv_key[F.item_base + iv] = ~0ull;
         }
@@ -234,8 +251,9 @@ __global__ void __launch_bounds__(kSliceThreads) slice_spec_kernel(JpegLaunch L)
         return;
     }
     const JFrame &F = *s.F;
-    const uint32_t S = F.slice_bits;
-    const unsigned long long nominal = (unsigned long long)s.j * S;
+    unsigned long long nominal;
+    uint32_t S;  // this slice's length
+    slice_span(s, F.slice_bits, nominal, S);
     // a guessed decode starts up to kSpecLead bits early; positions below are from p0
     const uint32_t lead = guess ? (uint32_t)min((unsigned long long)kSpecLead, nominal) : 0;
     const unsigned long long p0 = nominal - lead;
@@ -263,6 +281,7 @@ __global__ void __launch_bounds__(kSliceThreads) slice_spec_kernel(JpegLaunch L)
     bool own_blk = false;  // the block in progress is owned
     bool own_ok = true;    // the owned blocks so far are stored
     uint32_t own_n = 0, chunk_base = 0;
+    unsigned long long own_end = 0;  // position after the last stored one
     for (;;) {
         const uint32_t pr = r.used;
         if (pr >= end) {
@@ -321,6 +340,7 @@ __global__ void __launch_bounds__(kSliceThreads) slice_spec_kernel(JpegLaunch L)
         if (own_blk && own_ok) {  // block complete
             own_ok = store_owned(L, slot, own_n, chunk_base, stage4, dcv);
             own_n++;
+            own_end = p0 + r.used;
         }
         own_blk = false;
         add_dc(dc, tb.comp, dcv);
@@ -344,8 +364,10 @@ __global__ void __launch_bounds__(kSliceThreads) slice_spec_kernel(JpegLaunch L)
         if (own_ok) {
             own_ok = store_owned(L, slot, own_n, chunk_base, stage4, dcv);
             own_n++;
+            own_end = p0 + r.used;
         }
     }
+    own->last_end = own_end;
     own->n = own_n;
     own->ok = own_ok && exit_state != kStErr;
     add_dc(dc, tb.comp, dcv);  // the block in progress is counted, with its DC if decoded
@@ -392,9 +414,10 @@ __device__ bool resync_slice(const JpegLaunch &L, uint32_t slot, const SliceRef 
         return old_exit != kStErr;
     }
     const JFrame &F = *s.F;
-    const uint32_t S = F.slice_bits;
+    unsigned long long nominal;
+    uint32_t S;  // this slice's length
+    slice_span(s, F.slice_bits, nominal, S);
     const unsigned long long p0 = from >> 16;
-    const unsigned long long nominal = (unsigned long long)s.j * S;
     const uint32_t rel = (uint32_t)(p0 - nominal);  // < one symbol: from is the first boundary past nominal
     const unsigned long long lbits = (unsigned long long)(s.v.barrier - s.v.start) * 8;
     const uint32_t lim = clamp_u32(lbits - p0);
@@ -570,15 +593,27 @@ __global__ void slice_prefix_kernel(JpegLaunch L) {
 
 // ----------------------------------------------------------------- place ---
 
+// Records a slice's first event: an error, or the interval's completion.
+__device__ __forceinline__ void report(const JpegLaunch &L, const SliceRef &s, uint32_t slot, unsigned long long pos,
+                                       const Diag &d, uint32_t complete) {
+    SliceEvent e;
+    e.diag = d;
+    e.complete = complete;
+    L.events[slot] = e;
+    atomicMin(&L.iv_key[s.item], (pos << kKeyBits) | s.j);
+}
+
+
 // A thread per slice. The owned blocks that start after the point where the
 // slice's true decode met its speculative decode (SliceMatch) are final: their
 // DC predictors are settled as the final decode would (decoder.rs:507-515) and
 // the block map points at their levels. The final decode pass writes the blocks
 // before that point, and the whole slice when there is no such point, anything
-// failed, or it is the interval's last slice or owns the interval's last block
-// (their decode reports the interval's completion). A DC overflow among the
-// placed blocks also sends the whole slice there (reported with its position).
-// Returns true when the final decode pass has work in the slice.
+// failed, or it is the interval's last slice
+// (its decode reports the interval's completion; a placed last block reports it
+// here). A DC overflow among the placed blocks also sends the whole slice there
+// (reported with its position). Returns true when the final decode pass has
+// work in the slice.
 __device__ bool place_slice(const JpegLaunch &L, uint32_t slot, const SliceRef &s) {
     const SliceSync y = L.sync[slot];
     if (y.start == kStErr || y.start == kStGuess) return false;  // not reached: nothing to decode
@@ -590,7 +625,7 @@ __device__ bool place_slice(const JpegLaunch &L, uint32_t slot, const SliceRef &
     const SliceOwn *O = L.own + slot;
     const SliceMatch M = L.match[slot];
     uint32_t spec_first = 0;
-    bool usable = !s.last && P.base + nown < B && O->ok && M.q != kMatchNone && M.blocks <= nown;
+    bool usable = !s.last && O->ok && M.q != kMatchNone && M.blocks <= nown;
     if (usable && M.q != kMatchStart) spec_first = L.spec[slot].cp[M.q].own_next;
     usable = usable && spec_first <= O->n && O->n - spec_first == nown - M.blocks;
     if (usable && M.blocks < nown) {
@@ -632,6 +667,10 @@ __device__ bool place_slice(const JpegLaunch &L, uint32_t slot, const SliceRef &
             }
         }
     }
+    if (usable && M.blocks < nown && P.base + nown == B) {  // the interval's last block, placed
+        const unsigned long long endbit = O->last_end;
+        report(L, s, slot, endbit, make_diag(kDiagNone, s.v.start + (uint32_t)((endbit + 7) / 8)), 1);
+    }
     const uint32_t redo = usable ? M.blocks : 0xffffffffu;
     L.redo[slot] = redo;
     return redo != 0;
@@ -656,14 +695,6 @@ __global__ void __launch_bounds__(kSliceThreads) slice_place_kernel(JpegLaunch L
 
 // ---------------------------------------------------------------- decode ---
 
-__device__ __forceinline__ void report(const JpegLaunch &L, const SliceRef &s, uint32_t slot, unsigned long long pos,
-                                       const Diag &d, uint32_t complete) {
-    SliceEvent e;
-    e.diag = d;
-    e.complete = complete;
-    L.events[slot] = e;
-    atomicMin(&L.iv_key[s.item], (pos << kKeyBits) | s.j);
-}
 
 __global__ void __launch_bounds__(kSliceThreads) slice_decode_kernel(JpegLaunch L) {
     __shared__ __align__(16) int16_t s_stage[kSliceThreads * kStride];

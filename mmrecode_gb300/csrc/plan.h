@@ -83,7 +83,7 @@ struct JFrame {
     uint32_t n_blocks;
     uint32_t item;          // caller's batch item
     uint32_t slot_first;    // first slice slot of the chunked entropy decoder
-    uint32_t slot_count;    // slots reserved: ceil(8 * in_len / slice_bits) + n_intervals
+    uint32_t slot_count;    // slots reserved: ceil(8 * in_len / slice_bits) + 2 * n_intervals
     uint32_t slice_bits;    // bits per slice (multiple of 32, >= 128)
     uint32_t pad;
 };
@@ -102,7 +102,14 @@ struct IvInfo {
     uint32_t n_slices;    // 0: not decoded (header failure, or no RST precedes it)
     uint32_t blocks;      // coefficient blocks in the interval
     uint32_t flags;       // bit 0: the barrier is an RST marker
+    uint32_t tail;        // bits of the last slice when the interval's end was split off (else 0)
+    uint32_t pad;
 };
+
+// Slices are slice_bits long from the interval's start, except that the last one
+// is at most kSliceTail bits: when the remainder is longer, its end is split off
+// as an extra slice (the final decode pass redoes every last slice in full).
+constexpr uint32_t kSliceTail = 256;
 
 // Per slice: the state its decode starts from and what that decode produced.
 struct SliceSync {
@@ -123,12 +130,14 @@ struct SlicePoint {
     uint32_t own_next;
 };
 
-// Checkpoints 64, 256, 1024 and 2048 bits into a slice (those inside it). The
-// speculative decode of a slice starts kSpecLead bits before the slice: the
-// synchronisation distance of Huffman-coded JPEG data is a few hundred bits, so
-// it has usually met the true decode by the first checkpoint, and a re-decode
-// from the predecessor's exit matches there after a few symbols.
-constexpr int kSliceCheckpoints = 4;
+// Checkpoints 64, 128, 256, 512, 768, 1024, 1536 and 2048 bits into a slice
+// (those inside it). The speculative decode of a slice starts kSpecLead bits
+// before the slice: the synchronisation distance of Huffman-coded JPEG data is a
+// few hundred bits, so it has usually met the true decode by the first
+// checkpoint, and a re-decode from the predecessor's exit matches there after a
+// few symbols; the later ones bound how far the final decode pass must redo a
+// slice whose speculative decode met the true one late.
+constexpr int kSliceCheckpoints = 8;
 constexpr uint32_t kSpecLead = 512;
 
 struct SliceSpec {
@@ -149,14 +158,15 @@ constexpr int kOwnChunks = 16;
 constexpr uint32_t kLevelsInPlace = 0xffffffffu;  // block map: levels in the coefficient arena
 
 struct SliceOwn {
-    uint32_t n;                 // owned blocks written
-    uint32_t ok;                // 1: all n are complete, error-free and stored
-    uint32_t chunk[kOwnChunks]; // first scratch block of each chunk
+    unsigned long long last_end; // bit position (from the interval's start) after the last one
+    uint32_t n;                  // owned blocks written
+    uint32_t ok;                 // 1: all n are complete, error-free and stored
+    uint32_t chunk[kOwnChunks];  // first scratch block of each chunk
 };
 
 // Where the true decode of a slice met its speculative decode.
 constexpr uint32_t kMatchNone = 0xffffffffu;
-constexpr uint32_t kMatchStart = 4;  // a first slice: the speculative decode is the true one
+constexpr uint32_t kMatchStart = 0xfffffffeu;  // a first slice: the speculative decode is the true one
 struct SliceMatch {
     uint32_t q;        // checkpoint index, kMatchStart, or kMatchNone
     uint32_t blocks;   // true blocks started before the point (counting the one in progress)
