@@ -324,10 +324,9 @@ __global__ void __launch_bounds__(kSliceThreads) slice_spec_kernel(JpegLaunch L)
             k = 1;
             si = 0;
             tb = block_tabs(L, F, si);
-            if (own_blk) {
+            // (the stage may hold a partial block, or one whose store failed)
 #pragma unroll
-                for (int x = 0; x < 8; x++) stage4[x] = make_int4(0, 0, 0, 0);
-            }
+            for (int x = 0; x < 8; x++) stage4[x] = make_int4(0, 0, 0, 0);
             own_blk = false;
             own_ok = true;
             own_n = 0;
