@@ -437,10 +437,14 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the oracle CPU-baseline sample")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0,
+                    help="budget of the oracle CPU-baseline sample (0: skip it)")
     ap.add_argument("--plain-frames", type=int, default=60)
     ap.add_argument("--serve-seconds", type=float, default=2.0, help="seconds per serving load level (0: skip)")
     ap.add_argument("--mixed", type=int, default=1, help="run the 512-frame mixed batch (0: skip)")
+    ap.add_argument("--graphs", type=int, default=1,
+                    help="replay repeated batches as CUDA graphs (0: direct launches, e.g. under ncu, which "
+                         "crashed the process while several engine threads captured graphs)")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
@@ -448,7 +452,7 @@ def main():
     world, rank, local = _dist()
     cores = os.cpu_count() or 1
     pool = None
-    if rank == 0 and world == 1:
+    if rank == 0 and world == 1 and args.cpu_seconds > 0:  # (0: no CPU baseline, e.g. under a profiler)
         pool = mp.get_context("spawn").Pool(cores)  # before any CUDA call
 
     import ctypes
@@ -478,6 +482,9 @@ def main():
     host_out = torch.empty(n * rgb_bytes, dtype=torch.uint8, pin_memory=True)
     ctx = m.Context(local)               # engines decoding parts of a batch concurrently
     ctx1 = m.Context(local, engines=1)   # one engine: kernels never overlap, for per-kernel timing
+    if not args.graphs:
+        ctx.set_graphs(False)
+        ctx1.set_graphs(False)
 
     def items(device_resident: bool):
         arr = (_lib.GpuItem * n)()
@@ -574,12 +581,11 @@ def main():
                                               "slice_spec", "slice_sync", "slice_decode")}
     # algorithmic bytes per launch of each kernel of the step (every kernel runs once per step)
     kernels = {
-        # reads the compressed tokens, writes 64 int16 levels + one int32 DC per block
-        "slice_decode_kernel": (stage_times["slice_decode"], in_bytes + blocks * 132),
-        # reads the tokens once more (no output beyond per-slice states)
-        "slice_spec_kernel": (stage_times["slice_spec"], in_bytes),
-        # reads levels + DC, writes interleaved RGB
-        "idct_rgb_kernel": (stage_times["idct"], blocks * 132 + n * rgb_bytes),
+        # reads the compressed tokens, stores the 64 int16 levels and the DC difference of
+        # every block it owns (the final levels of nearly all blocks)
+        "slice_spec_kernel": (stage_times["slice_spec"], in_bytes + blocks * 130),
+        # reads levels, dequantised DC and the block map entry, writes interleaved RGB
+        "idct_rgb_kernel": (stage_times["idct"], blocks * 136 + n * rgb_bytes),
     }
 
     def roof(name):
