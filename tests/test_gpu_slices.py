@@ -135,3 +135,32 @@ def test_autotune_picks_a_size_per_class_and_output_is_unchanged():
         ref = oracle.jpeg_decode(p)
         assert r.status == 0
         assert payload == b"".join(d for (_, _, d) in ref.frame.planes)
+
+
+def _flat_with_texture(seed, w, h):
+    """4:2:0 frame: flat grey left half (a few bits per block), noisy right half."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    y = np.full((h, w), 120, np.uint8)
+    y[:, w // 2:] = rng.integers(0, 256, (h, w - w // 2), dtype=np.uint8)
+    cw, ch = (w + 1) // 2, (h + 1) // 2
+    c = np.full((ch, cw), 128, np.uint8)
+    c[:, cw // 2:] = rng.integers(96, 160, (ch, cw - cw // 2), dtype=np.uint8)
+    return m.VideoFrame(m.YUV420P8, w, h, [m.Plane(y.tobytes(), w, w, h), m.Plane(c.tobytes(), cw, cw, ch),
+                                          m.Plane(c.copy().tobytes(), cw, cw, ch)], m.RANGE_FULL)
+
+
+def test_slices_owning_more_blocks_than_their_store_holds(ctx):
+    # without restart intervals a large slice of flat image owns thousands of
+    # blocks: more than a slice's stored levels can hold, so the final decode
+    # pass redoes it; output must not change
+    packets = [m.encode_jpeg(_flat_with_texture(320 + i, 640, 480), q, True, 0) for i, q in enumerate((50, 75))]
+    refs = [oracle.jpeg_decode(p) for p in packets]
+    for bits in (2048, 8192, 65536, 1 << 20):
+        ctx.set_slice_bits(bits)
+        results = ctx.decode_batch(packets, m.CODEC_MJPEG, m.OUTPUT_PLANAR)
+        for i, ((r, payload), ref) in enumerate(zip(results, refs)):
+            assert r.status == ref.status == 0, (bits, i, r.message)
+            f = m.frame_from_batch(r, payload)
+            assert_same_decode(0, "", frame_planes_gpu(f), ref, f"flat[{i}] slice_bits={bits}")
+    ctx.set_slice_bits(0)
