@@ -128,6 +128,36 @@ __device__ __forceinline__ bool plain_chunk(const uint8_t *in, uint32_t ds, uint
     return !ff;
 }
 
+// Bytes of a 16-byte chunk equal to b: bit i set when byte i (in address order) is b.
+__device__ __forceinline__ uint32_t byte_mask(const uint4 &v, uint32_t b) {
+    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+    uint32_t m = 0;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const uint32_t e = __vcmpeq4(w[i], b * 0x01010101u);  // 0xff per equal byte
+        m |= ((e >> 7) & 1u | (e >> 14) & 2u | (e >> 21) & 4u | (e >> 28) & 8u) << (4 * i);
+    }
+    return m;
+}
+
+// A chunk whose 0xFF bytes are all stuffed data bytes: each followed by 0x00 (the
+// next chunk's first byte for the last one), none next to another 0xFF, and the
+// byte before the chunk, when 0xFF, followed by 0x00 here. Then every byte is a
+// token except the stuffing zeros (parser.rs:385-391): returns true with their
+// positions clear in *keep. Chunks with a marker or fill bytes return false.
+// (p >= data_start; p + 16 <= end of the scanned range.)
+__device__ __forceinline__ bool stuffed_chunk(const uint8_t *in, uint32_t len, uint32_t ds, uint32_t p, const uint4 &v,
+                                              uint32_t *keep) {
+    const uint32_t ff = byte_mask(v, 0xff), zero = byte_mask(v, 0x00);
+    const uint32_t prev = p > ds && in[p - 1] == 0xff ? 1u : 0u;
+    if ((ff & (ff >> 1)) || (prev & ff)) return false;                     // 0xFF next to 0xFF
+    const uint32_t drop = ((ff << 1) | prev) & 0xffffu;                    // bytes after a 0xFF
+    if (drop & ~zero) return false;                                        // a marker code
+    if (ff & 0x8000u && (p + 16 >= len || in[p + 16] != 0x00)) return false;
+    *keep = ~drop & 0xffffu;
+    return true;
+}
+
 __global__ void __launch_bounds__(kScanThreads) scan_count_kernel(JpegLaunch L) {
     uint32_t t = blockIdx.x;
     TileRef tr = tile_ref(L, t);
@@ -138,8 +168,12 @@ __global__ void __launch_bounds__(kScanThreads) scan_count_kernel(JpegLaunch L) 
     uint32_t tokens = 0, rsts = 0;
     unsigned long long term = ~0ull;
     uint4 v;
-    if (p0 >= ds && p0 + 16 <= len && plain_chunk(in, ds, p0, &v)) {
+    uint32_t keep;
+    const bool in_range = p0 >= ds && p0 + 16 <= len;
+    if (in_range && plain_chunk(in, ds, p0, &v)) {
         tokens = 16;
+    } else if (in_range && (((uintptr_t)in) & 15) == 0 && stuffed_chunk(in, len, ds, p0, v, &keep)) {
+        tokens = __popc(keep);
     } else if (p0 < len) {
         bool prev_ff = p0 > ds && in[p0 - 1] == 0xff;
 #pragma unroll 4
@@ -221,9 +255,13 @@ __global__ void __launch_bounds__(kScanThreads) scan_emit_kernel(JpegLaunch L) {
     uint8_t kinds[16], bytes[16];
     uint32_t tokens = 0, rsts = 0;
     uint4 v;
-    const bool plain = p0 >= ds && p0 + 16 <= term && plain_chunk(in, ds, p0, &v);
+    uint32_t keep = 0xffffu;  // tokens of a plain or stuffed chunk
+    const bool in_range = p0 >= ds && p0 + 16 <= term;
+    bool plain = in_range && plain_chunk(in, ds, p0, &v);
+    const bool stuffed = !plain && in_range && (((uintptr_t)in) & 15) == 0 && stuffed_chunk(in, len, ds, p0, v, &keep);
+    plain |= stuffed;
     if (plain) {
-        tokens = 16;
+        tokens = __popc(keep);
     } else {
         bool prev_ff = p0 > ds && p0 < len && in[p0 - 1] == 0xff;
 #pragma unroll
@@ -249,8 +287,11 @@ __global__ void __launch_bounds__(kScanThreads) scan_emit_kernel(JpegLaunch L) {
     uint8_t *st = s_tok + mis + etok;
     if (plain) {
         const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+        uint32_t n = 0;
 #pragma unroll
-        for (int i = 0; i < 16; i++) st[i] = (uint8_t)(w[i >> 2] >> (8 * (i & 3)));
+        for (int i = 0; i < 16; i++) {
+            if (keep & (1u << i)) st[n++] = (uint8_t)(w[i >> 2] >> (8 * (i & 3)));
+        }
     } else {
         uint32_t tok_pos = tile_tok + etok, n = 0;
         uint32_t rst_idx = L.tile_rst[t] + erst;
