@@ -116,13 +116,22 @@ __device__ __forceinline__ float stage_rows(const int16_t *levels, const int32_t
 // mode's ties-to-even never decides a sample. Clamping after an agreed rounding
 // agrees.
 //
-// round_nearest (rounding.h) avoids conversion instructions; larger |acc| than
-// it handles is left to the exact pass.
-__device__ __forceinline__ uint32_t round_sample(float acc, float near, bool &unsure) {
+// round_nearest (rounding.h) avoids conversion instructions and is exact for
+// |acc| < 2^22. Larger values need no check of their own: |s| <= C1/4 and
+// |acc - s| <= delta give C1 > 2^24 for |acc| >= 2^22, so near < 0 and the
+// sample is unsure already. Returns the unclamped integer sample (+128).
+__device__ __forceinline__ int32_t round_sample(float acc, float near, bool &unsure) {
     float r;
     const int32_t v = round_nearest(acc, r) + 128;
-    unsure = !(fabsf(acc - r) < near && fabsf(acc) < 0x1p22f);
-    return (uint32_t)min(max(v, 0), 255);
+    unsure = !(fabsf(acc - r) < near);
+    return v;
+}
+
+// Two samples saturated to 0..255 in one instruction: a in byte 0, b in byte 1.
+__device__ __forceinline__ uint32_t sat_pair_u8(int32_t a, int32_t b) {
+    uint32_t d;
+    asm("cvt.pack.sat.u8.s32.b32 %0, %1, %2, %3;" : "=r"(d) : "r"(b), "r"(a), "r"(0));
+    return d;
 }
 
 // Transform of one staged block by its four threads; thread q produces output
@@ -175,8 +184,9 @@ __device__ __forceinline__ unsigned long long idct_block(const float *blk, uint3
             o = fmaf(c_idct32[y * 8 + 7], t[7], o);
             const uint32_t col = side ? 7 - q : q;
             bool u0, u1;
-            out[y * stride + col] = (uint8_t)round_sample(e + o, near, u0);
-            out[(7 - y) * stride + col] = (uint8_t)round_sample(e - o, near, u1);
+            const uint32_t pair = sat_pair_u8(round_sample(e + o, near, u0), round_sample(e - o, near, u1));
+            out[y * stride + col] = (uint8_t)pair;
+            out[(7 - y) * stride + col] = (uint8_t)(pair >> 8);
             bits |= (u0 ? 1u : 0u) << (2 * y + side);
             bits |= (u1 ? 1u : 0u) << (2 * (7 - y) + side);
         }
