@@ -38,7 +38,7 @@ typedef struct mmr_gpu_config {
     int32_t device;   /* CUDA device ordinal */
     uint32_t flags;   /* reserved, 0 */
     uint32_t engines; /* batches decoded concurrently, each on its own CUDA stream with its own
-                         device arenas; 0 = 3. A large batch is split over them so that planning,
+                         device arenas; 0 = 4. A large batch is split over them so that planning,
                          uploads, kernels and read-backs of its parts overlap. */
 } mmr_gpu_config;
 

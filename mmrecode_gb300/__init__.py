@@ -220,7 +220,7 @@ class Context:
     """A GPU decode context: engines (CUDA stream + device arenas each) that decode batches."""
 
     def __init__(self, device: int = 0, engines: int = 0):
-        """``engines``: batches decoded concurrently (own CUDA stream and arenas each); 0 = 3."""
+        """``engines``: batches decoded concurrently (own CUDA streams and arenas each); 0 = 4."""
         lib = _lib.load()
         cfg = _lib.GpuConfig(ctypes.sizeof(_lib.GpuConfig), device, 0, engines)
         h = ctypes.c_void_p()

@@ -405,7 +405,7 @@ MMR_API void mmr_buffer_free(mmr_buffer *buffer) {
 MMR_API mmr_status mmr_gpu_context_create(const mmr_gpu_config *config, mmr_gpu_context **out_context) {
     if (!out_context) return invalid_argument("out_context is null");
     *out_context = nullptr;
-    int device = 0, engines = 3;
+    int device = 0, engines = 4;
     if (config) {
         if (config->struct_size != sizeof(mmr_gpu_config)) return invalid_argument("config struct_size mismatch");
         device = config->device;
