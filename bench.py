@@ -26,6 +26,7 @@ import argparse
 import json
 import multiprocessing as mp
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -150,6 +151,24 @@ def _peaks():
         return 6800.0, "fallback"
 
 
+def _cpu_model() -> str:
+    """The host CPU as /proc/cpuinfo names it (x86 'model name'; Arm implementer/part ids)."""
+    try:
+        info = open("/proc/cpuinfo").read().splitlines()
+    except OSError:
+        return platform.machine()
+    fields = {}
+    for line in info:
+        k, _, v = line.partition(":")
+        fields.setdefault(k.strip(), v.strip())
+    if "model name" in fields:
+        return fields["model name"]
+    arm_parts = {"0xd0c": "Neoverse N1", "0xd40": "Neoverse V1", "0xd49": "Neoverse N2", "0xd4f": "Neoverse V2"}
+    part = fields.get("CPU part", "")
+    name = arm_parts.get(part, f"Arm part {part}" if part else "")
+    return platform.machine() + (f" ({name})" if name else "")
+
+
 def _profile_figures():
     """Per-kernel figures from the committed ncu summaries: lines 'key: kernel value'."""
     out = {}
@@ -203,7 +222,7 @@ def reference_arm(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "u8/i32/f64", "data": "synthetic (seeded)",
         "config": {"workload": WORKLOAD, "frames_per_step": cores, "width": W, "height": H, "subsampling": SUB,
                    "quality": Q, "restart_interval_mcus": RI, "output": "rgb24"},
-        "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": cores, "kind": "port",
+        "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": cores, "kind": "port", "cpu": _cpu_model(),
                          "sample": f"{cores} frames per step of the {FRAMES}-frame workload, one per process"},
         "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -373,9 +392,10 @@ MIXED_SEED = 20261205
 
 def mixed_sweep(local: int, steps: int = 5, warmup: int = 3):
     """C4: 512 MJPEG frames, sizes in steps of 16 over 320x240..3840x2160, 4:2:0 /
-    4:2:2 / 4:4:4, q 50..95, restart interval none / one MCU row / 4 MCUs, planar
-    output, device-resident; slice size autotuned per frame class, then timed with
-    the repeated batch replayed from captured CUDA graphs."""
+    4:2:2 / 4:4:4, q 50..95, restart interval none / one MCU row / 4 MCUs, RGB24
+    output, device-resident; slice size autotuned per entropy class and the
+    transform's strip of MCUs per CTA per tiling class, then timed with the
+    repeated batch replayed from captured CUDA graphs."""
     import ctypes
 
     import torch
@@ -392,7 +412,7 @@ def mixed_sweep(local: int, steps: int = 5, warmup: int = 3):
     for p, off in zip(packets, offs):
         host.numpy()[off:off + len(p)] = memoryview(p)
     dev = host.to(f"cuda:{local}")
-    need = [m.probe(m.CODEC_MJPEG, p).planar_bytes for p in packets]
+    need = [m.probe(m.CODEC_MJPEG, p).rgb_bytes for p in packets]
     ooffs, o = [], 0
     for nb in need:
         ooffs.append(o)
@@ -406,7 +426,7 @@ def mixed_sweep(local: int, steps: int = 5, warmup: int = 3):
         it.device_data = dev.data_ptr() + offs[i]
         it.len = len(p)
         it.codec = m.CODEC_MJPEG
-        it.output = m.OUTPUT_PLANAR
+        it.output = m.OUTPUT_RGB24
         it.flags = m.ITEM_OUT_DEVICE
         it.out = dev_out.data_ptr() + ooffs[i]
         it.out_capacity = need[i]
@@ -424,11 +444,14 @@ def mixed_sweep(local: int, steps: int = 5, warmup: int = 3):
     dt = time.perf_counter() - t0
     ok = all(arr[i].status == 0 for i in range(len(packets)))
     ctx.close()
-    return {"workload": "c4-512-mixed-mjpeg(320x240..3840x2160, 420/422/444, q50-95, ri none/row/4)-planar",
+    def brief(t):
+        keep = ("kind", "frame_class", "frames", "slice_bits" if t["kind"] == "slice" else "strip_mcus")
+        return {k: t[k] for k in keep}
+
+    return {"workload": "c4-512-mixed-mjpeg(320x240..3840x2160, 420/422/444, q50-95, ri none/row/4)-rgb24",
             "frames_per_step": len(packets), "compressed_bytes": sum(len(p) for p in packets),
             "fps": len(packets) * steps / dt, "ms_per_step": 1000 * dt / steps, "graph_replays": replays,
-            "all_ok": ok, "tuned": [{"frame_class": t["frame_class"], "slice_bits": t["slice_bits"],
-                                      "frames": t["frames"]} for t in tuned]}
+            "all_ok": ok, "tuned": [brief(t) for t in tuned]}
 
 
 def main():
@@ -627,7 +650,7 @@ def main():
         bit_exact = True
         for i, (st, t1, rgb) in enumerate(res):
             bit_exact &= st == 0 and gpu_rgb[i * rgb_bytes:(i + 1) * rgb_bytes].tobytes() == rgb
-        cpu = {"value": k / multi_t, "unit": "frames/s", "cores": cores, "kind": "port",
+        cpu = {"value": k / multi_t, "unit": "frames/s", "cores": cores, "kind": "port", "cpu": _cpu_model(),
                "single_core_frames_per_s": len(sample) / single_t,
                "sample": f"{len(sample)} frames on 1 core, then {k} frames on {cores} processes, "
                          f"of the same 1080p 4:2:2 q90 workload (oracle restating the reference decoder)"}

@@ -124,24 +124,37 @@ typedef struct mmr_gpu_batch_stats {
 } mmr_gpu_batch_stats;
 
 /*
- * Autotuner: for each tuning class of MJPEG frame in the sample (restart layout:
- * none / intervals of <= 8 MCUs / longer; log2 of the compressed bits per
- * interval), decodes up to 64 of its frames at every candidate slice size
- * (1024, 2048, 4096, 8192 bits) and keeps the fastest entropy stage for that
- * class in this context. The items are decoded (outputs written) several times.
- * report (capacity entries, may be NULL) receives one entry per class; *count
- * the number of classes.
+ * Autotuner, two tables per context:
+ *  - kind 0, entropy classes (restart layout: none / intervals of <= 8 MCUs /
+ *    longer; log2 of the compressed bits per interval): decodes up to 64 of the
+ *    sample's MJPEG frames of the class at every candidate slice size (1024, 2048,
+ *    4096, 8192 bits) and keeps the fastest entropy stage;
+ *  - kind 1, tiling classes of the sample's RGB24 MJPEG frames the fused
+ *    transform takes ((layout: 0 = 4:4:4, 1 = 4:2:2, 2 = 4:2:0) << 8 | bit length
+ *    of the MCU columns): decodes up to 64 of them with the narrow and the wide
+ *    strip of MCUs per CTA (8 or 16 at 4:4:4, 4 or 8 otherwise) and keeps the
+ *    fastest transform stage.
+ * Later batches of this context use the tables (other classes keep the default:
+ * automatic slice size, wide strip). The items are decoded (outputs written)
+ * several times. report (capacity entries, may be NULL) receives one entry per
+ * class; *count the number of classes. mmr_gpu_set_tuning installs a table
+ * saved from an earlier run (only frame_class, kind, slice_bits and strip_mcus
+ * are read).
  */
 typedef struct mmr_gpu_tune_entry {
-    uint32_t frame_class; /* (layout << 8) | log2(bits per interval) */
-    uint32_t slice_bits;  /* chosen */
+    uint32_t frame_class; /* kind 0: (layout << 8) | log2(bits per interval); kind 1: tiling class */
+    uint32_t slice_bits;  /* kind 0: chosen */
     uint32_t frames;      /* sample frames of the class */
+    uint32_t kind;        /* 0: entropy slice size, 1: transform strip */
+    double entropy_ms[4]; /* kind 0, per candidate: 1024, 2048, 4096, 8192 bits */
+    uint32_t strip_mcus;  /* kind 1: chosen MCUs per transform CTA */
     uint32_t pad;
-    double entropy_ms[4]; /* per candidate: 1024, 2048, 4096, 8192 bits */
+    double transform_ms[2]; /* kind 1: narrow strip, wide strip */
 } mmr_gpu_tune_entry;
 
 MMR_API mmr_status mmr_gpu_autotune(mmr_gpu_context *context, mmr_gpu_item *items, size_t count,
                                     mmr_gpu_tune_entry *report, size_t capacity, size_t *report_count);
+MMR_API mmr_status mmr_gpu_set_tuning(mmr_gpu_context *context, const mmr_gpu_tune_entry *entries, size_t count);
 
 /*
  * CUDA-graph replay (default on): a batch whose packets stay on the device and

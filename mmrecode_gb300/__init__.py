@@ -216,6 +216,23 @@ class BatchResult:
     concealed_segments: int = 0
 
 
+def save_tuning(path: str, table: list) -> None:
+    """Writes an autotuner table (``Context.autotune``'s list) as JSON."""
+    import json
+    with open(path, "w") as f:
+        json.dump({"mmrecode_gpu_tuning": 1, "classes": table}, f, indent=1, sort_keys=True)
+
+
+def load_tuning(path: str) -> list:
+    """Reads a table written by ``save_tuning`` (for ``Context.set_tuning``)."""
+    import json
+    with open(path) as f:
+        doc = json.load(f)
+    if doc.get("mmrecode_gpu_tuning") != 1:
+        raise ValueError(f"{path}: not an MMRecode GPU tuning table")
+    return doc["classes"]
+
+
 class Context:
     """A GPU decode context: engines (CUDA stream + device arenas each) that decode batches."""
 
@@ -252,17 +269,40 @@ class Context:
         return _lib.load().mmr_gpu_last_batch_launches(self._h)
 
     def autotune(self, items) -> list:
-        """Tunes the slice size per frame class on a ``(_lib.GpuItem * n)`` sample (decoded
-        several times); returns one dict per class."""
-        cap = 64
+        """Tunes the slice size per entropy class and the transform strip per tiling class on
+        a ``(_lib.GpuItem * n)`` sample (decoded several times); returns one dict per class:
+        ``kind`` "slice" (``slice_bits``, ``entropy_ms`` per candidate) or "strip"
+        (``strip_mcus``, ``transform_ms`` for the narrow and the wide strip)."""
+        cap = 256
         rep = (_lib.TuneEntry * cap)()
         cnt = ctypes.c_size_t()
         st = _lib.load().mmr_gpu_autotune(self._h, items, len(items), rep, cap, ctypes.byref(cnt))
         if st != STATUS_OK:
             raise MmrError(st, _lib.last_error())
-        return [{"frame_class": rep[k].frame_class, "slice_bits": rep[k].slice_bits, "frames": rep[k].frames,
-                 "entropy_ms": dict(zip((1024, 2048, 4096, 8192), list(rep[k].entropy_ms)))}
-                for k in range(min(cnt.value, cap))]
+        out = []
+        for k in range(min(cnt.value, cap)):
+            e = rep[k]
+            if e.kind == 0:
+                out.append({"kind": "slice", "frame_class": e.frame_class, "slice_bits": e.slice_bits,
+                            "frames": e.frames, "entropy_ms": dict(zip((1024, 2048, 4096, 8192), list(e.entropy_ms)))})
+            else:
+                out.append({"kind": "strip", "frame_class": e.frame_class, "strip_mcus": e.strip_mcus,
+                            "frames": e.frames, "transform_ms": {"narrow": e.transform_ms[0], "wide": e.transform_ms[1]}})
+        return out
+
+    def set_tuning(self, table) -> None:
+        """Installs an autotuner table (the list ``autotune`` returned, e.g. reloaded with
+        ``load_tuning``) for later batches."""
+        arr = (_lib.TuneEntry * max(len(table), 1))()
+        for k, t in enumerate(table):
+            e = arr[k]
+            e.frame_class = int(t["frame_class"])
+            e.kind = 0 if t["kind"] == "slice" else 1
+            e.slice_bits = int(t.get("slice_bits", 0))
+            e.strip_mcus = int(t.get("strip_mcus", 0))
+        st = _lib.load().mmr_gpu_set_tuning(self._h, arr, len(table))
+        if st != STATUS_OK:
+            raise MmrError(st, _lib.last_error())
 
     def set_graphs(self, enable: bool) -> None:
         """CUDA-graph replay of repeated device-resident batches (default on)."""

@@ -90,7 +90,8 @@ class BatchStats(ctypes.Structure):
 
 class TuneEntry(ctypes.Structure):
     _fields_ = [("frame_class", ctypes.c_uint32), ("slice_bits", ctypes.c_uint32), ("frames", ctypes.c_uint32),
-                ("pad", ctypes.c_uint32), ("entropy_ms", ctypes.c_double * 4)]
+                ("kind", ctypes.c_uint32), ("entropy_ms", ctypes.c_double * 4), ("strip_mcus", ctypes.c_uint32),
+                ("pad", ctypes.c_uint32), ("transform_ms", ctypes.c_double * 2)]
 
 
 class JpegEncodeOptions(ctypes.Structure):
@@ -128,6 +129,7 @@ SIGNATURES = {
     "mmr_gpu_set_graphs": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int32),
     "mmr_gpu_autotune": ([ctypes.c_void_p, ctypes.POINTER(GpuItem), ctypes.c_size_t, ctypes.POINTER(TuneEntry),
                          ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int32),
+    "mmr_gpu_set_tuning": ([ctypes.c_void_p, ctypes.POINTER(TuneEntry), ctypes.c_size_t], ctypes.c_int32),
     "mmr_gpu_last_batch_stats": ([ctypes.c_void_p, ctypes.POINTER(BatchStats)], ctypes.c_int32),
     "mmr_mjpeg_encode_ex": ([ctypes.POINTER(VideoFrameView), ctypes.POINTER(JpegEncodeOptions), ctypes.POINTER(Buffer)],
                             ctypes.c_int32),

@@ -491,13 +491,42 @@ MMR_API mmr_status mmr_gpu_autotune(mmr_gpu_context *context, mmr_gpu_item *item
             if (!to_item(items[i], v[i], &err)) return invalid_argument(err);
         const std::vector<mmr::TuneResult> r = context->pool->autotune(v.data(), count);
         for (size_t k = 0; k < r.size() && report && k < capacity; k++) {
-            report[k].frame_class = r[k].frame_class;
-            report[k].slice_bits = r[k].slice_bits;
-            report[k].frames = r[k].frames;
-            report[k].pad = 0;
-            for (int c = 0; c < 4; c++) report[k].entropy_ms[c] = r[k].ms[c];
+            mmr_gpu_tune_entry &o = report[k];
+            memset(&o, 0, sizeof(o));
+            o.frame_class = r[k].frame_class;
+            o.kind = r[k].kind;
+            o.frames = r[k].frames;
+            if (r[k].kind == 0) {
+                o.slice_bits = r[k].slice_bits;
+                for (int c = 0; c < 4; c++) o.entropy_ms[c] = r[k].ms[c];
+            } else {
+                o.strip_mcus = r[k].strip_mcus;
+                for (int c = 0; c < 2; c++) o.transform_ms[c] = r[k].ms[c];
+            }
         }
         if (report_count) *report_count = r.size();
+        return finish(MMR_STATUS_OK, "");
+    } catch (...) {
+        return finish(MMR_STATUS_INTERNAL_ERROR, "panic contained at MMRecode C API boundary");
+    }
+}
+
+MMR_API mmr_status mmr_gpu_set_tuning(mmr_gpu_context *context, const mmr_gpu_tune_entry *entries, size_t count) {
+    if (!context) return invalid_argument("context is null");
+    if (count && !entries) return invalid_argument("entries is null");
+    std::vector<mmr::TuneResult> table(count);
+    for (size_t k = 0; k < count; k++) {
+        const mmr_gpu_tune_entry &e = entries[k];
+        if (e.kind > 1) return invalid_argument("tune entry kind must be 0 (slice size) or 1 (strip)");
+        if (e.kind == 0 && (e.slice_bits < 128 || e.slice_bits % 32 || e.slice_bits > (1u << 20)))
+            return invalid_argument("slice bits must be a multiple of 32 in 128..1048576");
+        table[k].kind = e.kind;
+        table[k].frame_class = e.frame_class;
+        table[k].slice_bits = e.slice_bits;
+        table[k].strip_mcus = e.strip_mcus;
+    }
+    try {
+        context->pool->set_tuning(table);
         return finish(MMR_STATUS_OK, "");
     } catch (...) {
         return finish(MMR_STATUS_INTERNAL_ERROR, "panic contained at MMRecode C API boundary");

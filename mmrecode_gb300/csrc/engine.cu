@@ -110,6 +110,19 @@ struct JPlan {
 
 // Tuning class of a planned MJPEG frame: restart layout (none, short, long
 // intervals) and log2 of its compressed bits per interval.
+int fused_layout(const JPlan &p) {
+    if (p.fmt == kGray8 || p.ncomp != 3 || !p.interleaved || p.comps[0].h != p.hmax || p.comps[0].v != p.vmax ||
+        p.comps[1].h != 1 || p.comps[1].v != 1 || p.comps[2].h != 1 || p.comps[2].v != 1)
+        return -1;
+    return fused_variant(p.hmax, p.vmax);
+}
+
+uint32_t tile_class_of(int variant, uint32_t mcu_cols) {
+    uint32_t bits = 0;
+    while (bits < 31 && (1u << bits) <= mcu_cols) bits++;
+    return (uint32_t)variant << 8 | bits;
+}
+
 uint32_t tune_class_of(const JPlan &p, size_t len) {
     const uint32_t layout = p.ri >= p.total_mcus ? 0 : p.ri <= 8 ? 1 : 2;
     uint64_t bits = 8 * (uint64_t)len / std::max<uint32_t>(1, p.n_intervals);
@@ -618,6 +631,18 @@ std::string render_message(const Diag &d, const uint8_t *in, size_t len, uint32_
 
 // ---------------------------------------------------------------- probe ---
 
+uint32_t jpeg_tile_class(const uint8_t *data, size_t len) {
+    JPlan p;
+    plan_jpeg(data, len, p);
+    if (!p.decode || p.ncomp > 4) return 0xffffffffu;
+    const int v = fused_layout(p);
+    return v < 0 ? 0xffffffffu : tile_class_of(v, p.mcu_cols);
+}
+
+uint32_t fused_strip_mcus(uint32_t tile_class, bool wide) {
+    return fused_slot_mcus(fused_slot((int)(tile_class >> 8), wide));
+}
+
 uint32_t jpeg_tune_class(const uint8_t *data, size_t len) {
     JPlan p;
     plan_jpeg(data, len, p);
@@ -805,8 +830,8 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
         std::vector<RgbJob> rgbjobs;
         std::vector<uint64_t> rgbfirst(1, 0);
         std::vector<uint32_t> rgbcta(1, 0);
-        std::vector<FusedJob> fjobs[3];
-        std::vector<uint32_t> fcta[3] = {{0}, {0}, {0}};
+        std::vector<FusedJob> fjobs[kFusedSlots];
+        std::vector<uint32_t> fcta[kFusedSlots] = {{0}, {0}, {0}, {0}, {0}, {0}};
 
         std::map<std::vector<uint8_t>, uint32_t> lut_index;
         std::vector<uint32_t> item_ok(n, 1);
@@ -947,22 +972,26 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
                 }
                 F.blk_off = blocks;
                 F.n_blocks = p.n_blocks;
-                // RGB straight from coefficients for the standard MCU layouts
-                int fused_v = -1;
-                if (can_output && it.output == kOutRgb24 && p.fmt != kGray8 && p.ncomp == 3 && p.interleaved &&
-                    p.comps[0].h == p.hmax && p.comps[0].v == p.vmax && p.comps[1].h == 1 && p.comps[1].v == 1 &&
-                    p.comps[2].h == 1 && p.comps[2].v == 1)
-                    fused_v = fused_variant(p.hmax, p.vmax);
+                // RGB straight from coefficients for the standard MCU layouts, in
+                // strips of the width tuned for the frame's class (wide by default)
+                const int fused_v = can_output && it.output == kOutRgb24 ? fused_layout(p) : -1;
                 if (fused_v >= 0) {
+                    bool wide = true;
+                    if (fused_wide_ >= 0) {
+                        wide = fused_wide_ != 0;
+                    } else {
+                        auto t = tuned_tile_.find(tile_class_of(fused_v, p.mcu_cols));
+                        if (t != tuned_tile_.end()) wide = t->second != 0;
+                    }
+                    const int slot = fused_slot(fused_v, wide);
                     FusedJob fj;
                     memset(&fj, 0, sizeof(fj));
                     fj.frame = (uint32_t)jframes.size();
-                    fj.strips_x = fused_strips_x(fused_v, p.mcu_cols);
+                    fj.strips_x = fused_strips_x(slot, p.mcu_cols);
                     fj.width = p.W;
                     fj.height = p.H;
-                    fjobs[fused_v].push_back(fj);
-                    fcta[fused_v].push_back(fcta[fused_v].back() + fj.strips_x * p.mcu_rows);
-
+                    fjobs[slot].push_back(fj);
+                    fcta[slot].push_back(fcta[slot].back() + fj.strips_x * p.mcu_rows);
                 }
                 for (uint32_t c = 0; c < p.ncomp && fused_v < 0; c++) {
                     JBlockRange r;
@@ -1167,8 +1196,8 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
                o_dframes = blob.add_vec(dframes), o_dstates = blob.add_vec(dstates), o_segfirst = blob.add_vec(seg_first),
                o_diffirst = blob.add_vec(dif_first), o_rgbjobs = blob.add_vec(rgbjobs),
                o_rgbcta = blob.add_vec(rgbcta);
-        size_t o_fjobs[3], o_fcta[3];
-        for (int v = 0; v < 3; v++) {
+        size_t o_fjobs[kFusedSlots], o_fcta[kFusedSlots];
+        for (int v = 0; v < kFusedSlots; v++) {
             o_fjobs[v] = blob.add_vec(fjobs[v]);
             o_fcta[v] = blob.add_vec(fcta[v]);
         }
@@ -1265,8 +1294,8 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
             launch_jpeg_entropy(JL, s);
             MMR_CUDA(record_event(I.ev[3], s, capturing));
             launch_jpeg_idct(JL, s);
-            FusedLaunch FL[3];
-            for (int v = 0; v < 3; v++) {
+            FusedLaunch FL[kFusedSlots];
+            for (int v = 0; v < kFusedSlots; v++) {
                 FL[v].jobs = reinterpret_cast<const FusedJob *>(db + o_fjobs[v]);
                 FL[v].cta_first = reinterpret_cast<const uint32_t *>(db + o_fcta[v]);
                 FL[v].n_jobs = (uint32_t)fjobs[v].size();

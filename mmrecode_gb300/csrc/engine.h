@@ -61,6 +61,14 @@ Probe probe_packet(uint32_t codec, const uint8_t *data, size_t len);
 // interval), UINT32_MAX when its headers fail or it has more than 4 components.
 uint32_t jpeg_tune_class(const uint8_t *data, size_t len);
 
+// Transform tiling class of an MJPEG packet decoded to RGB24 (fused layout
+// variant << 8 | bit length of the MCU columns), UINT32_MAX when the fused
+// kernel does not take its layout.
+uint32_t jpeg_tile_class(const uint8_t *data, size_t len);
+// MCUs per CTA of the fused transform's narrow or wide strip for the layout
+// variant of a tiling class (tiling class >> 8).
+uint32_t fused_strip_mcus(uint32_t tile_class, bool wide);
+
 // Renders a diagnostic as the reference's message. `data` is the packet, used
 // to turn token counts into byte offsets for entropy-stage errors.
 std::string render_message(const Diag &d, const uint8_t *data, size_t len, uint32_t data_start, uint32_t term);
@@ -120,6 +128,10 @@ public:
     }
     // Slice bits per tuning class, used when no fixed size is set.
     void set_tuned(const std::map<uint32_t, uint32_t> &t) { tuned_ = t; }
+    // Fused-transform strip per tiling class (1: wide, 0: narrow), and a width
+    // forcing every frame (-1: the tuned or default width).
+    void set_tuned_tiles(const std::map<uint32_t, uint32_t> &t) { tuned_tile_ = t; }
+    void set_fused_wide(int wide) { fused_wide_ = wide; }
 
     struct Impl;
 
@@ -131,6 +143,8 @@ private:
     uint32_t slice_bits_;
     bool graphs_ = true;
     std::map<uint32_t, uint32_t> tuned_;
+    std::map<uint32_t, uint32_t> tuned_tile_;
+    int fused_wide_ = -1;
     bool graph_replayed_ = false;
     Impl *impl_;
 };

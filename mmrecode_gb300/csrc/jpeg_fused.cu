@@ -43,9 +43,11 @@ struct FusedShape {
     static constexpr int RW = YW * 3;        // RGB bytes per tile row
 };
 
-// MCUs per CTA of the main pass
-template <int HM, int VM>
-__host__ __device__ constexpr int fused_nm() { return HM * VM == 1 ? 16 : 8; }
+// MCUs per CTA of each launch slot (layout variant * 2 + wide): a narrow and a
+// wide strip per layout, picked per frame class by the autotuner (wide by default)
+__host__ __device__ constexpr int fused_slot_nm(int slot) {
+    return slot == 0 ? 8 : slot == 1 ? 16 : slot == 2 || slot == 4 ? 4 : 8;
+}
 
 template <int HM, int VM, int NM>
 struct FusedSmem {
@@ -195,10 +197,8 @@ __device__ __forceinline__ void fused_tile(const JpegLaunch &L, const FusedLaunc
 }
 
 // Main pass: a CTA per strip of MCUs.
-template <int HM, int VM>
-__global__ void __launch_bounds__(FusedShape<HM, VM, fused_nm<HM, VM>()>::THREADS)
-    idct_rgb_kernel(JpegLaunch L, FusedLaunch FL) {
-    constexpr int NM = fused_nm<HM, VM>();
+template <int HM, int VM, int NM>
+__global__ void __launch_bounds__(FusedShape<HM, VM, NM>::THREADS) idct_rgb_kernel(JpegLaunch L, FusedLaunch FL) {
     __shared__ __align__(16) FusedSmem<HM, VM, NM> S;
     __shared__ uint32_t s_job;
     if (threadIdx.x == 0) {
@@ -227,23 +227,30 @@ int fused_variant(uint32_t hmax, uint32_t vmax) {
     return -1;
 }
 
-uint32_t fused_strips_x(int variant, uint32_t mcu_cols) {
-    const uint32_t nm = variant == 0 ? fused_nm<1, 1>() : variant == 1 ? fused_nm<2, 1>() : fused_nm<2, 2>();
+int fused_slot(int variant, bool wide) { return variant < 0 ? -1 : 2 * variant + (wide ? 1 : 0); }
+
+uint32_t fused_slot_mcus(int slot) { return (uint32_t)fused_slot_nm(slot); }
+
+uint32_t fused_strips_x(int slot, uint32_t mcu_cols) {
+    const uint32_t nm = fused_slot_mcus(slot);
     return (mcu_cols + nm - 1) / nm;
 }
 
-template <int HM, int VM>
+template <int HM, int VM, int NM>
 static void launch_variant(const JpegLaunch &L, const FusedLaunch &FL, cudaStream_t s) {
     if (!FL.n_ctas) return;
-    idct_rgb_kernel<HM, VM><<<FL.n_ctas, FusedShape<HM, VM, fused_nm<HM, VM>()>::THREADS, 0, s>>>(L, FL);
+    idct_rgb_kernel<HM, VM, NM><<<FL.n_ctas, FusedShape<HM, VM, NM>::THREADS, 0, s>>>(L, FL);
 }
 
 int fused_launches(const FusedLaunch &FL) { return FL.n_ctas ? 1 : 0; }
 
 void launch_jpeg_idct_rgb(const JpegLaunch &L, const FusedLaunch *FL, cudaStream_t s) {
-    launch_variant<1, 1>(L, FL[0], s);
-    launch_variant<2, 1>(L, FL[1], s);
-    launch_variant<2, 2>(L, FL[2], s);
+    launch_variant<1, 1, fused_slot_nm(0)>(L, FL[0], s);
+    launch_variant<1, 1, fused_slot_nm(1)>(L, FL[1], s);
+    launch_variant<2, 1, fused_slot_nm(2)>(L, FL[2], s);
+    launch_variant<2, 1, fused_slot_nm(3)>(L, FL[3], s);
+    launch_variant<2, 2, fused_slot_nm(4)>(L, FL[4], s);
+    launch_variant<2, 2, fused_slot_nm(5)>(L, FL[5], s);
 }
 
 }  // namespace mmr

@@ -94,8 +94,13 @@ struct FusedLaunch {
 };
 
 int fused_variant(uint32_t hmax, uint32_t vmax);  // 0: 1x1, 1: 2x1, 2: 2x2, -1: not fused
-uint32_t fused_strips_x(int variant, uint32_t mcu_cols);
-void launch_jpeg_idct_rgb(const JpegLaunch &L, const FusedLaunch *FL, cudaStream_t s);  // FL[3]
+// launch slot of a layout variant with a narrow or wide strip (MCUs per CTA:
+// 8 or 16 at 1x1, 4 or 8 otherwise); kFusedSlots launches, one per slot
+constexpr int kFusedSlots = 6;
+int fused_slot(int variant, bool wide);
+uint32_t fused_slot_mcus(int slot);
+uint32_t fused_strips_x(int slot, uint32_t mcu_cols);
+void launch_jpeg_idct_rgb(const JpegLaunch &L, const FusedLaunch *FL, cudaStream_t s);  // FL[kFusedSlots]
 int fused_launches(const FusedLaunch &FL);
 
 struct DvLaunch {

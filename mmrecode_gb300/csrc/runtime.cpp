@@ -166,32 +166,40 @@ void EnginePool::worker(int k) {
 
 std::vector<TuneResult> EnginePool::autotune(Item *items, size_t n) {
     std::lock_guard<std::mutex> call(call_mu_);
-    std::map<uint32_t, std::vector<Item>> classes;
+    std::map<uint32_t, std::vector<Item>> classes, tiles;
     for (size_t i = 0; i < n; i++) {
         if (items[i].codec != kCodecMjpeg) continue;
         const uint32_t c = jpeg_tune_class(items[i].data, items[i].len);
         if (c != 0xffffffffu && classes[c].size() < 64) classes[c].push_back(items[i]);
+        if (items[i].output != kOutRgb24) continue;
+        const uint32_t t = jpeg_tile_class(items[i].data, items[i].len);
+        if (t != 0xffffffffu && tiles[t].size() < 64) tiles[t].push_back(items[i]);
     }
     Engine &e = *engines_[0];
     e.set_level(0);
     const uint32_t keep_bits = e.slice_bits();
+    // best of three timed runs (the first run sizes the arenas and is not counted)
+    auto best_of = [&](std::vector<Item> &v, float EngineTimes::*stage) {
+        double m = 1e30;
+        for (int rep = 0; rep < 3; rep++) {
+            EngineTimes t;
+            e.decode(v.data(), v.size(), &t);
+            if (rep) m = std::min(m, (double)(t.*stage));
+        }
+        return m;
+    };
     std::vector<TuneResult> out;
     for (auto &kv : classes) {
         TuneResult r;
+        r.kind = 0;
         r.frame_class = kv.first;
         r.frames = (uint32_t)kv.second.size();
         double best = 1e30;
         for (int k = 0; k < 4; k++) {
             e.set_slice_bits(kTuneCandidates[k]);
-            double m = 1e30;
-            for (int rep = 0; rep < 3; rep++) {  // the first run sizes the arenas
-                EngineTimes t;
-                e.decode(kv.second.data(), kv.second.size(), &t);
-                if (rep) m = std::min(m, (double)t.entropy_ms);
-            }
-            r.ms[k] = m;
-            if (m < best) {
-                best = m;
+            r.ms[k] = best_of(kv.second, &EngineTimes::entropy_ms);
+            if (r.ms[k] < best) {
+                best = r.ms[k];
                 r.slice_bits = kTuneCandidates[k];
             }
         }
@@ -199,8 +207,42 @@ std::vector<TuneResult> EnginePool::autotune(Item *items, size_t n) {
         out.push_back(r);
     }
     e.set_slice_bits(keep_bits);
-    for (auto &en : engines_) en->set_tuned(tuned_);
+    e.set_tuned(tuned_);
+    for (auto &kv : tiles) {
+        TuneResult r;
+        r.kind = 1;
+        r.frame_class = kv.first;
+        r.frames = (uint32_t)kv.second.size();
+        for (int wide = 0; wide < 2; wide++) {
+            e.set_fused_wide(wide);
+            r.ms[wide] = best_of(kv.second, &EngineTimes::idct_ms);
+        }
+        const int wide = r.ms[1] <= r.ms[0] ? 1 : 0;
+        r.strip_mcus = fused_strip_mcus(kv.first, wide != 0);
+        tuned_tile_[kv.first] = (uint32_t)wide;
+        out.push_back(r);
+    }
+    e.set_fused_wide(-1);
+    for (auto &en : engines_) {
+        en->set_tuned(tuned_);
+        en->set_tuned_tiles(tuned_tile_);
+    }
     return out;
+}
+
+void EnginePool::set_tuning(const std::vector<TuneResult> &table) {
+    std::lock_guard<std::mutex> call(call_mu_);
+    for (const TuneResult &r : table) {
+        if (r.kind == 0) {
+            tuned_[r.frame_class] = r.slice_bits;
+        } else {
+            tuned_tile_[r.frame_class] = r.strip_mcus == fused_strip_mcus(r.frame_class, true) ? 1u : 0u;
+        }
+    }
+    for (auto &en : engines_) {
+        en->set_tuned(tuned_);
+        en->set_tuned_tiles(tuned_tile_);
+    }
 }
 
 int32_t EnginePool::decode(Item *items, size_t n, EngineTimes *times) {

@@ -26,9 +26,15 @@ void accumulate_times(EngineTimes &into, const EngineTimes &t);
 
 // One tuned class: the slice size chosen for it and the entropy-stage time of
 // every candidate on the sample (ms, best of the repetitions).
+// One class of the autotuner's table. kind 0: slice bits of an entropy class
+// (ms = entropy stage per candidate slice size); kind 1: strip of a transform
+// tiling class (strip_mcus = chosen MCUs per CTA, ms[0..1] = transform stage
+// with the narrow and the wide strip).
 struct TuneResult {
+    uint32_t kind = 0;
     uint32_t frame_class = 0;
     uint32_t slice_bits = 0;
+    uint32_t strip_mcus = 0;
     uint32_t frames = 0;
     double ms[4] = {0, 0, 0, 0};
 };
@@ -55,10 +61,14 @@ public:
     bool set_slice_bits(uint32_t bits);
     void set_graphs(bool on);
     // Measures the entropy stage of the sample's MJPEG frames, class by class, at
-    // every candidate slice size on one engine and keeps the fastest per class for
-    // all engines (classes not in the sample keep the automatic choice). Decodes
-    // the items (outputs included) several times.
+    // every candidate slice size, and the fused transform of its RGB24 frames,
+    // tiling class by class, with the narrow and the wide strip, on one engine,
+    // and keeps the fastest per class for all engines (classes not in the sample
+    // keep the automatic choice). Decodes the items (outputs included) several
+    // times.
     std::vector<TuneResult> autotune(Item *items, size_t n);
+    // Installs a table (from autotune, or saved from an earlier one) on all engines.
+    void set_tuning(const std::vector<TuneResult> &table);
     int size() const { return (int)engines_.size(); }
     Engine &engine(int k) { return *engines_[k]; }
     static constexpr size_t kMinChunk = 16;
@@ -94,7 +104,8 @@ private:
     uint64_t gen_ = 0;  // batches handed to the workers
     bool stop_ = false;
     uint32_t launches_ = 0;
-    std::map<uint32_t, uint32_t> tuned_;
+    std::map<uint32_t, uint32_t> tuned_;       // entropy class -> slice bits
+    std::map<uint32_t, uint32_t> tuned_tile_;  // tiling class -> wide strip (1) or narrow (0)
 };
 
 struct ServerConfig {

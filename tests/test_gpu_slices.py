@@ -164,3 +164,48 @@ def test_slices_owning_more_blocks_than_their_store_holds(ctx):
             f = m.frame_from_batch(r, payload)
             assert_same_decode(0, "", frame_planes_gpu(f), ref, f"flat[{i}] slice_bits={bits}")
     ctx.set_slice_bits(0)
+
+
+def test_autotune_strips_and_saved_table_leave_output_unchanged(tmp_path):
+    import ctypes
+    from mmrecode_gb300 import _lib
+    packets = (synth.mjpeg_stream(314, 4, 640, 480, "420", 75, 0) +
+               synth.mjpeg_stream(315, 4, 1280, 720, "422", 90, 80) +
+               synth.mjpeg_stream(316, 4, 352, 288, "444", 60, 4))
+    keep, arr = [], (_lib.GpuItem * len(packets))()
+    for i, p in enumerate(packets):
+        src = (ctypes.c_uint8 * len(p)).from_buffer_copy(p)
+        need = m.probe(m.CODEC_MJPEG, p).rgb_bytes
+        dst = (ctypes.c_uint8 * need)()
+        keep.append((src, dst))
+        it = arr[i]
+        it.struct_size = ctypes.sizeof(_lib.GpuItem)
+        it.data, it.len, it.codec, it.output = ctypes.addressof(src), len(p), m.CODEC_MJPEG, m.OUTPUT_RGB24
+        it.out, it.out_capacity = ctypes.addressof(dst), need
+    refs = [oracle.rgb24(oracle.jpeg_decode(p).frame) for p in packets]
+    with m.Context(engines=2) as ctx:
+        report = ctx.autotune(arr)
+        strips = [r for r in report if r["kind"] == "strip"]
+        assert {r["frame_class"] >> 8 for r in strips} == {0, 1, 2}  # 4:4:4, 4:2:2, 4:2:0
+        for r in strips:
+            narrow, wide = (8, 16) if r["frame_class"] >> 8 == 0 else (4, 8)
+            tm = r["transform_ms"]
+            assert r["strip_mcus"] == (wide if tm["wide"] <= tm["narrow"] else narrow)
+        path = str(tmp_path / "tuning.json")
+        m.save_tuning(path, report)
+        results = ctx.decode_batch(packets, m.CODEC_MJPEG, m.OUTPUT_RGB24)
+    for (r, payload), ref in zip(results, refs):
+        assert r.status == 0 and payload == ref
+    # the other strip everywhere, installed from the saved table: same output
+    table = m.load_tuning(path)
+    for t in table:
+        if t["kind"] == "strip":
+            narrow, wide = (8, 16) if t["frame_class"] >> 8 == 0 else (4, 8)
+            t["strip_mcus"] = wide if t["strip_mcus"] == narrow else narrow
+    with m.Context(engines=1) as ctx:
+        ctx.set_tuning(table)
+        results = ctx.decode_batch(packets, m.CODEC_MJPEG, m.OUTPUT_RGB24)
+        with pytest.raises(m.MmrError):
+            ctx.set_tuning([{"kind": "slice", "frame_class": 1, "slice_bits": 100}])
+    for (r, payload), ref in zip(results, refs):
+        assert r.status == 0 and payload == ref

@@ -32,3 +32,18 @@ def test_batched_decoder_queues_until_full():
     for _ in range(3):
         d.send_packet(m.Packet(b"\xff\xd8"))
     assert d.receive_frame() is None
+
+
+def test_tuning_table_json_round_trip(tmp_path):
+    import mmrecode_gb300 as m
+    table = [{"kind": "slice", "frame_class": 269, "slice_bits": 4096, "frames": 12,
+              "entropy_ms": {"1024": 1.5, "2048": 1.2, "4096": 1.1, "8192": 1.3}},
+             {"kind": "strip", "frame_class": 263, "strip_mcus": 4, "frames": 6,
+              "transform_ms": {"narrow": 0.2, "wide": 0.25}}]
+    path = str(tmp_path / "t.json")
+    m.save_tuning(path, table)
+    assert m.load_tuning(path) == table
+    (tmp_path / "bad.json").write_text('{"classes": []}')
+    import pytest
+    with pytest.raises(ValueError):
+        m.load_tuning(str(tmp_path / "bad.json"))
