@@ -278,6 +278,9 @@ MMR_API mmr_status mmr_gpu_server_replay(mmr_gpu_server *server, mmr_gpu_item *i
 
 /* mmr_gpu_set_slice_bits for a server's engines. */
 MMR_API mmr_status mmr_gpu_server_set_slice_bits(mmr_gpu_server *server, uint32_t bits);
+/* mmr_gpu_set_tuning for a server's engines (batches formed after the call use it). */
+MMR_API mmr_status mmr_gpu_server_set_tuning(mmr_gpu_server *server, const mmr_gpu_tune_entry *entries,
+                                             size_t count);
 
 #ifdef __cplusplus
 }

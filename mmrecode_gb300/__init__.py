@@ -233,6 +233,17 @@ def load_tuning(path: str) -> list:
     return doc["classes"]
 
 
+def _tune_entries(table) -> "ctypes.Array":
+    arr = (_lib.TuneEntry * max(len(table), 1))()
+    for k, t in enumerate(table):
+        e = arr[k]
+        e.frame_class = int(t["frame_class"])
+        e.kind = 0 if t["kind"] == "slice" else 1
+        e.slice_bits = int(t.get("slice_bits", 0))
+        e.strip_mcus = int(t.get("strip_mcus", 0))
+    return arr
+
+
 class Context:
     """A GPU decode context: engines (CUDA stream + device arenas each) that decode batches."""
 
@@ -293,13 +304,7 @@ class Context:
     def set_tuning(self, table) -> None:
         """Installs an autotuner table (the list ``autotune`` returned, e.g. reloaded with
         ``load_tuning``) for later batches."""
-        arr = (_lib.TuneEntry * max(len(table), 1))()
-        for k, t in enumerate(table):
-            e = arr[k]
-            e.frame_class = int(t["frame_class"])
-            e.kind = 0 if t["kind"] == "slice" else 1
-            e.slice_bits = int(t.get("slice_bits", 0))
-            e.strip_mcus = int(t.get("strip_mcus", 0))
+        arr = _tune_entries(table)
         st = _lib.load().mmr_gpu_set_tuning(self._h, arr, len(table))
         if st != STATUS_OK:
             raise MmrError(st, _lib.last_error())
@@ -492,6 +497,14 @@ class Server:
         if st != STATUS_OK:
             raise MmrError(st, _lib.last_error())
         return {name: getattr(s, name) for name, _ in _lib.ServerStats._fields_ if name != "struct_size"}
+
+    def set_tuning(self, table) -> None:
+        """Installs an autotuner table (``Context.autotune``'s list or ``load_tuning``'s) on
+        the server's engines."""
+        arr = _tune_entries(table)
+        st = _lib.load().mmr_gpu_server_set_tuning(self._h, arr, len(table))
+        if st != STATUS_OK:
+            raise MmrError(st, _lib.last_error())
 
     def set_slice_bits(self, bits: int) -> None:
         st = _lib.load().mmr_gpu_server_set_slice_bits(self._h, bits)

@@ -511,20 +511,31 @@ MMR_API mmr_status mmr_gpu_autotune(mmr_gpu_context *context, mmr_gpu_item *item
     }
 }
 
-MMR_API mmr_status mmr_gpu_set_tuning(mmr_gpu_context *context, const mmr_gpu_tune_entry *entries, size_t count) {
-    if (!context) return invalid_argument("context is null");
-    if (count && !entries) return invalid_argument("entries is null");
-    std::vector<mmr::TuneResult> table(count);
+namespace {
+
+// A tuning table from the caller's entries; nullptr (with the message) when one is invalid.
+const char *to_table(const mmr_gpu_tune_entry *entries, size_t count, std::vector<mmr::TuneResult> &table) {
+    table.assign(count, mmr::TuneResult());
     for (size_t k = 0; k < count; k++) {
         const mmr_gpu_tune_entry &e = entries[k];
-        if (e.kind > 1) return invalid_argument("tune entry kind must be 0 (slice size) or 1 (strip)");
+        if (e.kind > 1) return "tune entry kind must be 0 (slice size) or 1 (strip)";
         if (e.kind == 0 && (e.slice_bits < 128 || e.slice_bits % 32 || e.slice_bits > (1u << 20)))
-            return invalid_argument("slice bits must be a multiple of 32 in 128..1048576");
+            return "slice bits must be a multiple of 32 in 128..1048576";
         table[k].kind = e.kind;
         table[k].frame_class = e.frame_class;
         table[k].slice_bits = e.slice_bits;
         table[k].strip_mcus = e.strip_mcus;
     }
+    return nullptr;
+}
+
+}  // namespace
+
+MMR_API mmr_status mmr_gpu_set_tuning(mmr_gpu_context *context, const mmr_gpu_tune_entry *entries, size_t count) {
+    if (!context) return invalid_argument("context is null");
+    if (count && !entries) return invalid_argument("entries is null");
+    std::vector<mmr::TuneResult> table;
+    if (const char *err = to_table(entries, count, table)) return invalid_argument(err);
     try {
         context->pool->set_tuning(table);
         return finish(MMR_STATUS_OK, "");
@@ -695,6 +706,20 @@ MMR_API mmr_status mmr_gpu_server_replay(mmr_gpu_server *server, mmr_gpu_item *i
         }
         server->server->replay(v.data(), count, arrival_ns, latency_ms, max_lag_ns);
         for (size_t i = 0; i < count; i++) from_item(v[i], items[i]);
+        return finish(MMR_STATUS_OK, "");
+    } catch (...) {
+        return finish(MMR_STATUS_INTERNAL_ERROR, "panic contained at MMRecode C API boundary");
+    }
+}
+
+MMR_API mmr_status mmr_gpu_server_set_tuning(mmr_gpu_server *server, const mmr_gpu_tune_entry *entries,
+                                             size_t count) {
+    if (!server) return invalid_argument("server is null");
+    if (count && !entries) return invalid_argument("entries is null");
+    std::vector<mmr::TuneResult> table;
+    if (const char *err = to_table(entries, count, table)) return invalid_argument(err);
+    try {
+        server->server->set_tuning(table);
         return finish(MMR_STATUS_OK, "");
     } catch (...) {
         return finish(MMR_STATUS_INTERNAL_ERROR, "panic contained at MMRecode C API boundary");

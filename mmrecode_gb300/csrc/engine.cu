@@ -775,6 +775,14 @@ void set_result(Item &it, const Diag &d, const uint8_t *in, size_t len, uint32_t
 
 int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
     Impl &I = *impl_;
+    std::map<uint32_t, uint32_t> tuned, tuned_tile;  // this batch's copy of the tuning tables
+    int fused_wide;
+    {
+        std::lock_guard<std::mutex> g(tables_mu_);
+        tuned = tuned_;
+        tuned_tile = tuned_tile_;
+        fused_wide = fused_wide_;
+    }
     launches_ = 0;
     for (size_t i = 0; i < n; i++) {
         items[i].status = kOk;
@@ -962,8 +970,8 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
                 if (p.ncomp <= 4) {
                     uint32_t slice_bits = slice_bits_ ? slice_bits_ : auto_bits;
                     if (!slice_bits_) {
-                        auto t = tuned_.find(tune_class_of(p, it.len));
-                        if (t != tuned_.end()) slice_bits = t->second;
+                        auto t = tuned.find(tune_class_of(p, it.len));
+                        if (t != tuned.end()) slice_bits = t->second;
                     }
                     F.slice_bits = slice_bits;
                     F.slot_first = (uint32_t)n_slots;
@@ -977,11 +985,11 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
                 const int fused_v = can_output && it.output == kOutRgb24 ? fused_layout(p) : -1;
                 if (fused_v >= 0) {
                     bool wide = true;
-                    if (fused_wide_ >= 0) {
-                        wide = fused_wide_ != 0;
+                    if (fused_wide >= 0) {
+                        wide = fused_wide != 0;
                     } else {
-                        auto t = tuned_tile_.find(tile_class_of(fused_v, p.mcu_cols));
-                        if (t != tuned_tile_.end()) wide = t->second != 0;
+                        auto t = tuned_tile.find(tile_class_of(fused_v, p.mcu_cols));
+                        if (t != tuned_tile.end()) wide = t->second != 0;
                     }
                     const int slot = fused_slot(fused_v, wide);
                     FusedJob fj;

@@ -7,6 +7,7 @@
 
 #include <algorithm>
 #include <map>
+#include <mutex>
 #include <string>
 #include <utility>
 #include <vector>
@@ -127,11 +128,22 @@ public:
         return true;
     }
     // Slice bits per tuning class, used when no fixed size is set.
-    void set_tuned(const std::map<uint32_t, uint32_t> &t) { tuned_ = t; }
+    // (The tables may change while another thread decodes: a batch reads a copy
+    // taken at its start.)
+    void set_tuned(const std::map<uint32_t, uint32_t> &t) {
+        std::lock_guard<std::mutex> g(tables_mu_);
+        tuned_ = t;
+    }
     // Fused-transform strip per tiling class (1: wide, 0: narrow), and a width
     // forcing every frame (-1: the tuned or default width).
-    void set_tuned_tiles(const std::map<uint32_t, uint32_t> &t) { tuned_tile_ = t; }
-    void set_fused_wide(int wide) { fused_wide_ = wide; }
+    void set_tuned_tiles(const std::map<uint32_t, uint32_t> &t) {
+        std::lock_guard<std::mutex> g(tables_mu_);
+        tuned_tile_ = t;
+    }
+    void set_fused_wide(int wide) {
+        std::lock_guard<std::mutex> g(tables_mu_);
+        fused_wide_ = wide;
+    }
 
     struct Impl;
 
@@ -142,6 +154,7 @@ private:
     uint32_t launches_ = 0;
     uint32_t slice_bits_;
     bool graphs_ = true;
+    std::mutex tables_mu_;
     std::map<uint32_t, uint32_t> tuned_;
     std::map<uint32_t, uint32_t> tuned_tile_;
     int fused_wide_ = -1;

@@ -346,6 +346,18 @@ Server::~Server() {
     for (auto &t : threads_) t.join();
 }
 
+void Server::set_tuning(const std::vector<TuneResult> &table) {
+    std::map<uint32_t, uint32_t> tuned, tiles;
+    for (const TuneResult &r : table) {
+        if (r.kind == 0) tuned[r.frame_class] = r.slice_bits;
+        else tiles[r.frame_class] = r.strip_mcus == fused_strip_mcus(r.frame_class, true) ? 1u : 0u;
+    }
+    for (auto &e : engines_) {
+        e->set_tuned(tuned);
+        e->set_tuned_tiles(tiles);
+    }
+}
+
 bool Server::set_slice_bits(uint32_t bits) {
     std::lock_guard<std::mutex> g(mu_);
     bool ok = true;

@@ -154,6 +154,8 @@ public:
     bool known(uint64_t ticket);
     ServerStats stats(bool reset);
     bool set_slice_bits(uint32_t bits);
+    // Installs an autotuner table on the server's engines (later batches use it).
+    void set_tuning(const std::vector<TuneResult> &table);
     // Open-loop trace replay: submits item i at arrival_ns[i] after the call starts
     // (non-decreasing offsets), collects every result into items[i] and its latency
     // into latency_ms[i]; *max_lag_ns = the latest any submission left its slot.

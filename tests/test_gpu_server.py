@@ -139,3 +139,19 @@ def test_open_loop_replay_returns_every_result():
         p, c = pk[i % 7], codecs[i % 7]
         ref = oracle.jpeg_decode(p) if c == m.CODEC_MJPEG else oracle.dv_decode(p, False)
         assert ctypes.string_at(keep[i][1], arr[i].out_bytes) == b"".join(d for (_, _, d) in ref.frame.planes), i
+
+
+def test_installed_tuning_table_leaves_results_unchanged():
+    pk = synth.mjpeg_stream(512, 4, 640, 480, "422", 85, 40) + synth.mjpeg_stream(513, 4, 352, 288, "444", 70, 0)
+    table = [{"kind": "slice", "frame_class": (lay << 8) | b, "slice_bits": 1024} for lay in range(3) for b in range(20)]
+    table += [{"kind": "strip", "frame_class": (v << 8) | b, "strip_mcus": 4 if v else 8}
+              for v in range(3) for b in range(1, 9)]
+    with m.Server(engines=2, max_batch=4) as srv:
+        srv.set_tuning(table)
+        tickets = [srv.submit(p, m.CODEC_MJPEG, m.OUTPUT_RGB24) for p in pk]
+        for t, p in zip(tickets, pk):
+            r, payload, _ = srv.wait(t)
+            assert r.status == 0, r.message
+            assert payload == oracle.rgb24(oracle.jpeg_decode(p).frame)
+        with pytest.raises(m.MmrError):
+            srv.set_tuning([{"kind": "slice", "frame_class": 0, "slice_bits": 7}])
