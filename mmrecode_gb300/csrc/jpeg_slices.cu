@@ -215,7 +215,19 @@ __device__ __forceinline__ bool store_owned(const JpegLaunch &L, uint32_t slot, 
 // the levels of the blocks it owns along its own path (SliceOwn): blocks whose DC
 // symbol starts at or past the slice start and before the slice end, the last
 // one decoded to completion past the end.
-__global__ void __launch_bounds__(kSliceThreads) slice_spec_kernel(JpegLaunch L) {
+// Table indices of MCU block si (fewer live registers than pointers).
+struct TabIdx {
+    uint32_t dc, ac, comp;
+};
+
+__device__ __forceinline__ TabIdx tab_idx(const JpegLaunch &L, const JFrame &F, uint32_t si) {
+    const JBlockRec &R = L.brec[F.sched_off + si];
+    return TabIdx{R.dc_lut, R.ac_lut, R.comp};
+}
+
+// 8 CTAs per SM (64 registers): the pass is latency-bound, so resident warps are
+// what it runs on (at 9 it spills and runs slower)
+__global__ void __launch_bounds__(kSliceThreads, 8) slice_spec_kernel(JpegLaunch L) {
     __shared__ __align__(16) int16_t s_stage[kSliceThreads * kStride];
     __shared__ uint8_t s_zz[64];
     int16_t *stage = s_stage + threadIdx.x * kStride;
@@ -235,7 +247,6 @@ __global__ void __launch_bounds__(kSliceThreads) slice_spec_kernel(JpegLaunch L)
     out.pad = 0;
 #pragma unroll
     for (int c = 0; c < 4; c++) out.dc[c] = 0;
-    SliceOwn *own = L.own + slot;
     {
         SliceMatch m;  // a first slice starts true; the sync pass finds the others' point
         m.q = guess ? kMatchNone : kMatchStart;
@@ -246,8 +257,8 @@ __global__ void __launch_bounds__(kSliceThreads) slice_spec_kernel(JpegLaunch L)
     }
     if (s.last) {  // nothing reads the last slice's exit or counts; the decode pass redoes it
         L.sync[slot] = out;
-        own->n = 0;
-        own->ok = 0;
+        L.own[slot].n = 0;
+        L.own[slot].ok = 0;
         return;
     }
     const JFrame &F = *s.F;
@@ -264,16 +275,14 @@ __global__ void __launch_bounds__(kSliceThreads) slice_spec_kernel(JpegLaunch L)
     };
     const unsigned long long lbits = (unsigned long long)(s.v.barrier - s.v.start) * 8;
     const uint32_t lim = clamp_u32(lbits - p0);  // bits before the barrier, from p0
-    const uint64_t tokbit = (uint64_t)s.v.start * 8;
     Bits r;
-    bits_init(r, F.tok, tokbit + p0, 0);
+    bits_init(r, F.tok, (uint64_t)s.v.start * 8 + p0, 0);
     int k = guess ? 1 : 0;
     uint32_t si = 0;
-    BlockTabs tb = block_tabs(L, F, si);
+    TabIdx tb = tab_idx(L, F, si);
     uint32_t blocks = 0;
     int32_t dc[4] = {0, 0, 0, 0};
     int32_t dcv = 0;  // DC difference of the block in progress (0 before its DC symbol)
-    SliceSpec *sp = L.spec + slot;
     uint32_t q = 0, recorded = 0;
     uint32_t next_mark = guess ? mark_at(0) : 0xffffffffu;
     unsigned long long exit_state = kStErr;
@@ -281,7 +290,7 @@ __global__ void __launch_bounds__(kSliceThreads) slice_spec_kernel(JpegLaunch L)
     bool own_blk = false;  // the block in progress is owned
     bool own_ok = true;    // the owned blocks so far are stored
     uint32_t own_n = 0, chunk_base = 0;
-    unsigned long long own_end = 0;  // position after the last stored one
+    uint32_t own_end = 0;  // position (from p0) after the last stored one
     for (;;) {
         const uint32_t pr = r.used;
         if (pr >= end) {
@@ -297,7 +306,7 @@ __global__ void __launch_bounds__(kSliceThreads) slice_spec_kernel(JpegLaunch L)
                 cp.own_next = own_n + (own_blk && k != 0 ? 1u : 0u);
 #pragma unroll
                 for (int c = 0; c < 4; c++) cp.dc[c] = dc[c] + (tb.comp == (uint32_t)c ? dcv : 0);
-                sp->cp[q] = cp;
+                L.spec[slot].cp[q] = cp;
                 recorded |= 1u << q;
                 q++;
             }
@@ -309,13 +318,13 @@ __global__ void __launch_bounds__(kSliceThreads) slice_spec_kernel(JpegLaunch L)
         int32_t val;
         uint16_t err;
         uint32_t eb;
-        if (!decode_symbol(r, lim - pr, k0 == 0 ? tb.dc : tb.ac, L.symbols, k, val, err, eb)) {
+        if (!decode_symbol(r, lim - pr, L.luts + (k0 == 0 ? tb.dc : tb.ac), L.symbols, k, val, err, eb)) {
             if (!guess || err == kBarrierErr) break;  // exit_state stays kStErr
             // A decode from a guessed state met an invalid symbol: start again one bit
             // later; what came before cannot lead to the exit, so its checkpoints go,
             // and the owned blocks start again too (this path was not the true one).
             for (uint32_t x = 0; x < (uint32_t)kSliceCheckpoints; x++)
-                if (recorded & (1u << x)) sp->cp[x].state = kStErr;
+                if (recorded & (1u << x)) L.spec[slot].cp[x].state = kStErr;
             recorded = 0;
             blocks = 0;
 #pragma unroll
@@ -323,14 +332,14 @@ __global__ void __launch_bounds__(kSliceThreads) slice_spec_kernel(JpegLaunch L)
             dcv = 0;
             k = 1;
             si = 0;
-            tb = block_tabs(L, F, si);
+            tb = tab_idx(L, F, si);
             // (the stage may hold a partial block, or one whose store failed)
 #pragma unroll
             for (int x = 0; x < 8; x++) stage4[x] = make_int4(0, 0, 0, 0);
             own_blk = false;
             own_ok = true;
             own_n = 0;
-            bits_init(r, F.tok, tokbit + p0 + pr + 1, pr + 1);
+            bits_init(r, F.tok, (uint64_t)L.ivs[s.item].start * 8 + p0 + pr + 1, pr + 1);
             continue;
         }
         if (own_blk && own_ok) stage[s_zz[k - 1]] = (int16_t)val;
@@ -339,14 +348,14 @@ __global__ void __launch_bounds__(kSliceThreads) slice_spec_kernel(JpegLaunch L)
         if (own_blk && own_ok) {  // block complete
             own_ok = store_owned(L, slot, own_n, chunk_base, stage4, dcv);
             own_n++;
-            own_end = p0 + r.used;
+            own_end = r.used;
         }
         own_blk = false;
         add_dc(dc, tb.comp, dcv);
         dcv = 0;
         k = 0;
         si = si + 1 == F.sched_len ? 0 : si + 1;
-        tb = block_tabs(L, F, si);
+        tb = tab_idx(L, F, si);
     }
     // the owned block straddling the slice end is decoded to completion
     if (exit_state != kStErr && own_blk && own_ok) {
@@ -354,7 +363,7 @@ __global__ void __launch_bounds__(kSliceThreads) slice_spec_kernel(JpegLaunch L)
             int32_t val;
             uint16_t err;
             uint32_t eb;
-            if (!decode_symbol(r, lim - r.used, tb.ac, L.symbols, k, val, err, eb)) {
+            if (!decode_symbol(r, lim - r.used, L.luts + tb.ac, L.symbols, k, val, err, eb)) {
                 own_ok = false;
                 break;
             }
@@ -363,23 +372,24 @@ __global__ void __launch_bounds__(kSliceThreads) slice_spec_kernel(JpegLaunch L)
         if (own_ok) {
             own_ok = store_owned(L, slot, own_n, chunk_base, stage4, dcv);
             own_n++;
-            own_end = p0 + r.used;
+            own_end = r.used;
         }
     }
-    own->last_end = own_end;
+    SliceOwn *own = L.own + slot;
+    own->last_end = p0 + own_end;
     own->n = own_n;
     own->ok = own_ok && exit_state != kStErr;
     add_dc(dc, tb.comp, dcv);  // the block in progress is counted, with its DC if decoded
     if (guess) {
         for (uint32_t x = 0; x < (uint32_t)kSliceCheckpoints; x++)
-            if (!(recorded & (1u << x))) sp->cp[x].state = kStErr;
+            if (!(recorded & (1u << x))) L.spec[slot].cp[x].state = kStErr;
         SlicePoint e;
         e.state = exit_state;
         e.blocks = blocks;
         e.own_next = own_n;
 #pragma unroll
         for (int c = 0; c < 4; c++) e.dc[c] = dc[c];
-        sp->exit = e;
+        L.spec[slot].exit = e;
     }
     out.exit = exit_state;
     out.blocks = blocks;
