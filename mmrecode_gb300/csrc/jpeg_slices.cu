@@ -501,11 +501,19 @@ __device__ bool resync_slice(const JpegLaunch &L, uint32_t slot, const SliceRef 
 
 // Persistent threads take slots from a counter: re-decode lengths vary a lot
 // (most slices meet their first checkpoint, a few run to their end), so a lane
-// that is done takes the next slot instead of idling beside the slow ones.
+// that is done takes the next slot instead of idling beside the slow ones. The
+// lanes that reach the counter together take consecutive slots with one atomic
+// (one per slot serialised on the counter's address).
 __global__ void __launch_bounds__(kSliceThreads) slice_sync_kernel(JpegLaunch L, uint32_t pass) {
     uint32_t *next = L.sync_dirty + kSyncPasses + pass;
+    const uint32_t lane = threadIdx.x & 31;
     for (;;) {
-        const uint32_t slot = atomicAdd(next, 1u);
+        const unsigned act = __activemask();
+        const int leader = __ffs(act) - 1;
+        uint32_t base = 0;
+        if ((int)lane == leader) base = atomicAdd(next, (uint32_t)__popc(act));
+        base = __shfl_sync(act, base, leader);
+        const uint32_t slot = base + __popc(act & ((1u << lane) - 1u));
         if (slot >= L.n_slots) return;
         SliceRef s;
         if (!slice_ref(L, slot, s) || s.j == 0) continue;
