@@ -11,6 +11,9 @@ quality 90, Annex K Huffman tables, restart interval = one MCU row (120 MCUs of
   e2e     the same through mmr_gpu_decode_batch with pinned HOST buffers: the
           packets' H2D and the RGB frames' D2H are inside every step.
   plain   one frame per mmr_gpu_decode_batch call (host buffers), the plain GPU form.
+  stream_y4m  the same frames as one MJPEG file through the CLI's decode path
+          (mmr_gpu_stream_*): upload, framing on the GPU, batch decode, the
+          Y4M stream (planar 4:2:2) in pinned host memory.
 
 Inputs (337 MB) and outputs (1.87 GB) per step exceed the 129 MB L2, so no L2
 flush is needed between steps.
@@ -31,6 +34,8 @@ import statistics
 import subprocess
 import sys
 import time
+
+import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
@@ -465,6 +470,8 @@ def main():
     ap.add_argument("--plain-frames", type=int, default=60)
     ap.add_argument("--serve-seconds", type=float, default=2.0, help="seconds per serving load level (0: skip)")
     ap.add_argument("--mixed", type=int, default=1, help="run the 512-frame mixed batch (0: skip)")
+    ap.add_argument("--stream", type=int, default=1,
+                    help="decode the workload as one MJPEG file to Y4M, framed on the GPU (0: skip)")
     ap.add_argument("--graphs", type=int, default=1,
                     help="replay repeated batches as CUDA graphs (0: direct launches, e.g. under ncu, which "
                          "crashed the process while several engine threads captured graphs)")
@@ -626,6 +633,46 @@ def main():
     roofline = roof(dominant)
     roofline_transform = roof("idct_rgb_kernel")
 
+    # the CLI's `decode` path on the same frames as one MJPEG file (mmr_gpu_stream_*):
+    # upload, marker-candidate scan and framing, batch decode from the device copy,
+    # the Y4M stream (planar 4:2:2) into pinned host memory; every step opens and
+    # closes the stream
+    stream = None
+    if rank == 0 and args.stream:
+        host_stream = torch.empty(in_bytes, dtype=torch.uint8, pin_memory=True)
+        hs, o2 = host_stream.numpy(), 0
+        for p in packets:
+            hs[o2:o2 + len(p)] = np.frombuffer(p, np.uint8)
+            o2 += len(p)
+        src = (host_stream.data_ptr(), in_bytes)
+        with ctx.open_stream(src) as ms0:
+            y4m_bytes = ms0.y4m_bytes
+        y4m = torch.empty(y4m_bytes, dtype=torch.uint8, pin_memory=True)
+
+        def stream_step():
+            with ctx.open_stream(src) as ms:
+                o = ms.decode_into(y4m.data_ptr(), y4m_bytes)
+                assert o.status == 0 and o.frames_written == n, o.message
+                return ms.scan_ms, ms.upload_ms, ms.candidates
+
+        for _ in range(args.warmup):
+            stream_step()
+        scans = []
+        t = time.perf_counter()
+        for _ in range(args.steps):
+            scans.append(stream_step())
+        sdt = time.perf_counter() - t
+        scan_ms = sum(x[0] for x in scans) / len(scans)
+        scan_gbs = in_bytes / (scan_ms / 1e3) / 1e9
+        stream = {"value": n * args.steps / sdt, "unit": "frames/s", "frames_per_step": n,
+                  "h2d_bytes_per_step": in_bytes, "d2h_bytes_per_step": y4m_bytes,
+                  "upload_ms": sum(x[1] for x in scans) / len(scans),
+                  "framing": {"kernel": "marker_candidates_kernel", "ms_per_launch": scan_ms, "candidates": scans[-1][2],
+                              "roofline": {"bound": "hbm", "achieved": scan_gbs, "peak": peak, "peak_kind": peak_kind,
+                                           "unit": "GB/s", "frac": scan_gbs / peak,
+                                           "algorithmic_bytes_per_launch": in_bytes}}}
+        del y4m, host_stream
+
     mixed = mixed_sweep(local) if rank == 0 and args.mixed else None
     serving, served80 = None, None
     if rank == 0 and args.serve_seconds > 0:
@@ -679,6 +726,7 @@ def main():
                            "served_p99_at_80pct": served80["p99_ms"] if served80 else None},
             "serving": serving,
             "mixed_autotuned_graphs": mixed,
+            "stream_y4m": stream,
             "stage_ms": stage_times,
             "idct_exact_sample_fraction": exact_frac,
             "roofline": roofline,

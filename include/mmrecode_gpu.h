@@ -282,6 +282,71 @@ MMR_API mmr_status mmr_gpu_server_set_slice_bits(mmr_gpu_server *server, uint32_
 MMR_API mmr_status mmr_gpu_server_set_tuning(mmr_gpu_server *server, const mmr_gpu_tune_entry *entries,
                                              size_t count);
 
+/*
+ * Whole-stream decode to Y4M: the reference CLI's `mmrecode decode <in> <out>`
+ * for MJPEG and raw DV input (crates/cli/src/main.rs:1533-1580, 1605-1633), with
+ * the stream uploaded once and framed on the GPU, every frame decoded in one
+ * batch from device memory, and the Y4M bytes its Y4mWriter would write
+ * (crates/containers/y4m/src/lib.rs:219-300) laid out in the caller's buffer.
+ * The reference CLI reads the file itself; these calls take its bytes.
+ */
+#define MMR_STREAM_NONE 0u   /* empty input: "input contains no media frames" */
+#define MMR_STREAM_MJPEG 1u  /* concatenated JFIF images, each ending after its EOI */
+#define MMR_STREAM_DV 2u     /* raw DV frames, profile from the first DIF block */
+#define MMR_STREAM_MPEGTS 3u /* MPEG transport stream: outside this library */
+#define MMR_STREAM_MPEG2 4u  /* MPEG-2 video elementary stream: outside this library */
+
+typedef struct mmr_gpu_stream mmr_gpu_stream;
+
+typedef struct mmr_gpu_stream_info {
+    size_t struct_size;
+    uint32_t kind;           /* MMR_STREAM_*, detected in the CLI's order (main.rs:1536-1553, 1908-1921) */
+    mmr_status frame_status; /* MMR_STATUS_OK, or the error that ends the framing after frame_count frames
+                                (a parse_jpeg error of the next image, an incomplete raw DV frame, ...) */
+    size_t frame_count;      /* frames framed before frame_status's error */
+    size_t y4m_bytes;        /* capacity mmr_gpu_stream_decode_y4m needs */
+    uint64_t candidates;     /* marker candidates the device scan found (MJPEG) */
+    double upload_ms;        /* device time of the stream's upload */
+    double scan_ms;          /* device time of the marker-candidate scan (MJPEG) */
+    char message[512];       /* frame_status's message as the CLI prints it, "" when OK */
+} mmr_gpu_stream_info;
+
+/*
+ * Uploads the stream and frames it. `data` must stay valid until the stream is
+ * closed, and the context must outlive the stream. `input_name` is the name the
+ * CLI would print in "'<input>' ends with an incomplete raw DV frame" (NULL:
+ * "input"). Returns MMR_STATUS_OK with a stream also when framing stops at an
+ * error (reported in *info); other statuses leave *out_stream NULL.
+ */
+MMR_API mmr_status mmr_gpu_stream_open(mmr_gpu_context *context, const uint8_t *data, size_t len,
+                                       const char *input_name, mmr_gpu_stream **out_stream,
+                                       mmr_gpu_stream_info *info);
+
+/* Offset and length in the stream of framed frame `index`. */
+MMR_API mmr_status mmr_gpu_stream_frame(const mmr_gpu_stream *stream, size_t index, uint64_t *offset,
+                                        uint64_t *length);
+
+typedef struct mmr_gpu_stream_result {
+    size_t struct_size;
+    mmr_status status;     /* the CLI's first error (a frame that fails to decode, one the Y4M writer
+                              rejects, then the framing error), MMR_STATUS_OK if none */
+    size_t frames_written; /* frames in the Y4M bytes */
+    size_t bytes_written;  /* Y4M bytes at the start of `out`: what the CLI's output file holds */
+    char message[512];     /* status's message as the CLI prints it, "" when OK */
+} mmr_gpu_stream_result;
+
+/*
+ * Decodes every framed frame and writes the Y4M stream to out[0, capacity)
+ * (capacity >= info.y4m_bytes; bytes past result->bytes_written are scratch).
+ * Returns MMR_STATUS_OK unless an argument is invalid or the device failed;
+ * the stream's own outcome is in *result.
+ */
+MMR_API mmr_status mmr_gpu_stream_decode_y4m(mmr_gpu_stream *stream, uint8_t *out, size_t capacity,
+                                             mmr_gpu_stream_result *result);
+
+/* Frees a stream and its device copy; NULL is ignored. */
+MMR_API void mmr_gpu_stream_close(mmr_gpu_stream *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -33,6 +33,7 @@ CODEC_MJPEG, CODEC_DV = 1, 2
 OUTPUT_PLANAR, OUTPUT_RGB24 = 0, 1
 ITEM_CONCEAL, ITEM_OUT_DEVICE = 1, 2
 DV_MODE_88, DV_MODE_ACTIVITY = 0, 1
+STREAM_NONE, STREAM_MJPEG, STREAM_DV, STREAM_MPEGTS, STREAM_MPEG2 = 0, 1, 2, 3, 4
 
 MJPEG_CODEC_NAME = "video/mjpeg"  # crates/codecs/mjpeg/src/codec.rs:12
 DV_CODEC_NAME = "video/dv"        # crates/codecs/dv/src/codec.rs:12
@@ -377,6 +378,138 @@ class Context:
             payload = ctypes.string_at(outs[i], it.out_bytes) if it.status == STATUS_OK else None
             res.append((r, payload))
         return res
+
+
+    def open_stream(self, data, input_name: str = "input") -> "MediaStream":
+        """Uploads a whole stream (concatenated JFIF images or raw DV frames) and frames it
+        on the GPU; see :class:`MediaStream`."""
+        return MediaStream(self, data, input_name)
+
+
+@dataclass
+class StreamOutcome:
+    """What the reference CLI's ``decode`` loop ends with: ``status`` and ``message`` of its
+    first error (0 and "" if none), and the frames and Y4M bytes written before it."""
+
+    status: int
+    message: str
+    frames_written: int
+    bytes_written: int
+
+
+class MediaStream:
+    """A whole MJPEG or raw DV stream framed on the GPU (``mmr_gpu_stream_*``), as the
+    reference CLI's ``decode`` command frames it (crates/cli/src/main.rs:1533-1580,
+    1605-1633). ``data`` is ``bytes`` or ``(address, length)`` of host memory that stays
+    valid while the stream is open (pinned memory uploads fastest)."""
+
+    def __init__(self, ctx: Context, data, input_name: str = "input"):
+        lib = _lib.load()
+        if isinstance(data, tuple):
+            addr, n = data
+        else:
+            self._keep = bytes(data)
+            addr, n = ctypes.cast(ctypes.c_char_p(self._keep), ctypes.c_void_p).value, len(self._keep)
+        self._ctx = ctx  # the stream uses the context's engines
+        info = _lib.StreamInfo()
+        info.struct_size = ctypes.sizeof(_lib.StreamInfo)
+        h = ctypes.c_void_p()
+        st = lib.mmr_gpu_stream_open(ctx._h, addr, n, input_name.encode(), ctypes.byref(h), ctypes.byref(info))
+        if st != STATUS_OK:
+            raise MmrError(st, _lib.last_error())
+        self._h = h
+        self.kind = info.kind
+        self.frame_status = info.frame_status
+        self.frame_message = info.message.decode("utf-8", "replace")
+        self.frame_count = info.frame_count
+        self.y4m_bytes = info.y4m_bytes
+        self.candidates = info.candidates
+        self.upload_ms = info.upload_ms
+        self.scan_ms = info.scan_ms
+
+    def frames(self) -> list:
+        """(offset, length) of every framed frame."""
+        lib = _lib.load()
+        out = []
+        off, ln = ctypes.c_uint64(), ctypes.c_uint64()
+        for i in range(self.frame_count):
+            st = lib.mmr_gpu_stream_frame(self._h, i, ctypes.byref(off), ctypes.byref(ln))
+            if st != STATUS_OK:
+                raise MmrError(st, _lib.last_error())
+            out.append((off.value, ln.value))
+        return out
+
+    def decode_into(self, address: int, capacity: int) -> StreamOutcome:
+        """Decodes every frame and writes the Y4M stream at ``address`` (host memory of at
+        least ``y4m_bytes``)."""
+        r = _lib.StreamResult()
+        r.struct_size = ctypes.sizeof(_lib.StreamResult)
+        st = _lib.load().mmr_gpu_stream_decode_y4m(self._h, address, capacity, ctypes.byref(r))
+        if st != STATUS_OK:
+            raise MmrError(st, _lib.last_error())
+        return StreamOutcome(r.status, r.message.decode("utf-8", "replace"), r.frames_written, r.bytes_written)
+
+    def decode_y4m(self) -> tuple:
+        """(:class:`StreamOutcome`, the Y4M bytes the CLI's output file holds)."""
+        if not self.frame_count:
+            return StreamOutcome(self.frame_status, self.frame_message, 0, 0), b""
+        buf = bytearray(self.y4m_bytes)
+        addr = ctypes.addressof((ctypes.c_char * len(buf)).from_buffer(buf))
+        res = self.decode_into(addr, len(buf))
+        return res, bytes(memoryview(buf)[: res.bytes_written])
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.load().mmr_gpu_stream_close(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def decode_stream_y4m(data, input_name: str = "input", ctx: Context | None = None) -> tuple:
+    """The reference CLI's ``decode`` on a stream's bytes: (:class:`StreamOutcome`, Y4M bytes)."""
+    own = ctx is None
+    ctx = ctx or Context()
+    try:
+        with ctx.open_stream(data, input_name) as ms:
+            return ms.decode_y4m()
+    finally:
+        if own:
+            ctx.close()
+
+
+def decode_file(input_path: str, output_path: str, ctx: Context | None = None) -> str:
+    """``mmrecode decode <input> <output>`` for MJPEG and raw DV input (crates/cli/src/
+    main.rs:1533-1580, 1605-1633): writes the Y4M file and returns the line the CLI prints,
+    or raises :class:`MmrError` with the CLI's error after writing what it would have
+    written (no file when the input is rejected before the output is created)."""
+    with open(input_path, "rb") as f:
+        data = f.read()
+    own = ctx is None
+    ctx = ctx or Context()
+    try:
+        with ctx.open_stream(data, str(input_path)) as ms:
+            if not ms.frame_count and (ms.kind != STREAM_MJPEG or not data):
+                # empty input, MPEG streams, an incomplete raw DV file: no output file
+                raise MmrError(ms.frame_status, ms.frame_message)
+            res, y4m = ms.decode_y4m()
+            kind = ms.kind
+    finally:
+        if own:
+            ctx.close()
+    with open(output_path, "wb") as f:
+        f.write(y4m)
+    if res.status != STATUS_OK:
+        raise MmrError(res.status, res.message)
+    what = "JPEG frame(s)" if kind == STREAM_MJPEG else "raw DV frame(s)"
+    return f"Decoded {res.frames_written} {what} to {output_path}"
 
 
 def _result(it) -> BatchResult:

@@ -99,6 +99,17 @@ class JpegEncodeOptions(ctypes.Structure):
                 ("restart_interval", ctypes.c_uint16)]
 
 
+class StreamInfo(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_size_t), ("kind", ctypes.c_uint32), ("frame_status", ctypes.c_int32),
+                ("frame_count", ctypes.c_size_t), ("y4m_bytes", ctypes.c_size_t), ("candidates", ctypes.c_uint64),
+                ("upload_ms", ctypes.c_double), ("scan_ms", ctypes.c_double), ("message", ctypes.c_char * 512)]
+
+
+class StreamResult(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_size_t), ("status", ctypes.c_int32), ("frames_written", ctypes.c_size_t),
+                ("bytes_written", ctypes.c_size_t), ("message", ctypes.c_char * 512)]
+
+
 # Every function the headers declare, with its ctypes signature.
 SIGNATURES = {
     "mmr_abi_version": ([], ctypes.c_uint32),
@@ -148,6 +159,13 @@ SIGNATURES = {
     "mmr_gpu_server_replay": ([ctypes.c_void_p, ctypes.POINTER(GpuItem), ctypes.c_size_t,
                               ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_double),
                               ctypes.POINTER(ctypes.c_int64)], ctypes.c_int32),
+    "mmr_gpu_stream_open": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_char_p,
+                            ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(StreamInfo)], ctypes.c_int32),
+    "mmr_gpu_stream_frame": ([ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_uint64),
+                             ctypes.POINTER(ctypes.c_uint64)], ctypes.c_int32),
+    "mmr_gpu_stream_decode_y4m": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(StreamResult)],
+                                  ctypes.c_int32),
+    "mmr_gpu_stream_close": ([ctypes.c_void_p], None),
 }
 
 _lib = None

@@ -16,9 +16,11 @@
 #include "engine.h"
 #include "last_error.h"
 #include "runtime.h"
+#include "stream.h"
 
 using mmr::Engine;
 using mmr::Item;
+using mmr::with_prefix;
 
 namespace {
 
@@ -30,17 +32,6 @@ thread_local std::string g_last_error;
 mmr_status finish(mmr_status st, const std::string &msg) {
     g_last_error = st == MMR_STATUS_OK ? std::string() : msg;
     return st;
-}
-
-// ApiError Display (lib.rs:73-80) and core Error Display (crates/core/src/error.rs:18-27).
-std::string with_prefix(int32_t st, const std::string &m) {
-    switch (st) {
-    case MMR_STATUS_INVALID_ARGUMENT: return "invalid argument: " + m;
-    case MMR_STATUS_INVALID_DATA: return "invalid data: " + m;
-    case MMR_STATUS_UNSUPPORTED: return "unsupported: " + m;
-    case MMR_STATUS_INVALID_STATE: return "invalid state: " + m;
-    default: return m;
-    }
 }
 
 mmr_status invalid_argument(const std::string &m) { return finish(MMR_STATUS_INVALID_ARGUMENT, "invalid argument: " + m); }
@@ -257,6 +248,10 @@ struct mmr_gpu_server {
     mmr::Server *server;
 };
 
+struct mmr_gpu_stream {
+    mmr::Stream *stream;
+};
+
 namespace {
 
 bool to_item(const mmr_gpu_item &g, Item &it, const char **err) {
@@ -273,7 +268,7 @@ bool to_item(const mmr_gpu_item &g, Item &it, const char **err) {
     it.len = g.len;
     it.codec = g.codec;
     it.output = g.output;
-    it.flags = (g.flags & MMR_ITEM_CONCEAL) ? mmr::kFlagConceal : 0;
+    it.flags = (g.flags & MMR_ITEM_CONCEAL) ? (uint32_t)mmr::kFlagConceal : 0u;
     it.out = static_cast<uint8_t *>(g.out);
     it.out_capacity = g.out_capacity;
     it.out_on_device = (g.flags & MMR_ITEM_OUT_DEVICE) != 0;
@@ -730,6 +725,75 @@ MMR_API mmr_status mmr_gpu_server_set_slice_bits(mmr_gpu_server *server, uint32_
     if (!server) return invalid_argument("server is null");
     if (!server->server->set_slice_bits(bits)) return invalid_argument("slice bits must be 0 or a multiple of 32 in 128..1048576");
     return finish(MMR_STATUS_OK, "");
+}
+
+MMR_API mmr_status mmr_gpu_stream_open(mmr_gpu_context *context, const uint8_t *data, size_t len,
+                                       const char *input_name, mmr_gpu_stream **out_stream,
+                                       mmr_gpu_stream_info *info) {
+    if (!out_stream) return invalid_argument("out_stream is null");
+    *out_stream = nullptr;
+    if (!context) return invalid_argument("context is null");
+    if (len > 0 && !data) return invalid_argument("data is null while length is nonzero");
+    if (info && info->struct_size != sizeof(mmr_gpu_stream_info)) return invalid_argument("info struct_size mismatch");
+    try {
+        mmr::Stream *s = new mmr::Stream(*context->pool, data, len, input_name ? input_name : "input");
+        if (info) {
+            memset(info, 0, sizeof(*info));
+            info->struct_size = sizeof(*info);
+            info->kind = s->kind();
+            info->frame_status = s->frame_status();
+            info->frame_count = s->frame_count();
+            info->y4m_bytes = s->y4m_bytes();
+            info->candidates = s->candidates();
+            info->upload_ms = s->upload_ms();
+            info->scan_ms = s->scan_ms();
+            snprintf(info->message, sizeof info->message, "%s", s->frame_message().c_str());
+        }
+        *out_stream = new mmr_gpu_stream{s};
+        return finish(MMR_STATUS_OK, "");
+    } catch (const std::exception &e) {
+        return finish(MMR_STATUS_INTERNAL_ERROR, std::string("CUDA device failure: ") + e.what());
+    } catch (...) {
+        return finish(MMR_STATUS_INTERNAL_ERROR, "panic contained at MMRecode C API boundary");
+    }
+}
+
+MMR_API mmr_status mmr_gpu_stream_frame(const mmr_gpu_stream *stream, size_t index, uint64_t *offset,
+                                        uint64_t *length) {
+    if (!stream) return invalid_argument("stream is null");
+    if (!offset || !length) return invalid_argument("offset or length is null");
+    if (index >= stream->stream->frame_count()) return invalid_argument("frame index out of range");
+    *offset = stream->stream->frame_offset(index);
+    *length = stream->stream->frame_length(index);
+    return finish(MMR_STATUS_OK, "");
+}
+
+MMR_API mmr_status mmr_gpu_stream_decode_y4m(mmr_gpu_stream *stream, uint8_t *out, size_t capacity,
+                                             mmr_gpu_stream_result *result) {
+    if (!stream) return invalid_argument("stream is null");
+    if (!result) return invalid_argument("result is null");
+    if (result->struct_size != sizeof(mmr_gpu_stream_result)) return invalid_argument("result struct_size mismatch");
+    if (stream->stream->frame_count() && (!out || capacity < stream->stream->y4m_bytes()))
+        return invalid_argument("output buffer is smaller than the stream's Y4M bytes");
+    try {
+        const mmr::StreamResult r = stream->stream->decode_y4m(out, capacity);
+        memset(result, 0, sizeof(*result));
+        result->struct_size = sizeof(*result);
+        result->status = r.status;
+        result->frames_written = r.frames_written;
+        result->bytes_written = r.bytes_written;
+        snprintf(result->message, sizeof result->message, "%s", r.message.c_str());
+        if (r.status == MMR_STATUS_INTERNAL_ERROR) return finish(MMR_STATUS_INTERNAL_ERROR, r.message);
+        return finish(MMR_STATUS_OK, "");
+    } catch (...) {
+        return finish(MMR_STATUS_INTERNAL_ERROR, "panic contained at MMRecode C API boundary");
+    }
+}
+
+MMR_API void mmr_gpu_stream_close(mmr_gpu_stream *stream) {
+    if (!stream) return;
+    delete stream->stream;
+    delete stream;
 }
 
 }  // extern "C"

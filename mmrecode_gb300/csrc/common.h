@@ -148,6 +148,14 @@ MMR_HD int32_t diag_status(uint16_t kind) {
     }
 }
 
+// 0x80 in each byte of x that is zero, else 0 (exact: (x & 0x7f) + 0x7f never
+// carries out of its byte).
+MMR_HD uint32_t zero_bytes(uint32_t x) { return ~(((x & 0x7f7f7f7fu) + 0x7f7f7f7fu) | x | 0x7f7f7f7fu); }
+
+// Nonzero iff some byte of w is 0xFF (the borrow test for a zero byte of ~w,
+// exact as a test for any).
+MMR_HD uint32_t any_ff(uint32_t w) { return (~w - 0x01010101u) & w & 0x80808080u; }
+
 MMR_HD Diag make_diag(uint16_t kind, uint32_t offset = 0, uint32_t aux = 0, uint32_t aux2 = 0) {
     Diag d;
     d.status = diag_status(kind);

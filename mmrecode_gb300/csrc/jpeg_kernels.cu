@@ -124,7 +124,7 @@ __device__ __forceinline__ bool plain_chunk(const uint8_t *in, uint32_t ds, uint
     const uint32_t w[4] = {v->x, v->y, v->z, v->w};
     bool ff = p > ds && in[p - 1] == 0xff;
 #pragma unroll
-    for (int i = 0; i < 4; i++) ff |= __vcmpeq4(w[i], 0xffffffffu) != 0;
+    for (int i = 0; i < 4; i++) ff |= any_ff(w[i]) != 0;
     return !ff;
 }
 
@@ -134,7 +134,7 @@ __device__ __forceinline__ uint32_t byte_mask(const uint4 &v, uint32_t b) {
     uint32_t m = 0;
 #pragma unroll
     for (int i = 0; i < 4; i++) {
-        const uint32_t e = __vcmpeq4(w[i], b * 0x01010101u);  // 0xff per equal byte
+        const uint32_t e = zero_bytes(w[i] ^ (b * 0x01010101u));  // 0x80 per equal byte
         m |= ((e >> 7) & 1u | (e >> 14) & 2u | (e >> 21) & 4u | (e >> 28) & 8u) << (4 * i);
     }
     return m;

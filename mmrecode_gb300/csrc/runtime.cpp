@@ -68,13 +68,17 @@ bool EnginePool::stage(const Item *items, size_t n) {
     bool any = false;
     for (size_t i = 0; i < n; i++) {
         const Item &it = items[i];
-        // single-buffer host payloads (planes written to separate pointers stay on the engine's path)
-        if (it.dev_data || !it.data || !it.len || it.out_on_device || !it.out || !it.out_capacity || it.plane_out[0])
-            continue;
-        redirected_[i] = 1;
+        // single-buffer host outputs (planes written to separate pointers stay on the
+        // engine's path), with their packets when those are in host memory too
+        if (it.out_on_device || !it.out || !it.out_capacity || it.plane_out[0]) continue;
+        if (!it.dev_data && (!it.data || !it.len)) continue;
+        redirected_[i] = kStagedOut;
         any = true;
-        in_off[i] = total;
-        total += (it.len + 255) / 256 * 256;
+        if (!it.dev_data) {
+            redirected_[i] |= kStagedIn;
+            in_off[i] = total;
+            total += (it.len + 255) / 256 * 256;
+        }
         out_off[i] = total;
         total += (it.out_capacity + 255) / 256 * 256;
     }
@@ -94,7 +98,7 @@ bool EnginePool::stage(const Item *items, size_t n) {
     uint8_t *base = static_cast<uint8_t *>(stage_ptr_);
     for (size_t i = 0; i < n; i++) {
         if (!redirected_[i]) continue;
-        staged_[i].dev_data = base + in_off[i];
+        if (redirected_[i] & kStagedIn) staged_[i].dev_data = base + in_off[i];
         staged_[i].out = base + out_off[i];
         staged_[i].out_on_device = true;
     }
@@ -130,7 +134,7 @@ void EnginePool::worker(int k) {
             c.status = kOk;
             if (staging) {  // inputs up, ahead of the chunk's kernels on the same stream
                 for (size_t j = 0; j < c.n && c.status == kOk; j++)
-                    if (redirected_[c.first + j] &&
+                    if ((redirected_[c.first + j] & kStagedIn) &&
                         cudaMemcpyAsync(const_cast<uint8_t *>(c.items[j].dev_data), c.items[j].data, c.items[j].len,
                                         cudaMemcpyHostToDevice, e.stream()) != cudaSuccess)
                         c.status = kInternal;
@@ -142,7 +146,7 @@ void EnginePool::worker(int k) {
             if (staging && c.status == kOk) {  // outputs down, while this engine takes its next chunk
                 for (size_t j = 0; j < c.n && c.status == kOk; j++) {
                     const Item &it = c.items[j];
-                    if (redirected_[c.first + j] && it.status == kOk && it.out_bytes &&
+                    if ((redirected_[c.first + j] & kStagedOut) && it.status == kOk && it.out_bytes &&
                         cudaMemcpyAsync(orig_[c.first + j].out, it.out, it.out_bytes, cudaMemcpyDeviceToHost,
                                         down_[k]) != cudaSuccess)
                         c.status = kInternal;

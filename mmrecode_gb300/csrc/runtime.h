@@ -48,9 +48,9 @@ public:
     EnginePool &operator=(const EnginePool &) = delete;
 
     // Decodes the items; batches of at least 2 * min_chunk items are split into
-    // chunks decoded concurrently by all engines. Payloads in host memory are
-    // staged through device buffers: a chunk's inputs go up on its engine's
-    // stream, the chunk decodes device-resident (and replays as a graph when it
+    // chunks decoded concurrently by all engines. Outputs in host memory (and
+    // packets in host memory) are staged through device buffers: a chunk's
+    // packets go up on its engine's stream, the chunk decodes device-resident (and replays as a graph when it
     // repeats), and its outputs come down on the engine's download stream while
     // the engine takes its next chunk. Staged chunk i runs at stream priority
     // level i, so concurrent chunks finish in order and their downloads spread
@@ -70,6 +70,7 @@ public:
     // Installs a table (from autotune, or saved from an earlier one) on all engines.
     void set_tuning(const std::vector<TuneResult> &table);
     int size() const { return (int)engines_.size(); }
+    int device() const { return device_; }
     Engine &engine(int k) { return *engines_[k]; }
     static constexpr size_t kMinChunk = 16;
 
@@ -93,7 +94,9 @@ private:
     void *stage_ptr_ = nullptr;
     size_t stage_cap_ = 0;
     std::vector<Item> staged_;
-    std::vector<uint8_t> redirected_;  // per item: payloads go through staging
+    std::vector<uint8_t> redirected_;  // per item: kStagedIn | kStagedOut
+    static constexpr uint8_t kStagedIn = 1;   // the packet goes up through the staging buffer
+    static constexpr uint8_t kStagedOut = 2;  // the output comes down from it
     const Item *orig_ = nullptr;       // the caller's items of the current batch
     std::vector<std::thread> threads_;
     std::mutex call_mu_;  // one decode call at a time
