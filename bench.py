@@ -14,6 +14,8 @@ quality 90, Annex K Huffman tables, restart interval = one MCU row (120 MCUs of
   stream_y4m  the same frames as one MJPEG file through the CLI's decode path
           (mmr_gpu_stream_*): upload, framing on the GPU, batch decode, the
           Y4M stream (planar 4:2:2) in pinned host memory.
+  encode_gpu  the encoder side: the decoded frames encoded back to JPEG on the
+          GPU (mmr_gpu_jpeg_encode_batch, byte-identical to the CPU encoder).
 
 Inputs (337 MB) and outputs (1.87 GB) per step exceed the 129 MB L2, so no L2
 flush is needed between steps.
@@ -395,6 +397,99 @@ def serving_sweep(local: int, seconds: float, frames_per_stream: int = 3):
 MIXED_SEED = 20261205
 
 
+def encode_bench(ctx, packets, args, local, m, _lib):
+    """The encoder side (mmr_gpu_jpeg_encode_batch): the workload's frames, decoded to
+    planar 4:2:2 on the device, encoded back at the workload's settings (q90, Annex K
+    tables, restart interval one MCU row); device-resident and from/to pinned host
+    memory, two frames checked against the CPU encoder, which is also timed."""
+    import ctypes
+
+    import torch
+
+    n = len(packets)
+    cw = (W + 1) // 2
+    pbytes = W * H + 2 * cw * H
+    dev = f"cuda:{local}"
+    planar = torch.empty(n * pbytes, dtype=torch.uint8, device=dev)
+    dec = (_lib.GpuItem * n)()
+    for i, p in enumerate(packets):
+        it = dec[i]
+        it.struct_size = ctypes.sizeof(_lib.GpuItem)
+        it.data = ctypes.cast(ctypes.c_char_p(p), ctypes.c_void_p)
+        it.len = len(p)
+        it.codec, it.output, it.flags = m.CODEC_MJPEG, m.OUTPUT_PLANAR, m.ITEM_OUT_DEVICE
+        it.out = planar.data_ptr() + i * pbytes
+        it.out_capacity = pbytes
+    ctx.decode_raw(dec)
+    assert all(dec[i].status == 0 for i in range(n))
+    cap = 4 << 20  # per frame (a q90 1080p 4:2:2 frame encodes to about 1.1 MB)
+    dev_out = torch.empty(n * cap, dtype=torch.uint8, device=dev)
+    host_planar = torch.empty(n * pbytes, dtype=torch.uint8, pin_memory=True)
+    host_planar.copy_(planar)
+    host_out = torch.empty(n * cap, dtype=torch.uint8, pin_memory=True)
+
+    def items(device: bool):
+        arr = (_lib.EncodeItem * n)()
+        base_in = planar.data_ptr() if device else host_planar.data_ptr()
+        base_out = dev_out.data_ptr() if device else host_out.data_ptr()
+        for i in range(n):
+            it = arr[i]
+            it.struct_size = ctypes.sizeof(_lib.EncodeItem)
+            v = it.frame
+            v.struct_size = ctypes.sizeof(_lib.VideoFrameView)
+            v.format, v.range, v.width, v.height, v.plane_count = m.YUV422P8, m.RANGE_FULL, W, H, 3
+            offs = (0, W * H, W * H + cw * H)
+            for c, (pw, off) in enumerate(zip((W, cw, cw), offs)):
+                v.planes[c].data = ctypes.cast(base_in + i * pbytes + off, _lib.u8p)
+                v.planes[c].data_len, v.planes[c].stride, v.planes[c].width, v.planes[c].height = pw * H, pw, pw, H
+            it.flags = (m.ITEM_IN_DEVICE | m.ITEM_OUT_DEVICE) if device else 0
+            it.out = base_out + i * cap
+            it.out_capacity = cap
+        return arr
+
+    def timed(arr):
+        for _ in range(args.warmup):
+            ctx.encode_raw(arr, Q, True, RI)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for _ in range(args.steps):
+            ctx.encode_raw(arr, Q, True, RI)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t
+        assert all(arr[i].status == 0 for i in range(n)), arr[0].message
+        return dt, ctx.encode_stats()
+
+    resident = items(True)
+    dt, st = timed(resident)
+    hostbuf = items(False)
+    edt, _ = timed(hostbuf)
+    # two frames against the CPU encoder restatement (byte-identical to the reference's)
+    cpu_t, same = 0.0, True
+    hp = host_planar.numpy()
+    for i in range(2):
+        y = hp[i * pbytes:i * pbytes + W * H].tobytes()
+        cb = hp[i * pbytes + W * H:i * pbytes + W * H + cw * H].tobytes()
+        cr = hp[i * pbytes + W * H + cw * H:(i + 1) * pbytes].tobytes()
+        fr = m.VideoFrame(m.YUV422P8, W, H, [m.Plane(y, W, W, H), m.Plane(cb, cw, cw, H), m.Plane(cr, cw, cw, H)],
+                          m.RANGE_FULL)
+        t0 = time.perf_counter()
+        ref = m.encode_jpeg(fr, Q, True, RI)
+        cpu_t += time.perf_counter() - t0
+        got = dev_out[i * cap:i * cap + resident[i].out_len].cpu().numpy().tobytes()
+        same &= got == ref
+    out_bytes = sum(resident[i].out_len for i in range(n))
+    return {"value": n * args.steps / dt, "unit": "frames/s", "frames_per_step": n,
+            "config": "decoded 1920x1080 4:2:2 frames -> JPEG q90, Annex K tables, restart interval 120 MCUs",
+            "device_ms_per_step": st["device_ms"], "blocks_per_step": st["blocks"],
+            "exact_coefficient_fraction": st["exact_coefficients"] / max(1, 64 * st["blocks"]),
+            "jpeg_bytes_per_step": out_bytes,
+            "e2e": {"value": n * args.steps / edt, "unit": "frames/s", "h2d_bytes_per_step": n * pbytes,
+                    "d2h_bytes_per_step": out_bytes},
+            "bit_exact_sample": bool(same),
+            "cpu_encoder": {"value": 2 / cpu_t, "unit": "frames/s", "cores": 1,
+                            "sample": "2 of the frames, the CPU encoder restatement on one core"}}
+
+
 def mixed_sweep(local: int, steps: int = 5, warmup: int = 3):
     """C4: 512 MJPEG frames, sizes in steps of 16 over 320x240..3840x2160, 4:2:0 /
     4:2:2 / 4:4:4, q 50..95, restart interval none / one MCU row / 4 MCUs, RGB24
@@ -470,6 +565,8 @@ def main():
     ap.add_argument("--plain-frames", type=int, default=60)
     ap.add_argument("--serve-seconds", type=float, default=2.0, help="seconds per serving load level (0: skip)")
     ap.add_argument("--mixed", type=int, default=1, help="run the 512-frame mixed batch (0: skip)")
+    ap.add_argument("--encode", type=int, default=1,
+                    help="encode the workload's decoded frames back to JPEG on the GPU (0: skip)")
     ap.add_argument("--stream", type=int, default=1,
                     help="decode the workload as one MJPEG file to Y4M, framed on the GPU (0: skip)")
     ap.add_argument("--graphs", type=int, default=1,
@@ -673,6 +770,8 @@ def main():
                                            "algorithmic_bytes_per_launch": in_bytes}}}
         del y4m, host_stream
 
+    encode = encode_bench(ctx, packets, args, local, m, _lib) if rank == 0 and args.encode else None
+
     mixed = mixed_sweep(local) if rank == 0 and args.mixed else None
     serving, served80 = None, None
     if rank == 0 and args.serve_seconds > 0:
@@ -727,6 +826,7 @@ def main():
             "serving": serving,
             "mixed_autotuned_graphs": mixed,
             "stream_y4m": stream,
+            "encode_gpu": encode,
             "stage_ms": stage_times,
             "idct_exact_sample_fraction": exact_frac,
             "roofline": roofline,

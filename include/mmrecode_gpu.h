@@ -177,6 +177,49 @@ typedef struct mmr_jpeg_encode_options {
 MMR_API mmr_status mmr_mjpeg_encode_ex(const mmr_video_frame_view *frame, const mmr_jpeg_encode_options *options,
                                        mmr_buffer *out_buffer);
 
+/*
+ * Batch JPEG encode on the GPU: the forward DCT, quantisation and Huffman coding
+ * of encode_jpeg (crates/codecs/mjpeg/src/encoder.rs:44-87, 341-545) for many
+ * frames per pass, every output byte equal to mmr_mjpeg_encode_ex's with the same
+ * options (mmr_mjpeg_encode's with quality only). No counterpart in the reference
+ * library.
+ */
+#define MMR_ITEM_IN_DEVICE 4u /* encode: the frame's plane data is device memory */
+
+typedef struct mmr_gpu_encode_item {
+    size_t struct_size;
+    mmr_video_frame_view frame; /* planar input (host memory, or device with MMR_ITEM_IN_DEVICE) */
+    uint32_t flags;             /* MMR_ITEM_IN_DEVICE, MMR_ITEM_OUT_DEVICE */
+    uint8_t *out;               /* the JPEG bytes (host, or device with MMR_ITEM_OUT_DEVICE) */
+    size_t out_capacity;        /* mmr_gpu_jpeg_encode_bound() always suffices */
+    /* filled in by the call */
+    mmr_status status;
+    size_t out_len;
+    char message[200];          /* per-item diagnostic, "" on success */
+} mmr_gpu_encode_item;
+
+/* An output capacity that holds any encoded frame of this format and size. */
+MMR_API size_t mmr_gpu_jpeg_encode_bound(mmr_pixel_format format, size_t width, size_t height,
+                                         uint16_t restart_interval);
+
+/*
+ * Encodes `count` frames with one set of options in one pass on the context's
+ * device. Per-item status in items[i].status; the call returns MMR_STATUS_OK
+ * unless its arguments are invalid or the device failed.
+ */
+MMR_API mmr_status mmr_gpu_jpeg_encode_batch(mmr_gpu_context *context, const mmr_jpeg_encode_options *options,
+                                             mmr_gpu_encode_item *items, size_t count);
+
+typedef struct mmr_gpu_encode_stats {
+    size_t struct_size;
+    double device_ms;            /* uploads, kernels and downloads of the last encode batch */
+    uint64_t blocks;             /* 8x8 blocks transformed */
+    uint64_t exact_coefficients; /* quotients the fp32 transform left to the binary64 recomputation */
+    uint64_t bytes_out;          /* JPEG bytes produced */
+} mmr_gpu_encode_stats;
+
+MMR_API mmr_status mmr_gpu_last_encode_stats(const mmr_gpu_context *context, mmr_gpu_encode_stats *stats);
+
 #define MMR_DV_MODE_88 0u       /* every block 8-8 (the reference encoder) */
 #define MMR_DV_MODE_ACTIVITY 1u /* 2-4-8 where inter-field activity exceeds intra-field activity */
 

@@ -31,7 +31,7 @@ GRAY8, YUV420P8, YUV422P8, YUV444P8, YUV411P8 = 1, 2, 3, 4, 5
 RANGE_UNSPECIFIED, RANGE_FULL, RANGE_LIMITED = 0, 1, 2
 CODEC_MJPEG, CODEC_DV = 1, 2
 OUTPUT_PLANAR, OUTPUT_RGB24 = 0, 1
-ITEM_CONCEAL, ITEM_OUT_DEVICE = 1, 2
+ITEM_CONCEAL, ITEM_OUT_DEVICE, ITEM_IN_DEVICE = 1, 2, 4
 DV_MODE_88, DV_MODE_ACTIVITY = 0, 1
 STREAM_NONE, STREAM_MJPEG, STREAM_DV, STREAM_MPEGTS, STREAM_MPEG2 = 0, 1, 2, 3, 4
 
@@ -379,6 +379,45 @@ class Context:
             res.append((r, payload))
         return res
 
+
+    def encode_raw(self, items, quality: int = 75, annex_k: bool = False, restart_interval: int = 0) -> None:
+        """``mmr_gpu_jpeg_encode_batch`` on a prepared ``(_lib.EncodeItem * n)`` array."""
+        o = _lib.JpegEncodeOptions(ctypes.sizeof(_lib.JpegEncodeOptions), quality, 1 if annex_k else 0,
+                                   restart_interval)
+        st = _lib.load().mmr_gpu_jpeg_encode_batch(self._h, ctypes.byref(o), items, len(items))
+        if st != STATUS_OK:
+            raise MmrError(st, _lib.last_error())
+
+    def encode_jpeg_batch(self, frames, quality: int = 75, annex_k: bool = False,
+                          restart_interval: int = 0) -> list:
+        """Encodes host frames in one GPU pass; (status, message, JPEG bytes or None) per frame,
+        the bytes equal to :func:`encode_jpeg`'s with the same options."""
+        lib = _lib.load()
+        n = len(frames)
+        items = (_lib.EncodeItem * n)()
+        keep, outs = [], []
+        for i, fr in enumerate(frames):
+            it = items[i]
+            it.struct_size = ctypes.sizeof(_lib.EncodeItem)
+            it.frame = _view(fr, keep)
+            cap = lib.mmr_gpu_jpeg_encode_bound(fr.format, fr.width, fr.height, restart_interval)
+            buf = ctypes.create_string_buffer(cap)
+            outs.append(buf)
+            it.out = ctypes.cast(buf, ctypes.c_void_p)
+            it.out_capacity = cap
+        self.encode_raw(items, quality, annex_k, restart_interval)
+        return [(items[i].status, items[i].message.decode("utf-8", "replace"),
+                 outs[i].raw[: items[i].out_len] if items[i].status == STATUS_OK else None) for i in range(n)]
+
+    def encode_stats(self) -> dict:
+        """Device time, blocks, binary64 recomputations and bytes of the last encode batch."""
+        st_ = _lib.EncodeStats()
+        st_.struct_size = ctypes.sizeof(_lib.EncodeStats)
+        st = _lib.load().mmr_gpu_last_encode_stats(self._h, ctypes.byref(st_))
+        if st != STATUS_OK:
+            raise MmrError(st, _lib.last_error())
+        return {"device_ms": st_.device_ms, "blocks": st_.blocks, "exact_coefficients": st_.exact_coefficients,
+                "bytes_out": st_.bytes_out}
 
     def open_stream(self, data, input_name: str = "input") -> "MediaStream":
         """Uploads a whole stream (concatenated JFIF images or raw DV frames) and frames it

@@ -99,6 +99,17 @@ class JpegEncodeOptions(ctypes.Structure):
                 ("restart_interval", ctypes.c_uint16)]
 
 
+class EncodeItem(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_size_t), ("frame", VideoFrameView), ("flags", ctypes.c_uint32),
+                ("out", ctypes.c_void_p), ("out_capacity", ctypes.c_size_t), ("status", ctypes.c_int32),
+                ("out_len", ctypes.c_size_t), ("message", ctypes.c_char * 200)]
+
+
+class EncodeStats(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_size_t), ("device_ms", ctypes.c_double), ("blocks", ctypes.c_uint64),
+                ("exact_coefficients", ctypes.c_uint64), ("bytes_out", ctypes.c_uint64)]
+
+
 class StreamInfo(ctypes.Structure):
     _fields_ = [("struct_size", ctypes.c_size_t), ("kind", ctypes.c_uint32), ("frame_status", ctypes.c_int32),
                 ("frame_count", ctypes.c_size_t), ("y4m_bytes", ctypes.c_size_t), ("candidates", ctypes.c_uint64),
@@ -166,6 +177,10 @@ SIGNATURES = {
     "mmr_gpu_stream_decode_y4m": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(StreamResult)],
                                   ctypes.c_int32),
     "mmr_gpu_stream_close": ([ctypes.c_void_p], None),
+    "mmr_gpu_jpeg_encode_bound": ([ctypes.c_uint32, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_uint16], ctypes.c_size_t),
+    "mmr_gpu_jpeg_encode_batch": ([ctypes.c_void_p, ctypes.POINTER(JpegEncodeOptions), ctypes.POINTER(EncodeItem),
+                                  ctypes.c_size_t], ctypes.c_int32),
+    "mmr_gpu_last_encode_stats": ([ctypes.c_void_p, ctypes.POINTER(EncodeStats)], ctypes.c_int32),
 }
 
 _lib = None

@@ -13,6 +13,7 @@
 #include "../../include/mmrecode.h"
 #include "../../include/mmrecode_gpu.h"
 #include "encode.h"
+#include "encode_gpu.h"
 #include "engine.h"
 #include "last_error.h"
 #include "runtime.h"
@@ -242,6 +243,8 @@ struct mmr_gpu_context {
     double last_ms;
     uint32_t last_launches;
     mmr::EngineTimes times;
+    mmr::GpuJpegEncoder *encoder = nullptr;  // created by the first encode batch
+    std::mutex encoder_mu;
 };
 
 struct mmr_gpu_server {
@@ -412,7 +415,11 @@ MMR_API mmr_status mmr_gpu_context_create(const mmr_gpu_config *config, mmr_gpu_
         return finish(MMR_STATUS_INTERNAL_ERROR, "no usable CUDA device for the GPU decoder");
     }
     try {
-        mmr_gpu_context *c = new mmr_gpu_context{new mmr::EnginePool(device, engines), 0.0, 0, mmr::EngineTimes()};
+        mmr::EnginePool *pool = new mmr::EnginePool(device, engines);
+        mmr_gpu_context *c = new mmr_gpu_context;
+        c->pool = pool;
+        c->last_ms = 0.0;
+        c->last_launches = 0;
         *out_context = c;
         return finish(MMR_STATUS_OK, "");
     } catch (const std::exception &e) {
@@ -422,6 +429,7 @@ MMR_API mmr_status mmr_gpu_context_create(const mmr_gpu_config *config, mmr_gpu_
 
 MMR_API void mmr_gpu_context_destroy(mmr_gpu_context *context) {
     if (!context) return;
+    delete context->encoder;
     delete context->pool;
     delete context;
 }
@@ -794,6 +802,85 @@ MMR_API void mmr_gpu_stream_close(mmr_gpu_stream *stream) {
     if (!stream) return;
     delete stream->stream;
     delete stream;
+}
+
+MMR_API size_t mmr_gpu_jpeg_encode_bound(mmr_pixel_format format, size_t width, size_t height,
+                                         uint16_t restart_interval) {
+    return mmr::jpeg_encode_bound(format, width, height, restart_interval);
+}
+
+MMR_API mmr_status mmr_gpu_jpeg_encode_batch(mmr_gpu_context *context, const mmr_jpeg_encode_options *options,
+                                             mmr_gpu_encode_item *items, size_t count) {
+    if (!context) return invalid_argument("context is null");
+    if (!options) return invalid_argument("options is null");
+    if (options->struct_size != sizeof(mmr_jpeg_encode_options)) return invalid_argument("options struct_size mismatch");
+    if (count && !items) return invalid_argument("items is null");
+    try {
+        for (size_t i = 0; i < count; i++)
+            if (items[i].struct_size != sizeof(mmr_gpu_encode_item)) return invalid_argument("item struct_size mismatch");
+        std::vector<mmr::EncodeItem> work;
+        std::vector<size_t> index;
+        for (size_t i = 0; i < count; i++) {
+            mmr_gpu_encode_item &g = items[i];
+            g.out_len = 0;
+            g.message[0] = 0;
+            mmr::EncodeItem it;
+            memset(&it.frame, 0, sizeof(it.frame));
+            if (g.frame.struct_size != sizeof(mmr_video_frame_view)) {
+                g.status = MMR_STATUS_INVALID_ARGUMENT;
+                snprintf(g.message, sizeof g.message, "invalid argument: frame struct_size is %zu, expected %zu",
+                         g.frame.struct_size, sizeof(mmr_video_frame_view));
+                continue;
+            }
+            const mmr_status st = frame_from_view(&g.frame, it.frame);  // the ABI's view checks (lib.rs:1061-1127)
+            if (st != MMR_STATUS_OK) {
+                g.status = st;
+                snprintf(g.message, sizeof g.message, "%s", g_last_error.c_str());
+                continue;
+            }
+            it.in_on_device = (g.flags & MMR_ITEM_IN_DEVICE) != 0;
+            it.out_on_device = (g.flags & MMR_ITEM_OUT_DEVICE) != 0;
+            it.out = g.out;
+            it.out_capacity = g.out_capacity;
+            work.push_back(it);
+            index.push_back(i);
+        }
+        mmr::JpegEncodeOptions o;
+        o.quality = options->quality;
+        o.annex_k = options->annex_k_huffman != 0;
+        o.restart_interval = options->restart_interval;
+        int32_t st = mmr::kOk;
+        {
+            std::lock_guard<std::mutex> g(context->encoder_mu);
+            if (!context->encoder) context->encoder = new mmr::GpuJpegEncoder(context->pool->device());
+            st = context->encoder->encode(work.data(), work.size(), o);
+        }
+        for (size_t k = 0; k < work.size(); k++) {
+            mmr_gpu_encode_item &g = items[index[k]];
+            g.status = work[k].status;
+            g.out_len = work[k].out_len;
+            const std::string m = work[k].status == MMR_STATUS_OK ? std::string() : with_prefix(work[k].status, work[k].message);
+            snprintf(g.message, sizeof g.message, "%s", m.c_str());
+        }
+        if (st != mmr::kOk) return finish(MMR_STATUS_INTERNAL_ERROR, "CUDA device failure during encode");
+        return finish(MMR_STATUS_OK, "");
+    } catch (const std::exception &e) {
+        return finish(MMR_STATUS_INTERNAL_ERROR, std::string("could not run the GPU encoder: ") + e.what());
+    } catch (...) {
+        return finish(MMR_STATUS_INTERNAL_ERROR, "panic contained at MMRecode C API boundary");
+    }
+}
+
+MMR_API mmr_status mmr_gpu_last_encode_stats(const mmr_gpu_context *context, mmr_gpu_encode_stats *stats) {
+    if (!context) return invalid_argument("context is null");
+    if (!stats) return invalid_argument("stats is null");
+    if (stats->struct_size != sizeof(mmr_gpu_encode_stats)) return invalid_argument("stats struct_size mismatch");
+    const mmr::EncodeStats t = context->encoder ? context->encoder->last_stats() : mmr::EncodeStats();
+    stats->device_ms = t.device_ms;
+    stats->blocks = t.blocks;
+    stats->exact_coefficients = t.exact_coefficients;
+    stats->bytes_out = t.bytes_out;
+    return finish(MMR_STATUS_OK, "");
 }
 
 }  // extern "C"

@@ -85,14 +85,8 @@ Table annex(uint8_t cls, uint8_t id, const uint8_t *bits, const uint8_t *vals, s
     return t;
 }
 
-struct Code {
-    uint16_t bits;
-    uint8_t length;
-    bool present;
-};
-
 // encoder.rs:427-473 HuffmanEncoder::new
-bool huffman_encoder(const Table &t, Code codes[256]) {
+bool huffman_encoder(const Table &t, HuffCode codes[256]) {
     for (int i = 0; i < 256; i++) codes[i] = {0, 0, false};
     uint32_t code = 0;
     size_t si = 0;
@@ -182,39 +176,39 @@ struct Comp {
 
 }  // namespace
 
-EncodeResult encode_jpeg(const FrameIn &f, const JpegEncodeOptions &opt) {
-    EncodeResult r;
+bool plan_jpeg_encode(const FrameIn &f, const JpegEncodeOptions &opt, JpegEncodePlan *plan) {
+    JpegEncodePlan &P = *plan;
     auto fail = [&](int32_t st, const char *m) {
-        r.status = st;
-        r.message = m;
-        r.data.clear();
-        return r;
+        P.status = st;
+        P.message = m;
+        return false;
     };
     // validate_frame (encoder.rs:101-160)
     if (f.width == 0 || f.height == 0 || f.width > 65535 || f.height > 65535)
         return fail(kInvalidData, "JPEG frame dimensions must be between 1 and 65535");
     if (f.range == kRangeLimited)
         return fail(kUnsupported, "limited-range input requires conversion to full-range JPEG samples");
-    std::vector<Comp> comps;
+    Comp comps[3] = {{1, 1, 1, 0}, {2, 1, 1, 1}, {3, 1, 1, 1}};
+    size_t nc = 3;
     switch (f.format) {
-    case kGray8: comps = {{1, 1, 1, 0}}; break;
-    case kYuv420: comps = {{1, 2, 2, 0}, {2, 1, 1, 1}, {3, 1, 1, 1}}; break;
-    case kYuv422: comps = {{1, 2, 1, 0}, {2, 1, 1, 1}, {3, 1, 1, 1}}; break;
-    case kYuv444: comps = {{1, 1, 1, 0}, {2, 1, 1, 1}, {3, 1, 1, 1}}; break;
+    case kGray8: nc = 1; break;
+    case kYuv420: comps[0].h = comps[0].v = 2; break;
+    case kYuv422: comps[0].h = 2; break;
+    case kYuv444: break;
     default: return fail(kUnsupported, "pixel format is not supported by JPEG");
     }
     uint8_t hmax = 1, vmax = 1;
-    for (auto &c : comps) {
-        hmax = std::max(hmax, c.h);
-        vmax = std::max(vmax, c.v);
+    for (size_t i = 0; i < nc; i++) {
+        hmax = std::max(hmax, comps[i].h);
+        vmax = std::max(vmax, comps[i].v);
     }
     // validate_input_planes (encoder.rs:177-215)
-    if (f.plane_count != comps.size()) {
+    if (f.plane_count != nc) {
         char m[128];
-        snprintf(m, sizeof m, "JPEG input requires %zu plane(s), found %zu", comps.size(), f.plane_count);
+        snprintf(m, sizeof m, "JPEG input requires %zu plane(s), found %zu", nc, f.plane_count);
         return fail(kInvalidData, m);
     }
-    for (size_t i = 0; i < comps.size(); i++) {
+    for (size_t i = 0; i < nc; i++) {
         size_t w = (f.width * comps[i].h + hmax - 1) / hmax, h = (f.height * comps[i].v + vmax - 1) / vmax;
         const PlaneIn &p = f.planes[i];
         if (p.width != w || p.height != h || p.stride < w || p.data_len < p.stride * p.height) {
@@ -225,10 +219,21 @@ EncodeResult encode_jpeg(const FrameIn &f, const JpegEncodeOptions &opt) {
     }
     if (opt.quality < 1 || opt.quality > 100) return fail(kInvalidData, "JPEG quality must be between 1 and 100");
 
-    uint8_t qt[2][64];
-    scale_quant(kLumaQ, opt.quality, qt[0]);
-    scale_quant(kChromaQ, opt.quality, qt[1]);
-    bool multi = comps.size() > 1;
+    P.ncomp = (uint32_t)nc;
+    for (size_t i = 0; i < nc; i++) {
+        P.comp_h[i] = comps[i].h;
+        P.comp_v[i] = comps[i].v;
+        P.comp_tq[i] = comps[i].tq;
+        P.comp_table[i] = opt.annex_k ? comps[i].tq : 0;
+    }
+    P.hmax = hmax;
+    P.vmax = vmax;
+    P.mcu_cols = (f.width + (size_t)hmax * 8 - 1) / ((size_t)hmax * 8);
+    P.mcu_rows = (f.height + (size_t)vmax * 8 - 1) / ((size_t)vmax * 8);
+    P.restart_interval = opt.restart_interval;
+    scale_quant(kLumaQ, opt.quality, P.qt[0]);
+    scale_quant(kChromaQ, opt.quality, P.qt[1]);
+    const bool multi = nc > 1;
     std::vector<Table> tables;
     if (opt.annex_k) {
         tables.push_back(annex(0, 0, kDcLumaBits, kDcVals, 12));
@@ -241,31 +246,32 @@ EncodeResult encode_jpeg(const FrameIn &f, const JpegEncodeOptions &opt) {
         tables.push_back(simple_dc());
         tables.push_back(simple_ac());
     }
-    Code dc_codes[2][256], ac_codes[2][256];
+    for (int k = 0; k < 2; k++)
+        for (int i = 0; i < 256; i++) P.dc[k][i] = P.ac[k][i] = {0, 0, false};
     for (auto &t : tables)
-        if (!huffman_encoder(t, t.cls ? ac_codes[t.id] : dc_codes[t.id]))
+        if (!huffman_encoder(t, t.cls ? P.ac[t.id] : P.dc[t.id]))
             return fail(kInvalidData, "JPEG Huffman table is oversubscribed");
 
-    std::vector<uint8_t> &out = r.data;
+    std::vector<uint8_t> &out = P.header;
     out = {0xff, 0xd8};
     segment(out, 0xe0, {'J', 'F', 'I', 'F', 0, 1, 2, 0, 0, 1, 0, 1, 0, 0});
     {  // DQT (encoder.rs:269-283)
         std::vector<uint8_t> p;
         p.push_back(0);
-        for (int k = 0; k < 64; k++) p.push_back(qt[0][kZigzag[k]]);
+        for (int k = 0; k < 64; k++) p.push_back(P.qt[0][kZigzag[k]]);
         if (multi) {
             p.push_back(1);
-            for (int k = 0; k < 64; k++) p.push_back(qt[1][kZigzag[k]]);
+            for (int k = 0; k < 64; k++) p.push_back(P.qt[1][kZigzag[k]]);
         }
         segment(out, 0xdb, p);
     }
     {  // SOF0 (encoder.rs:285-310)
         std::vector<uint8_t> p = {8, (uint8_t)(f.height >> 8), (uint8_t)f.height, (uint8_t)(f.width >> 8),
-                                  (uint8_t)f.width, (uint8_t)comps.size()};
-        for (auto &c : comps) {
-            p.push_back(c.id);
-            p.push_back((uint8_t)((c.h << 4) | c.v));
-            p.push_back(c.tq);
+                                  (uint8_t)f.width, (uint8_t)nc};
+        for (size_t i = 0; i < nc; i++) {
+            p.push_back(comps[i].id);
+            p.push_back((uint8_t)((comps[i].h << 4) | comps[i].v));
+            p.push_back(comps[i].tq);
         }
         segment(out, 0xc0, p);
     }
@@ -280,45 +286,59 @@ EncodeResult encode_jpeg(const FrameIn &f, const JpegEncodeOptions &opt) {
     }
     if (opt.restart_interval) segment(out, 0xdd, {(uint8_t)(opt.restart_interval >> 8), (uint8_t)opt.restart_interval});
     {  // SOS (encoder.rs:327-335)
-        std::vector<uint8_t> p = {(uint8_t)comps.size()};
-        for (auto &c : comps) {
-            p.push_back(c.id);
-            uint8_t tbl = opt.annex_k ? c.tq : 0;
-            p.push_back((uint8_t)((tbl << 4) | tbl));
+        std::vector<uint8_t> p = {(uint8_t)nc};
+        for (size_t i = 0; i < nc; i++) {
+            p.push_back(comps[i].id);
+            p.push_back((uint8_t)((P.comp_table[i] << 4) | P.comp_table[i]));
         }
         p.push_back(0);
         p.push_back(63);
         p.push_back(0);
         segment(out, 0xda, p);
     }
+    return true;
+}
+
+EncodeResult encode_jpeg(const FrameIn &f, const JpegEncodeOptions &opt) {
+    EncodeResult r;
+    JpegEncodePlan P;
+    if (!plan_jpeg_encode(f, opt, &P)) {
+        r.status = P.status;
+        r.message = P.message;
+        return r;
+    }
+    auto fail = [&](int32_t st, const char *m) {
+        r.status = st;
+        r.message = m;
+        r.data.clear();
+        return r;
+    };
+    std::vector<uint8_t> &out = r.data;
+    out = P.header;
     // encode_scan (encoder.rs:346-390)
-    size_t mcu_w = (size_t)hmax * 8, mcu_h = (size_t)vmax * 8;
-    size_t mcu_cols = (f.width + mcu_w - 1) / mcu_w, mcu_rows = (f.height + mcu_h - 1) / mcu_h;
-    std::vector<int32_t> pred(comps.size(), 0);
+    std::vector<int32_t> pred(P.ncomp, 0);
     Writer w;
     w.data.reserve(f.width * f.height);
     uint8_t block[64];
     int32_t coef[64];
     uint32_t rst = 0;
     size_t mcu_index = 0;
-    for (size_t my = 0; my < mcu_rows; my++)
-        for (size_t mx = 0; mx < mcu_cols; mx++, mcu_index++) {
-            if (opt.restart_interval && mcu_index > 0 && mcu_index % opt.restart_interval == 0) {
+    for (size_t my = 0; my < P.mcu_rows; my++)
+        for (size_t mx = 0; mx < P.mcu_cols; mx++, mcu_index++) {
+            if (P.restart_interval && mcu_index > 0 && mcu_index % P.restart_interval == 0) {
                 w.pad();
                 w.data.push_back(0xff);
                 w.data.push_back((uint8_t)(0xd0 + (rst & 7)));
                 rst++;
                 std::fill(pred.begin(), pred.end(), 0);
             }
-            for (size_t ci = 0; ci < comps.size(); ci++) {
-                const Comp &c = comps[ci];
+            for (size_t ci = 0; ci < P.ncomp; ci++) {
                 const PlaneIn &pl = f.planes[ci];
-                const uint8_t *q = qt[c.tq];
-                uint8_t tsel = opt.annex_k ? c.tq : 0;
-                const Code *dcc = dc_codes[tsel], *acc = ac_codes[tsel];
-                for (size_t by = 0; by < c.v; by++)
-                    for (size_t bx = 0; bx < c.h; bx++) {
-                        size_t x = (mx * c.h + bx) * 8, y = (my * c.v + by) * 8;
+                const uint8_t *q = P.qt[P.comp_tq[ci]];
+                const HuffCode *dcc = P.dc[P.comp_table[ci]], *acc = P.ac[P.comp_table[ci]];
+                for (size_t by = 0; by < P.comp_v[ci]; by++)
+                    for (size_t bx = 0; bx < P.comp_h[ci]; bx++) {
+                        size_t x = (mx * P.comp_h[ci] + bx) * 8, y = (my * P.comp_v[ci] + by) * 8;
                         // read_block (encoder.rs:392-402): edge replication
                         for (size_t yy = 0; yy < 8; yy++) {
                             size_t sy = std::min(y + yy, pl.height - 1);
