@@ -673,9 +673,13 @@ int32_t GpuJpegEncoder::encode(EncodeItem *items, size_t n, const JpegEncodeOpti
                     continue;
                 }
                 uint8_t *dst = I.in.as<uint8_t>() + at;
-                if (cudaMemcpy2DAsync(dst, pl.width, pl.data, pl.stride, pl.width, pl.height, cudaMemcpyHostToDevice,
-                                      I.s) != cudaSuccess)
-                    throw std::runtime_error("GPU encoder: upload failed");
+                // contiguous planes go up as one linear copy, strided ones row by row
+                const cudaError_t e =
+                    pl.stride == pl.width
+                        ? cudaMemcpyAsync(dst, pl.data, pl.width * pl.height, cudaMemcpyHostToDevice, I.s)
+                        : cudaMemcpy2DAsync(dst, pl.width, pl.data, pl.stride, pl.width, pl.height,
+                                            cudaMemcpyHostToDevice, I.s);
+                if (e != cudaSuccess) throw std::runtime_error("GPU encoder: upload failed");
                 fr[k].plane[c] = dst;
                 fr[k].stride[c] = pl.width;
                 at += (pl.width * pl.height + 255) / 256 * 256;
