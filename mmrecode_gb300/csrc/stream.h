@@ -48,8 +48,10 @@ bool jpeg_frame_extent(const uint8_t *in, size_t len, const uint64_t *cand, size
                        size_t *consumed, int32_t *status, std::string *message);
 
 // The 8-bit Y4M stream header of a frame (Y4mWriter::write_frame, lib.rs:
-// 246-260), or the writer's error for formats it cannot represent.
-bool y4m_header(uint32_t format, uint32_t range, bool interlaced_bottom_first, size_t width, size_t height,
+// 246-260): interlace 'b' (bottom field first, the DV decoder's frames) or 'p'
+// (progressive, the MJPEG decoder's), or the writer's error for formats it cannot
+// represent.
+bool y4m_header(uint32_t format, uint32_t range, bool bottom_first, size_t width, size_t height,
                 std::string *header, int32_t *status, std::string *message);
 
 struct StreamResult {
