@@ -78,3 +78,19 @@ def test_dv_248_mode_round_trip():
     y0 = np.frombuffer(r.frame.planes[0][2], np.uint8).astype(int)
     y1 = np.frombuffer(d.frame.planes[0][2], np.uint8).astype(int)
     assert ((y0 - y1) ** 2).mean() < 2.0
+
+
+def test_gpu_encode_bound_covers_worst_case_outputs():
+    # mmr_gpu_jpeg_encode_bound is host code: every frame the encoder can produce fits.
+    lib = m._lib.load()
+    rng = np.random.default_rng(3)
+    cases = [(m.GRAY8, 1, 1, 1), (m.YUV420P8, 2, 2, 3), (m.YUV422P8, 2, 1, 3), (m.YUV444P8, 1, 1, 3)]
+    for fmt, sx, sy, n in cases:
+        for w, h in [(1, 1), (9, 7), (64, 48), (123, 77)]:
+            cw, ch = (w + sx - 1) // sx, (h + sy - 1) // sy
+            dims = [(w, h)] + [(cw, ch)] * (n - 1)
+            planes = [m.Plane(rng.integers(0, 256, (ph, pw), dtype=np.uint8).tobytes(), pw, pw, ph) for pw, ph in dims]
+            frame = m.VideoFrame(fmt, w, h, planes, m.RANGE_FULL)
+            for annex, ri in [(False, 0), (True, 1), (True, 3)]:
+                data = m.encode_jpeg(frame, 100, annex, ri)  # q100 noise: the largest coefficients
+                assert len(data) <= lib.mmr_gpu_jpeg_encode_bound(fmt, w, h, ri)
