@@ -564,6 +564,9 @@ GpuJpegEncoder::GpuJpegEncoder(int device) : impl_(new Impl) {
     impl_->device = device;
     if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&impl_->s, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&impl_->ev0) != cudaSuccess || cudaEventCreate(&impl_->ev1) != cudaSuccess) {
+        if (impl_->ev0) cudaEventDestroy(impl_->ev0);
+        if (impl_->ev1) cudaEventDestroy(impl_->ev1);
+        if (impl_->s) cudaStreamDestroy(impl_->s);
         cudaGetLastError();
         delete impl_;
         throw std::runtime_error("GPU encoder: cannot create its stream");

@@ -203,8 +203,16 @@ Stream::Stream(EnginePool &pool, const uint8_t *data, size_t len, const std::str
         if (s_) cudaStreamDestroy(s_);
         throw std::runtime_error("cannot allocate the stream on the device");
     }
-    if (kind_ == kStreamDv) frame_dv();
-    else frame_mjpeg();
+    try {
+        if (kind_ == kStreamDv) frame_dv();
+        else frame_mjpeg();
+    } catch (...) {  // a constructor that throws runs no destructor: free the device copy here
+        cudaStreamSynchronize(s_);
+        cudaStreamDestroy(s_);
+        cudaFree(dev_);
+        cudaGetLastError();
+        throw;
+    }
     // Y4M layout: the first frame's header, then "FRAME\n" and the planes of each
     const size_t nf = frames_.size();
     planar_.resize(nf);
