@@ -192,33 +192,37 @@ __global__ void __launch_bounds__(256) fdct_kernel(EncLaunch L) {
         }
     }
     __syncthreads();
-    if (!valid) return;
-    const int u = r;  // column pass: this thread's column
-    const uint8_t *qt = L.qt + tq * 64;
-    const float *rq = L.rq + tq * 64;
-    int16_t *out = L.coef + blk * 64;  // zigzag order
+    __shared__ __align__(16) int16_t s_out[kEncBlocksPerCta][64];  // the block in zigzag order
+    if (valid) {
+        const int u = r;  // column pass: this thread's column
+        const uint8_t *qt = L.qt + tq * 64;
+        const float *rq = L.rq + tq * 64;
 #pragma unroll
-    for (int v = 0; v < 8; v++) {
-        float acc = 0.0f, mag = 0.0f;
+        for (int v = 0; v < 8; v++) {
+            float acc = 0.0f, mag = 0.0f;
 #pragma unroll
-        for (int y = 0; y < 8; y++) {
-            acc = fmaf(c_m32[y * 8 + v], s_row[lb][y][u], acc);
-            mag = fmaf(fabsf(c_m32[y * 8 + v]), s_mag[lb][y][u], mag);
+            for (int y = 0; y < 8; y++) {
+                acc = fmaf(c_m32[y * 8 + v], s_row[lb][y][u], acc);
+                mag = fmaf(fabsf(c_m32[y * 8 + v]), s_mag[lb][y][u], mag);
+            }
+            const int q = qt[v * 8 + u];
+            const float r_q = rq[v * 8 + u];
+            const float quot = acc * r_q;
+            const float a = fabsf(quot);
+            int k;
+            if (fabsf(a - floorf(a) - 0.5f) < tie_guard(mag * (1.0f + 1.0f / 1048576.0f), r_q, a)) {
+                k = exact_coefficient(s_raw[lb], u, v, q);
+                atomicAdd(L.exact, 1ull);
+            } else {
+                k = (int)rintf(quot);
+            }
+            if (v | u) k = min(max(k, -1023), 1023);  // encode_scan (encoder.rs:372-374)
+            s_out[lb][L.nat2zz[v * 8 + u]] = (int16_t)k;
         }
-        const int q = qt[v * 8 + u];
-        const float r_q = rq[v * 8 + u];
-        const float quot = acc * r_q;
-        const float a = fabsf(quot);
-        int k;
-        if (fabsf(a - floorf(a) - 0.5f) < tie_guard(mag * (1.0f + 1.0f / 1048576.0f), r_q, a)) {
-            k = exact_coefficient(s_raw[lb], u, v, q);
-            atomicAdd(L.exact, 1ull);
-        } else {
-            k = (int)rintf(quot);
-        }
-        if (v | u) k = min(max(k, -1023), 1023);  // encode_scan (encoder.rs:372-374)
-        out[L.nat2zz[v * 8 + u]] = (int16_t)k;
     }
+    __syncthreads();
+    if (valid)  // 16 bytes per thread: the block's 128 bytes in one coalesced row
+        reinterpret_cast<uint4 *>(L.coef + blk * 64)[r] = reinterpret_cast<const uint4 *>(s_out[lb])[r];
 }
 
 // ------------------------------------------------------------- Huffman ---
