@@ -58,6 +58,20 @@ class _JpegInfo(ctypes.Structure):
     ]
 
 
+class _JpegLayout(ctypes.Structure):
+    _fields_ = [
+        ("width", ctypes.c_uint32),
+        ("height", ctypes.c_uint32),
+        ("ncomp", ctypes.c_uint32),
+        ("h", ctypes.c_uint8 * 3),
+        ("v", ctypes.c_uint8 * 3),
+        ("tq", ctypes.c_uint8 * 3),
+        ("annex_k", ctypes.c_uint8),
+        ("restart_interval", ctypes.c_uint16),
+        ("qt", (ctypes.c_uint8 * 64) * 2),
+    ]
+
+
 class _Concealed(ctypes.Structure):
     _fields_ = [("sequence", ctypes.c_size_t), ("slot", ctypes.c_size_t)]
 
@@ -111,6 +125,14 @@ def lib():
         L.orc_dv_idct248.argtypes = [ctypes.POINTER(ctypes.c_int32), u8p]
         L.orc_dv_cos.argtypes = [ctypes.c_int]
         L.orc_dv_cos.restype = ctypes.c_double
+        vp = ctypes.c_void_p
+        for name in ("orc_jpeg_idct_many", "orc_dv_idct88_many", "orc_dv_idct248_many"):
+            getattr(L, name).argtypes = [vp, ctypes.c_size_t, vp]
+        L.orc_jpeg_fdct_quantize_many.argtypes = [vp, vp, ctypes.c_size_t, vp]
+        L.orc_jpeg_write_levels.argtypes = [ctypes.POINTER(_JpegLayout), vp, ctypes.c_size_t, vp, ctypes.c_size_t,
+                                            ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(_Result)]
+        L.orc_jpeg_encode.argtypes = [ctypes.POINTER(_Frame), ctypes.c_int, ctypes.c_int, ctypes.c_int, vp,
+                                      ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(_Result)]
         _lib = L
     return _lib
 
@@ -230,3 +252,91 @@ def dv_idct248(coefficients) -> bytes:
 
 def dv_cos(k: int) -> float:
     return lib().orc_dv_cos(k)
+
+
+# ------------------------------------------------------------ many blocks ---
+
+def _blocks(fn, coefficients):
+    """coefficients: int32 array (n, 64) -> uint8 array (n, 64)."""
+    import numpy as np
+
+    c = np.ascontiguousarray(coefficients, dtype=np.int32).reshape(-1, 64)
+    out = np.empty(c.shape, dtype=np.uint8)
+    fn(c.ctypes.data, c.shape[0], out.ctypes.data)
+    return out
+
+
+def jpeg_idct_many(coefficients):
+    """transform.rs:86-109 on each row of an (n, 64) int32 array."""
+    return _blocks(lib().orc_jpeg_idct_many, coefficients)
+
+
+def dv_idct88_many(coefficients):
+    """dv decoder.rs:520-548 on each row."""
+    return _blocks(lib().orc_dv_idct88_many, coefficients)
+
+
+def dv_idct248_many(coefficients):
+    """dv decoder.rs:555-602 on each row."""
+    return _blocks(lib().orc_dv_idct248_many, coefficients)
+
+
+def fdct_quantize_many(samples, quant):
+    """transform.rs:111-134: samples uint8 (n, 64), quantisers uint8 (n, 64) -> int32 (n, 64)."""
+    import numpy as np
+
+    s = np.ascontiguousarray(samples, dtype=np.uint8).reshape(-1, 64)
+    q = np.ascontiguousarray(quant, dtype=np.uint8).reshape(-1, 64)
+    out = np.empty(s.shape, dtype=np.int32)
+    lib().orc_jpeg_fdct_quantize_many(s.ctypes.data, q.ctypes.data, s.shape[0], out.ctypes.data)
+    return out
+
+
+# ------------------------------------------------------------ encoder ---
+
+def jpeg_write_levels(width, height, sampling, tq, qt, levels, annex_k=False, restart_interval=0) -> bytes:
+    """A baseline JPEG whose quantised coefficients are `levels` (int32 (nblocks, 64),
+    natural order, DC absolute, blocks in scan order); sampling = [(h, v)] per
+    component, tq = quantisation table per component, qt = 1 or 2 tables of 64
+    (natural order). Header and scan layout as the reference encoder writes them."""
+    import numpy as np
+
+    L = _JpegLayout()
+    L.width, L.height, L.ncomp = width, height, len(sampling)
+    for c, (h, v) in enumerate(sampling):
+        L.h[c], L.v[c], L.tq[c] = h, v, tq[c]
+    for t, table in enumerate(qt):
+        for k in range(64):
+            L.qt[t][k] = int(table[k])
+    L.annex_k = 1 if annex_k else 0
+    L.restart_interval = restart_interval
+    lv = np.ascontiguousarray(levels, dtype=np.int32).reshape(-1, 64)
+    cap = 256 + lv.shape[0] * 512
+    out = (ctypes.c_uint8 * cap)()
+    n, res = ctypes.c_size_t(0), _Result()
+    st = lib().orc_jpeg_write_levels(ctypes.byref(L), lv.ctypes.data, lv.shape[0], out, cap, ctypes.byref(n),
+                                     ctypes.byref(res))
+    if st != OK:
+        raise ValueError(res.message.decode())
+    return bytes(out[:n.value])
+
+
+def jpeg_encode(fmt, width, height, planes, quality, annex_k=False, restart_interval=0) -> bytes:
+    """encode_jpeg (crates/codecs/mjpeg/src/encoder.rs:44-87) of planar 8-bit input:
+    planes = [(width, height, bytes)] with stride == width."""
+    fr = _Frame()
+    fr.format, fr.range, fr.width, fr.height, fr.plane_count = fmt, RANGE_FULL, width, height, len(planes)
+    keep = []
+    for i, (w, h, data) in enumerate(planes):
+        arr = (ctypes.c_uint8 * max(len(data), 1)).from_buffer_copy(data if data else b"\0")
+        keep.append(arr)
+        fr.planes[i].data = ctypes.cast(arr, ctypes.POINTER(ctypes.c_uint8))
+        fr.planes[i].width, fr.planes[i].height = w, h
+    cap = 4096 + 4 * sum(len(p[2]) for p in planes)
+    out = (ctypes.c_uint8 * cap)()
+    n, res = ctypes.c_size_t(0), _Result()
+    st = lib().orc_jpeg_encode(ctypes.byref(fr), quality, 1 if annex_k else 0, restart_interval, out, cap,
+                               ctypes.byref(n), ctypes.byref(res))
+    if st != OK:
+        raise ValueError(res.message.decode())
+    return bytes(out[:n.value])

@@ -474,6 +474,14 @@ void orc_dv_idct248(const int32_t c[64], uint8_t out[64]) {
             }
 }
 
+void orc_dv_idct88_many(const int32_t *coefficients, size_t n, uint8_t *out) {
+    for (size_t b = 0; b < n; b++) orc_dv_idct88(coefficients + 64 * b, out + 64 * b);
+}
+
+void orc_dv_idct248_many(const int32_t *coefficients, size_t n, uint8_t *out) {
+    for (size_t b = 0; b < n; b++) orc_dv_idct248(coefficients + 64 * b, out + 64 * b);
+}
+
 /* decoder.rs:470-505 put_block / put_split_chroma */
 static int put_block(orc_plane *pl, size_t x, size_t y, const uint8_t px[64], orc_result *res) {
     if (x + 8 > pl->width || y + 8 > pl->height) {

@@ -631,8 +631,9 @@ static const int ZIGZAG_TO_NATURAL[64] = {
     41, 34, 27, 20, 13, 6,  7,  14, 21, 28, 35, 42, 49, 56, 57, 50, 43, 36, 29, 22, 15, 23,
     30, 37, 44, 51, 58, 59, 52, 45, 38, 31, 39, 46, 53, 60, 61, 54, 47, 55, 62, 63};
 
-/* transform.rs:2-84: the reference's literal f64 matrix, decimal digits as written there. */
-static const double IDCT_MATRIX[8][8] = {
+/* transform.rs:2-84: the reference's literal f64 matrix, decimal digits as written there
+ * (also used by the encoder restatement, encode.c). */
+const double ORC_IDCT_MATRIX[8][8] = {
     {0.3535533905932738, 0.4903926402016152, 0.4619397662556434, 0.4157348061512726,
      0.3535533905932738, 0.2777851165098011, 0.1913417161825449, 0.09754516100806417},
     {0.3535533905932738, 0.4157348061512726, 0.1913417161825449, -0.0975451610080641,
@@ -666,13 +667,17 @@ void orc_jpeg_idct(const int32_t coefficients[64], uint8_t out[64]) {
     for (int v = 0; v < 8; v++)
         for (int x = 0; x < 8; x++)
             for (int u = 0; u < 8; u++)
-                temporary[v * 8 + x] += IDCT_MATRIX[x][u] * (double)coefficients[v * 8 + u];
+                temporary[v * 8 + x] += ORC_IDCT_MATRIX[x][u] * (double)coefficients[v * 8 + u];
     for (int y = 0; y < 8; y++)
         for (int x = 0; x < 8; x++) {
             double sum = 0.0;
-            for (int v = 0; v < 8; v++) sum += IDCT_MATRIX[y][v] * temporary[v * 8 + x];
+            for (int v = 0; v < 8; v++) sum += ORC_IDCT_MATRIX[y][v] * temporary[v * 8 + x];
             out[y * 8 + x] = round_clamp_u8(sum + 128.0);
         }
+}
+
+void orc_jpeg_idct_many(const int32_t *coefficients, size_t n, uint8_t *out) {
+    for (size_t b = 0; b < n; b++) orc_jpeg_idct(coefficients + 64 * b, out + 64 * b);
 }
 
 /* ------------------------------------------------------------------ */

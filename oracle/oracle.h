@@ -123,6 +123,38 @@ void orc_dv_idct248(const int32_t coefficients[64], uint8_t out[64]);
 /* The libm cos values the DV transforms use: cos(fl(k*PI)/16), k = 0..127. */
 double orc_dv_cos(int k);
 
+/* ---- MJPEG encoder side (crates/codecs/mjpeg/src/encoder.rs; encode.c) ---- */
+
+/* Layout and tables of a baseline JPEG written from chosen quantised levels. */
+typedef struct orc_jpeg_layout {
+    uint32_t width, height;
+    uint32_t ncomp;            /* 1..3; component ids 1..ncomp */
+    uint8_t h[3], v[3];        /* sampling factors */
+    uint8_t tq[3];             /* quantisation table of each component (0 or 1) */
+    uint8_t annex_k;           /* 0: the reference encoder's simple Huffman tables; 1: Annex K */
+    uint16_t restart_interval; /* MCUs per interval, 0 = no DRI */
+    uint8_t qt[2][64];         /* natural order */
+} orc_jpeg_layout;
+
+/* transform.rs:111-134 forward_dct_quantize on one block. */
+void orc_jpeg_fdct_quantize(const uint8_t samples[64], const uint8_t quantization[64], int32_t out[64]);
+void orc_jpeg_fdct_quantize_many(const uint8_t *samples, const uint8_t *quantization, size_t n, int32_t *out);
+
+int orc_jpeg_write_levels(const orc_jpeg_layout *layout, const int32_t *levels, size_t nblocks, uint8_t *out,
+                          size_t cap, size_t *len, orc_result *res);
+
+/* encode_jpeg (encoder.rs:44-87) plus the Annex K / restart options. */
+int orc_jpeg_encode(const orc_frame *frame, int quality, int annex_k, int restart_interval, uint8_t *out,
+                    size_t cap, size_t *len, orc_result *res);
+
+/* Many blocks at once (test volume): n blocks of 64, consecutive. */
+void orc_jpeg_idct_many(const int32_t *coefficients, size_t n, uint8_t *out);
+void orc_dv_idct88_many(const int32_t *coefficients, size_t n, uint8_t *out);
+void orc_dv_idct248_many(const int32_t *coefficients, size_t n, uint8_t *out);
+
+/* transform.rs:2-84, shared by jpeg.c and encode.c */
+extern const double ORC_IDCT_MATRIX[8][8];
+
 /* ---- Colour (crates/cli/src/terminal_preview.rs:7159-7236, 7308-7330) ---- */
 
 /* Interleaved RGB24 at 1:1 scale; out holds width*height*3 bytes. */
