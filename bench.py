@@ -11,6 +11,10 @@ quality 90, Annex K Huffman tables, restart interval = one MCU row (120 MCUs of
   e2e     the same through mmr_gpu_decode_batch with pinned HOST buffers: the
           packets' H2D and the RGB frames' D2H are inside every step.
   plain   one frame per mmr_gpu_decode_batch call (host buffers), the plain GPU form.
+  mjpeg_vga_420  the plain configuration: 30 frames of 640x480 4:2:0 q75 without
+          restart markers (one interval per frame: the self-synchronising chunked
+          entropy decode), planar output.
+  dv25_ntsc      1000 NTSC DV25 frames (720x480 4:1:1, 120000 bytes each), planar.
   stream_y4m  the same frames as one MJPEG file through the CLI's decode path
           (mmr_gpu_stream_*): upload, framing on the GPU, batch decode, the
           Y4M stream (planar 4:2:2) in pinned host memory.
@@ -21,8 +25,14 @@ Inputs (337 MB) and outputs (1.87 GB) per step exceed the 129 MB L2, so no L2
 flush is needed between steps.
 
 --impl reference times the reference decoder's algorithm (the C restatement in
-oracle/, the reference being Rust with no toolchain on the box) on the host
-cores, one frame per worker process, on the same workload.
+oracle/, the reference being Rust with no toolchain on the box) on all host
+cores, one frame per worker process, on the same 300-frame step; its input is
+generated by the oracle's encoder restatement (oracle/synth.py), so that arm
+never loads the product library.
+
+--profile c2|c1|dv runs one small decode batch (38 frames of the 1080p workload,
+the 30 VGA frames, or 120 DV frames) on one engine a few times and exits: the
+case ncu captures are taken on.
 """
 
 from __future__ import annotations
@@ -58,8 +68,49 @@ def _oracle_decode(packet: bytes):
     return r.status, dt, rgb
 
 
-def _oracle_decode_time(packet: bytes) -> float:
-    return _oracle_decode(packet)[1]
+def _oracle_rgb_digest(packet: bytes):
+    """Reference path of one frame (decode_jpeg + RGB24 at 1:1): status, seconds, SHA-256 of the RGB."""
+    import hashlib
+
+    import oracle
+    t = time.perf_counter()
+    r = oracle.jpeg_decode(packet)
+    rgb = oracle.rgb24(r.frame) if r.status == 0 else None
+    dt = time.perf_counter() - t
+    return r.status, dt, hashlib.sha256(rgb).hexdigest() if rgb is not None else None
+
+
+def _oracle_planar_digest(job):
+    """(codec, packet) -> status, seconds, SHA-256 of the planar frame (Y | Cb | Cr)."""
+    import hashlib
+
+    import oracle
+    codec, packet = job
+    t = time.perf_counter()
+    r = oracle.jpeg_decode(packet) if codec == "mjpeg" else oracle.dv_decode(packet)
+    dt = time.perf_counter() - t
+    if r.status != 0:
+        return r.status, dt, None
+    return 0, dt, hashlib.sha256(b"".join(p[2] for p in r.frame.planes)).hexdigest()
+
+
+def _round(x):
+    """Floats to 5 significant digits (keeps the JSON line short)."""
+    if isinstance(x, float):
+        return float(f"{x:.5g}")
+    if isinstance(x, dict):
+        return {k: _round(v) for k, v in x.items()}
+    if isinstance(x, (list, tuple)):
+        return [_round(v) for v in x]
+    return x
+
+
+def _config(world: int, in_bytes: int) -> dict:
+    """The headline workload, identical for both arms."""
+    return {"workload": WORKLOAD, "frames_per_gpu": FRAMES, "width": W, "height": H, "subsampling": SUB,
+            "quality": Q, "restart_interval_mcus": RI, "output": "rgb24", "huffman": "annex-k",
+            "compressed_bytes_per_step": in_bytes, "l2": "inputs/outputs per step exceed L2; no flush",
+            "parallelism": f"replicas x{world}"}
 
 
 def _dist():
@@ -201,36 +252,40 @@ def make_workload(rank: int):
 
 
 def reference_arm(args):
+    """The reference algorithm (oracle restatement) on every host core: each step
+    decodes and converts all 300 frames, one frame per worker process. Input comes
+    from the oracle's encoder restatement: this arm never loads the product library."""
     world, rank, _ = _dist()
     if rank != 0:
         return 0
     import oracle
+    import oracle.synth as osynth
     oracle.build()
     cores = os.cpu_count() or 1
-    packets = make_workload(0)
     ctx = mp.get_context("spawn")
     with ctx.Pool(cores) as pool:
-        def step(k):
-            sample = [packets[(k * cores + i) % FRAMES] for i in range(cores)]
+        packets = osynth.mjpeg_stream(workload_seed(0), FRAMES, W, H, SUB, Q, RI, annex_k=True, pool=pool)
+        in_bytes = sum(len(p) for p in packets)
+
+        def step():
             t = time.perf_counter()
-            pool.map(_oracle_decode_time, sample, chunksize=1)
-            return time.perf_counter() - t, len(sample)
-        for k in range(args.warmup):
-            step(k)
-        total_t, total_f = 0.0, 0
-        for k in range(args.steps):
-            dt, nf = step(args.warmup + k)
-            total_t += dt
-            total_f += nf
-    fps = total_f / total_t
+            res = pool.map(_oracle_rgb_digest, packets, chunksize=1)
+            assert all(r[0] == 0 for r in res)
+            return time.perf_counter() - t
+        for _ in range(args.warmup):
+            step()
+        total_t = 0.0
+        for _ in range(args.steps):
+            total_t += step()
+    fps = FRAMES * args.steps / total_t
     line = {
         "impl": "reference", "metric": METRIC, "value": fps, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000 * total_t / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "u8/i32/f64", "data": "synthetic (seeded)",
-        "config": {"workload": WORKLOAD, "frames_per_step": cores, "width": W, "height": H, "subsampling": SUB,
-                   "quality": Q, "restart_interval_mcus": RI, "output": "rgb24"},
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8/i32/f64", "data": "synthetic (seeded gradients+rectangles+noise)",
+        "config": _config(world, in_bytes),
         "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": cores, "kind": "port", "cpu": _cpu_model(),
-                         "sample": f"{cores} frames per step of the {FRAMES}-frame workload, one per process"},
+                         "sample": f"every step decodes all {FRAMES} frames (decode + RGB24), one frame per process "
+                                   f"on {cores} processes; input from the oracle encoder"},
         "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -554,6 +609,224 @@ def mixed_sweep(local: int, steps: int = 5, warmup: int = 3):
             "all_ok": ok, "tuned": [brief(t) for t in tuned]}
 
 
+VGA_SEED = 20261201
+VGA_FRAMES, VGA_W, VGA_H = 30, 640, 480
+DV_SEED = 20261204
+DV_FRAMES = 1000
+
+
+def _device_items(m, _lib, torch, local, packets, codec, output, out_bytes):
+    """Packets resident in HBM, one output slot per frame in HBM: (items, keep-alive)."""
+    import ctypes
+
+    offs, o = [], 0
+    for p in packets:
+        offs.append(o)
+        o += (len(p) + 255) // 256 * 256
+    host_in = torch.empty(o, dtype=torch.uint8, pin_memory=True)
+    hv = host_in.numpy()
+    for p, off in zip(packets, offs):
+        hv[off:off + len(p)] = np.frombuffer(p, np.uint8)
+    dev_in = host_in.to(f"cuda:{local}")
+    slot = (max(out_bytes) + 255) // 256 * 256
+    dev_out = torch.empty(len(packets) * slot, dtype=torch.uint8, device=f"cuda:{local}")
+    host_out = torch.empty(len(packets) * slot, dtype=torch.uint8, pin_memory=True)
+
+    def items(device_resident: bool):
+        arr = (_lib.GpuItem * len(packets))()
+        for i, p in enumerate(packets):
+            it = arr[i]
+            it.struct_size = ctypes.sizeof(_lib.GpuItem)
+            it.data = host_in.data_ptr() + offs[i]
+            it.device_data = dev_in.data_ptr() + offs[i] if device_resident else None
+            it.len = len(p)
+            it.codec = codec
+            it.output = output
+            it.flags = m.ITEM_OUT_DEVICE if device_resident else 0
+            it.out = (dev_out.data_ptr() if device_resident else host_out.data_ptr()) + i * slot
+            it.out_capacity = out_bytes[i]
+        return arr
+    return items, (host_in, dev_in, dev_out, host_out), slot
+
+
+def _timed(ctx, arr, steps, warmup):
+    import torch
+
+    for _ in range(warmup):
+        ctx.decode_raw(arr)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    launches = 0
+    for _ in range(steps):
+        ctx.decode_raw(arr)
+        launches += ctx.last_batch_launches
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    for i in range(len(arr)):
+        assert arr[i].status == 0, arr[i].message
+    return dt, launches
+
+
+def _gpu_digests(dev_out, slot, sizes):
+    import hashlib
+
+    host = dev_out.cpu().numpy()
+    return [hashlib.sha256(host[i * slot:i * slot + n].tobytes()).hexdigest() for i, n in enumerate(sizes)]
+
+
+def _cpu_leg(pool, jobs, cores, single_seconds):
+    """Oracle time on one core (a bounded sample) and on all cores (every frame), with digests."""
+    single_t, k = 0.0, 0
+    while single_t < single_seconds and k < len(jobs):
+        single_t += _oracle_planar_digest(jobs[k])[1]
+        k += 1
+    t = time.perf_counter()
+    res = pool.map(_oracle_planar_digest, jobs, chunksize=max(1, len(jobs) // (4 * cores)))
+    multi_t = time.perf_counter() - t
+    return res, {"value": len(jobs) / multi_t, "unit": "frames/s", "cores": cores, "kind": "port",
+                 "cpu": _cpu_model(), "single_core_frames_per_s": k / single_t,
+                 "sample": f"{k} frames on 1 core, then all {len(jobs)} frames on {cores} processes "
+                           f"(oracle restating the reference decoder)"}
+
+
+def small_legs(args, local, pool, cores, m, _lib, peak, peak_kind, figures):
+    """Configuration 1 (30 VGA 4:2:0 q75 frames without restart markers, planar) and
+    configuration 3 (1000 NTSC DV25 frames, planar): frames/s device-resident and
+    through host buffers, the plain one-frame-per-call form, stage times on one
+    engine, rooflines, the oracle on one and on all cores, and every frame's
+    samples against the oracle (SHA-256 per frame)."""
+    import ctypes
+
+    import torch
+
+    from mmrecode_gb300 import synth
+
+    out = {}
+    ctx1 = m.Context(local, engines=1)
+    ctx = m.Context(local)
+    for name in ("mjpeg_vga_420", "dv25_ntsc"):
+        if name == "mjpeg_vga_420":
+            if not args.c1:
+                continue
+            packets = synth.mjpeg_stream(VGA_SEED, VGA_FRAMES, VGA_W, VGA_H, "420", 75, 0)
+            codec, label = m.CODEC_MJPEG, "mjpeg"
+            sizes = [VGA_W * VGA_H + 2 * (VGA_W // 2) * (VGA_H // 2)] * len(packets)
+            workload = "c1-30-mjpeg-640x480-420-q75-annexk-no-restart-planar"
+        else:
+            if not args.dv:
+                continue
+            packets = synth.dv_stream(DV_SEED, DV_FRAMES)
+            codec, label = m.CODEC_DV, "dv"
+            sizes = [720 * 480 + 2 * 180 * 480] * len(packets)
+            workload = "c3-1000-dv25-ntsc-720x480-411-planar"
+        n = len(packets)
+        in_bytes = sum(len(p) for p in packets)
+        items, keep, slot = _device_items(m, _lib, torch, local, packets, codec, m.OUTPUT_PLANAR, sizes)
+        resident, hostbuf = items(True), items(False)
+        steps = max(args.steps, 10)
+        dt, launches = _timed(ctx, resident, steps, max(args.warmup, 3))
+        edt, _ = _timed(ctx, hostbuf, steps, 3)
+        # stage times on one engine (nothing overlapping)
+        stage = []
+        for _ in range(5):
+            ctx1.decode_raw(resident)
+            stage.append(ctx1.stats())
+        stage = stage[2:]
+        avg = lambda k: sum(x[k] for x in stage) / len(stage)
+        # the plain form: one frame per call from host buffers
+        lat = []
+        for i in range(min(n, 60) + 3):
+            one = (_lib.GpuItem * 1)()
+            ctypes.memmove(ctypes.addressof(one), ctypes.addressof(hostbuf[i % n]), ctypes.sizeof(_lib.GpuItem))
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            ctx1.decode_raw(one)
+            lat.append(time.perf_counter() - t)
+            assert one[0].status == 0
+        lat = sorted(1000 * x for x in lat[3:])
+        leg = {"workload": workload, "frames_per_step": n, "compressed_bytes_per_step": in_bytes,
+               "value": n * steps / dt, "unit": "frames/s", "ms_per_step": 1000 * dt / steps,
+               "gpu_launches_per_step": launches // steps,
+               "e2e": {"value": n * steps / edt, "unit": "frames/s", "h2d_bytes_per_step": in_bytes,
+                       "d2h_bytes_per_step": sum(sizes)},
+               "plain_gpu": {"value": len(lat) / (sum(lat) / 1000), "unit": "frames/s",
+                             "p50_ms": lat[len(lat) // 2], "p99_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))]}}
+        if label == "mjpeg":
+            blocks = stage[-1]["jpeg_blocks"]
+            st = {k: avg(k + "_ms") for k in ("scan", "entropy", "idct", "slice_spec", "slice_sync", "slice_decode")}
+            ent_bytes = in_bytes + blocks * 130
+            achieved = ent_bytes / (st["entropy"] / 1e3) / 1e9
+            leg["stage_ms"] = st
+            leg["roofline"] = {"bound": "issue", "kernel": "slice_spec_kernel+slice_sync+slice_decode (entropy stage)",
+                               "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+                               "frac": achieved / peak, "algorithmic_bytes_per_launch": ent_bytes,
+                               "ms_per_launch": st["entropy"],
+                               "issue_active_pct_ncu": figures.get(("issue_active_pct", "slice_spec_kernel@c1"))}
+        else:
+            blocks = stage[-1]["dv_blocks"]
+            st = {"dv_segment": avg("dv_segment_ms"), "dv_idct": avg("dv_idct_ms")}
+            seg_bytes = in_bytes + blocks * 128
+            idct_bytes = blocks * 128 + sum(sizes)
+            leg["stage_ms"] = st
+            leg["roofline"] = {"bound": "hbm", "kernel": "dv_idct_kernel",
+                               "achieved": idct_bytes / (st["dv_idct"] / 1e3) / 1e9, "peak": peak,
+                               "peak_kind": peak_kind, "unit": "GB/s",
+                               "frac": idct_bytes / (st["dv_idct"] / 1e3) / 1e9 / peak,
+                               "algorithmic_bytes_per_launch": idct_bytes, "ms_per_launch": st["dv_idct"],
+                               "issue_active_pct_ncu": figures.get(("issue_active_pct", "dv_idct_kernel"))}
+            leg["roofline_segment"] = {"bound": "issue", "kernel": "segment_kernel",
+                                       "achieved": seg_bytes / (st["dv_segment"] / 1e3) / 1e9, "peak": peak,
+                                       "peak_kind": peak_kind, "unit": "GB/s",
+                                       "frac": seg_bytes / (st["dv_segment"] / 1e3) / 1e9 / peak,
+                                       "algorithmic_bytes_per_launch": seg_bytes, "ms_per_launch": st["dv_segment"],
+                                       "issue_active_pct_ncu": figures.get(("issue_active_pct", "segment_kernel"))}
+        if pool is not None:
+            ctx.decode_raw(resident)
+            torch.cuda.synchronize()
+            gpu = _gpu_digests(keep[2], slot, sizes)
+            res, cpu = _cpu_leg(pool, [(label, p) for p in packets], cores, args.cpu_seconds / 6)
+            leg["cpu_baseline"] = cpu
+            leg["bit_exact_frames"] = sum(1 for (st_, _, d), g in zip(res, gpu) if st_ == 0 and d == g)
+            leg["bit_exact"] = leg["bit_exact_frames"] == n
+        out[name] = leg
+        del keep
+    ctx.close()
+    ctx1.close()
+    return out
+
+
+def profile_mode(args):
+    """A small decode batch on one engine, a few times (what ncu captures)."""
+    import torch
+
+    import __graft_entry__
+    __graft_entry__.build()
+    import mmrecode_gb300 as m
+    from mmrecode_gb300 import _lib, synth
+
+    torch.cuda.set_device(0)
+    if args.profile == "c2":
+        packets = synth.mjpeg_stream(SEED, 38, W, H, SUB, Q, RI)
+        codec, output, sizes = m.CODEC_MJPEG, m.OUTPUT_RGB24, [W * H * 3] * 38
+    elif args.profile == "c1":
+        packets = synth.mjpeg_stream(VGA_SEED, VGA_FRAMES, VGA_W, VGA_H, "420", 75, 0)
+        codec, output, sizes = m.CODEC_MJPEG, m.OUTPUT_PLANAR, [VGA_W * VGA_H * 3 // 2] * VGA_FRAMES
+    else:
+        packets = synth.dv_stream(DV_SEED, 120)
+        codec, output, sizes = m.CODEC_DV, m.OUTPUT_PLANAR, [720 * 480 + 2 * 180 * 480] * 120
+    items, keep, _ = _device_items(m, _lib, torch, 0, packets, codec, output, sizes)
+    arr = items(True)
+    ctx = m.Context(0, engines=1)
+    ctx.set_graphs(False)
+    for _ in range(max(args.steps, 1)):
+        ctx.decode_raw(arr)
+    torch.cuda.synchronize()
+    assert all(arr[i].status == 0 for i in range(len(arr)))
+    print(json.dumps({"profile": args.profile, "frames": len(packets), "stats": ctx.stats()}))
+    ctx.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -572,9 +845,17 @@ def main():
     ap.add_argument("--graphs", type=int, default=1,
                     help="replay repeated batches as CUDA graphs (0: direct launches, e.g. under ncu, which "
                          "crashed the process while several engine threads captured graphs)")
+    ap.add_argument("--c1", type=int, default=1, help="the 30-frame VGA 4:2:0 plain configuration (0: skip)")
+    ap.add_argument("--dv", type=int, default=1, help="the 1000-frame NTSC DV25 configuration (0: skip)")
+    ap.add_argument("--profile", choices=["c2", "c1", "dv"], default=None,
+                    help="decode one small batch on one engine --steps times and exit (for ncu captures)")
+    ap.add_argument("--detail-out", default=None,
+                    help="also write the full record (autotune tables, per-level serving figures) to this file")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
+    if args.profile:
+        return profile_mode(args)
 
     world, rank, local = _dist()
     cores = os.cpu_count() or 1
@@ -721,7 +1002,7 @@ def main():
         tpb = figures.get(("traffic_bytes_per_block", name))
         out = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "peak_kind": peak_kind,
                "unit": "GB/s", "frac": achieved / peak, "traffic": tpb * blocks if tpb else None,
-               "algorithmic_bytes_per_launch": nbytes, "ms_per_launch": ms}
+               "algorithmic_bytes": nbytes, "ms": ms}
         issue = figures.get(("issue_active_pct", name))
         if issue is not None:
             out["issue_active_pct_ncu"] = issue
@@ -779,64 +1060,85 @@ def main():
         served80 = next((lv for lv in serving["levels"] if lv["load"] == 0.8), None)
 
     cpu = None
-    bit_exact = None
+    bit_exact, bit_exact_frames = None, None
     if pool is not None:
-        # oracle sample: single core, then all cores; also checks the GPU output of those frames
-        single_t, sample = 0.0, []
-        while single_t < args.cpu_seconds / 3 and len(sample) < n:
-            st, t1, rgb = _oracle_decode(packets[len(sample)])
-            single_t += t1
-            sample.append((st, rgb))
-        k = min(n, cores)
-        t = time.perf_counter()
-        res = pool.map(_oracle_decode, packets[:k], chunksize=1)
-        multi_t = time.perf_counter() - t
-        pool.close()
+        # the oracle on one core (bounded sample), then every frame on all cores; every
+        # frame's RGB is checked against the GPU output (SHA-256 per frame)
+        import hashlib
+        single_t, k = 0.0, 0
+        while single_t < args.cpu_seconds / 3 and k < n:
+            single_t += _oracle_rgb_digest(packets[k])[1]
+            k += 1
+        run(resident, 1, 0)
         gpu_rgb = dev_out.cpu().numpy()
-        bit_exact = True
-        for i, (st, t1, rgb) in enumerate(res):
-            bit_exact &= st == 0 and gpu_rgb[i * rgb_bytes:(i + 1) * rgb_bytes].tobytes() == rgb
-        cpu = {"value": k / multi_t, "unit": "frames/s", "cores": cores, "kind": "port", "cpu": _cpu_model(),
-               "single_core_frames_per_s": len(sample) / single_t,
-               "sample": f"{len(sample)} frames on 1 core, then {k} frames on {cores} processes, "
+        t = time.perf_counter()
+        res = pool.map(_oracle_rgb_digest, packets, chunksize=1)
+        multi_t = time.perf_counter() - t
+        bit_exact_frames = sum(1 for i, (st, _, d) in enumerate(res)
+                               if st == 0 and d == hashlib.sha256(gpu_rgb[i * rgb_bytes:(i + 1) * rgb_bytes]).hexdigest())
+        bit_exact = bit_exact_frames == n
+        cpu = {"value": n / multi_t, "unit": "frames/s", "cores": cores, "kind": "port", "cpu": _cpu_model(),
+               "single_core_frames_per_s": k / single_t,
+               "sample": f"{k} frames on 1 core, then all {n} frames on {cores} processes, "
                          f"of the same 1080p 4:2:2 q90 workload (oracle restating the reference decoder)"}
+    small = small_legs(args, local, pool, cores, m, _lib, peak, peak_kind, figures) if rank == 0 else {}
+    if pool is not None:
+        pool.close()
 
     if rank == 0:
+        detail = {"serving": serving, "mixed_autotuned_graphs": mixed, "stream_y4m": stream, "encode_gpu": encode,
+                  "stage_ms": stage_times, "idct_exact_sample_fraction": exact_frac, **small}
+        if args.detail_out:
+            with open(args.detail_out, "w") as f:
+                json.dump(detail, f, indent=1)
+
+        def brief_leg(leg):
+            if not leg:
+                return None
+            keep = {k: leg.get(k) for k in ("value", "ms_per_step", "bit_exact_frames", "frames_per_step")}
+            keep["e2e"] = leg["e2e"]["value"]
+            keep["plain"] = leg["plain_gpu"]["value"]
+            keep["stage_ms"] = leg["stage_ms"]
+            keep["roofline_frac"] = leg["roofline"]["frac"]
+            keep["cpu_all_cores"] = (leg.get("cpu_baseline") or {}).get("value")
+            return keep
+
         line = {
             "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u8/i32/f64", "data": "synthetic (seeded gradients+rectangles+noise)",
-            "config": {"workload": WORKLOAD, "frames_per_gpu": n, "width": W, "height": H, "subsampling": SUB,
-                       "quality": Q, "restart_interval_mcus": RI, "output": "rgb24", "huffman": "annex-k",
-                       "compressed_bytes_per_step": in_bytes, "l2": "inputs/outputs per step exceed L2; no flush",
-                       "parallelism": f"replicas x{world}"},
-            "e2e": {"value": e2e, "unit": "frames/s", "h2d_bytes_per_step": in_bytes,
-                    "d2h_bytes_per_step": n * rgb_bytes,
-                    # the link alone: copy-engine bandwidths of this run and the frame rate
-                    # the device-to-host copy of the outputs caps e2e at
-                    "link_d2h_GBps": d2h_gbs, "link_h2d_GBps": h2d_gbs,
-                    "link_cap_frames_per_s": d2h_gbs * 1e9 / rgb_bytes},
+            "config": _config(world, in_bytes),
             "compressed_MBps": value * in_bytes / n / 1e6,
-            "plain_gpu": {"value": plain_fps, "unit": "frames/s", "p50_ms": pct(lat_ms, 0.5), "p99_ms": pct(lat_ms, 0.99),
-                          "frames": len(lat)},
-            "batched_over_plain": value / plain_fps,
-            "latency_ms": {"batched_p50": ms_per_step, "batched_p99": ms_per_step,
-                           "served_p50_at_80pct": served80["p50_ms"] if served80 else None,
-                           "served_p99_at_80pct": served80["p99_ms"] if served80 else None},
-            "serving": serving,
-            "mixed_autotuned_graphs": mixed,
-            "stream_y4m": stream,
-            "encode_gpu": encode,
-            "stage_ms": stage_times,
-            "idct_exact_sample_fraction": exact_frac,
+            "stage_ms": {k: stage_times[k] for k in ("scan", "slice_spec", "slice_sync", "slice_decode", "idct")},
             "roofline": roofline,
             "roofline_transform_colour": roofline_transform,
             "cpu_baseline": cpu,
-            "bit_exact_sample": bit_exact,
+            "stream_y4m": stream and {"value": stream["value"], "framing_frac": stream["framing"]["roofline"]["frac"]},
+            "encode_gpu": encode and {"value": encode["value"], "e2e": encode["e2e"]["value"],
+                                      "bit_exact_sample": encode["bit_exact_sample"]},
+            "mixed_c4": mixed and {"value": mixed["fps"], "ms_per_step": mixed["ms_per_step"], "all_ok": mixed["all_ok"],
+                                   "classes_tuned": len(mixed["tuned"])},
+            "mjpeg_vga_420_c1": brief_leg(small.get("mjpeg_vga_420")),
+            "dv25_ntsc_c3": brief_leg(small.get("dv25_ntsc")),
+            "serving_c5": serving and {"peak_fps": serving["peak_fps_closed_loop"],
+                                       "p50_p99_ms_by_load": {str(lv["load"]): [lv["p50_ms"], lv["p99_ms"]]
+                                                              for lv in serving["levels"]},
+                                       "failed": serving["failed_requests"]},
+            "plain_gpu": {"value": plain_fps, "unit": "frames/s", "p50_ms": pct(lat_ms, 0.5), "p99_ms": pct(lat_ms, 0.99),
+                          "frames": len(lat)},
+            "batched_over_plain": value / plain_fps,
+            "latency_ms": {"batched_step": ms_per_step,
+                           "served_p50_at_80pct": served80["p50_ms"] if served80 else None,
+                           "served_p99_at_80pct": served80["p99_ms"] if served80 else None},
+            "e2e": {"value": e2e, "unit": "frames/s", "h2d_bytes_per_step": in_bytes,
+                    "d2h_bytes_per_step": n * rgb_bytes,
+                    # the link alone: the frame rate the device-to-host copy of the outputs caps e2e at
+                    "link_d2h_GBps": d2h_gbs, "link_cap_frames_per_s": d2h_gbs * 1e9 / rgb_bytes},
+            "bit_exact": bit_exact, "bit_exact_frames": bit_exact_frames,
             "gpu_launches": launches,
             "clocks": clocks,
         }
-        print(json.dumps(line))
+        print(json.dumps(_round(line), separators=(",", ":")))
     ctx.close()
     return 0
 

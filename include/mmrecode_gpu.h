@@ -121,6 +121,8 @@ typedef struct mmr_gpu_batch_stats {
     /* slices of the chunked entropy decoder, and those whose levels the final decode
        pass redid instead of taking the speculative decode's */
     uint64_t slices, slices_redone;
+    /* inside dv_ms: DIF identifier check + segment (VLC) decode, then transform + placement */
+    double dv_segment_ms, dv_idct_ms;
 } mmr_gpu_batch_stats;
 
 /*
@@ -246,6 +248,11 @@ MMR_API mmr_status mmr_dv_encode_ex(const mmr_video_frame_view *frame, uint32_t 
  * device address and writes a lookup table into it), so make that first call
  * before any stream capture. All calls share the array: calls that overlap on
  * the GPU (several threads decoding on the same device) race, so serialise them.
+ * The work runs on the calling thread's per-thread default stream
+ * (cudaStreamPerThread), so it does not wait for, or hold back, the
+ * application's other streams; the call returns when its output is in `out`.
+ * After a device reset (cudaDeviceReset) the next call notices that the lookup
+ * table is gone and sets the device up again.
  * info->struct_size must be sizeof(mmr_gpu_frame_info); the call fills *info.
  */
 MMR_API mmr_status mmr_dv_decode_static(const uint8_t *data, size_t len, uint8_t *out, size_t out_capacity,

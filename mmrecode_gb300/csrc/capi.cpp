@@ -584,6 +584,8 @@ MMR_API mmr_status mmr_gpu_last_batch_stats(const mmr_gpu_context *context, mmr_
     stats->graph_replays = t.graph_replays;
     stats->slices = t.slices;
     stats->slices_redone = t.slices_redone;
+    stats->dv_segment_ms = t.dv_segment_ms;
+    stats->dv_idct_ms = t.dv_idct_ms;
     return finish(MMR_STATUS_OK, "");
 }
 

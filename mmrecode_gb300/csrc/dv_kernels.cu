@@ -13,6 +13,7 @@
 //              (decoder.rs:520-602); then placement (decoder.rs:395-505).
 #include <cuda_runtime.h>
 
+#include "dv_idct_core.h"
 #include "kernels.h"
 #include "rounding.h"
 #include "tables.h"
@@ -25,9 +26,6 @@ __constant__ uint8_t c_dv_shifts[88] = MMR_DV_QUANT_SHIFTS_INIT;
 __constant__ int c_dv_qoff[4] = MMR_DV_QUANT_OFFSET_INIT;
 __constant__ int32_t c_dv_w88[64] = MMR_DV_IWEIGHT_88_INIT;
 __constant__ int32_t c_dv_w248[64] = MMR_DV_IWEIGHT_248_INIT;
-__constant__ double c_cos16[128] = {
-#include "cos_table.inc"
-};
 
 namespace {
 
@@ -321,64 +319,8 @@ __device__ __forceinline__ void mb_coords(bool pal, uint32_t seqs, uint32_t sequ
 
 constexpr int kIdctThreads = 256;  // 4 blocks x 64 samples
 
-__constant__ float c_cos16f[128] = {
-#include "cos_table.inc"
-};
-
-constexpr double kFrac = 0.7071067811865476;  // FRAC_1_SQRT_2
-
-// The reference's binary64 8-8 direct sum for sample (y, x) (decoder.rs:520-548):
-// terms ((((cu*cv)*c)*cos_u)*cos_v) accumulated in (v, u) order, then / 4.0. Zero
-// coefficients are skipped: their term is +-0.0, which leaves any sum that is not
-// -0.0 unchanged, and these sums are never -0.0.
-__device__ __noinline__ double exact_88(const int32_t *c, int y, int x) {
-    const double kk00 = __dmul_rn(kFrac, kFrac);
-    double sum = 0.0;
-    for (int v = 0; v < 8; v++) {
-        for (int u = 0; u < 8; u++) {
-            const int32_t cv = c[v * 8 + u];
-            if (cv == 0) continue;
-            const double k = (u == 0 && v == 0) ? kk00 : (u == 0 || v == 0) ? kFrac : 1.0;
-            double t = __dmul_rn(k, (double)cv);
-            t = __dmul_rn(t, c_cos16[(2 * x + 1) * u]);
-            t = __dmul_rn(t, c_cos16[(2 * y + 1) * v]);
-            sum = __dadd_rn(sum, t);
-        }
-    }
-    return sum / 4.0;
-}
-
-// The reference's binary64 2-4-8 transform for sample (y, x) (decoder.rs:555-602):
-// butterfly of row pairs, horizontal pass per row (/ 2.0), four-term field pass (/ 2.0).
-__device__ __noinline__ double exact_248(const int32_t *c, int y, int x) {
-    const int field = y & 1, yy = y >> 1;
-    double sum = 0.0;
-    for (int v = 0; v < 4; v++) {
-        const int row = v * 2 + field, pair = row >> 1;
-        double hs = 0.0;
-        for (int u = 0; u < 8; u++) {
-            const double first = (double)c[pair * 16 + u], second = (double)c[pair * 16 + 8 + u];
-            const double b = (row & 1) ? __dsub_rn(first, second) : __dadd_rn(first, second);
-            if (b != 0.0) hs = __dadd_rn(hs, __dmul_rn(__dmul_rn(u == 0 ? kFrac : 1.0, b), c_cos16[(2 * x + 1) * u]));
-        }
-        const double h = hs / 2.0;
-        if (h != 0.0) sum = __dadd_rn(sum, __dmul_rn(__dmul_rn(v == 0 ? kFrac : 1.0, h), c_cos16[2 * (2 * yy + 1) * v]));
-    }
-    return sum / 2.0;
-}
-
-// Both transforms are first evaluated in fp32 as separable sums (8 + 8 terms for
-// 8-8; butterfly, 8 + 4 terms for 2-4-8), each factor cu * cos the fp32 product
-// of the fp32 roundings (3u, u = 2^-24) and each pass an FMA chain. Against the
-// exact real value of the reference's terms (its doubles: FRAC_1_SQRT_2, the cos
-// table, the integer c) the fp32 sum is off by at most (3u + 8u) + (3u + 8u) = 22u B
-// for 8-8 and 11u + 3u + 4u = 18u B for 2-4-8; the binary64 sequence by < 70 *
-// 2^-53 B. B = sum |terms| <= C1 = sum |c| for 8-8 (|cos| <= 1, cu cv <= 1) and
-// <= C1 / 2 per 2-4-8 field (a butterfly output is at most |c1| + |c2|); after the
-// final / 4.0 or / 2.0, |value32 - value64| <= 5.5u C1 < delta = 2^-21 C1 + 2^-30
-// (= 8u C1 + 2^-30, margin 1.45). If no half-integer lies within delta of value32
-// both round (half away from zero) and clamp alike; the rest are recomputed in
-// the reference order.
+// One thread per sample, four blocks per CTA: the fp32 transform and its exact
+// fallback (dv_idct_core.h), then placement.
 __global__ void __launch_bounds__(kIdctThreads) dv_idct_kernel(DvLaunch L) {
     __shared__ int32_t s_c[4][64];
     __shared__ float s_h[4][64];
@@ -417,55 +359,12 @@ __global__ void __launch_bounds__(kIdctThreads) dv_idct_kernel(DvLaunch L) {
     __syncthreads();
     const int y = px >> 3, x = px & 7;
     // pass 1: h[row][x]
-    if (valid && !failed) {
-        const int row = y;
-        float h = 0.0f;
-        if (mode) {
-            const int pair = row >> 1;
-#pragma unroll
-            for (int u = 0; u < 8; u++) {
-                const float first = (float)s_c[lb][pair * 16 + u], second = (float)s_c[lb][pair * 16 + 8 + u];
-                const float b = (row & 1) ? first - second : first + second;  // exact: |c| < 2^23
-                h = fmaf((u == 0 ? (float)kFrac : 1.0f) * c_cos16f[(2 * x + 1) * u], b, h);
-            }
-            h *= 0.5f;
-        } else {
-#pragma unroll
-            for (int u = 0; u < 8; u++)
-                h = fmaf((u == 0 ? (float)kFrac : 1.0f) * c_cos16f[(2 * x + 1) * u], (float)s_c[lb][row * 8 + u], h);
-        }
-        s_h[lb][row * 8 + x] = h;
-    }
+    if (valid && !failed) s_h[lb][y * 8 + x] = dv_row_pass(s_c[lb], mode, y, x);
     __syncthreads();
     if (!valid) return;
     uint8_t sample = 0;
-    if (!failed) {
-        float value;
-        if (mode) {
-            const int field = y & 1, yy = y >> 1;
-            float s = 0.0f;
-#pragma unroll
-            for (int v = 0; v < 4; v++)
-                s = fmaf((v == 0 ? (float)kFrac : 1.0f) * c_cos16f[2 * (2 * yy + 1) * v], s_h[lb][(v * 2 + field) * 8 + x], s);
-            value = s * 0.5f;
-        } else {
-            float s = 0.0f;
-#pragma unroll
-            for (int v = 0; v < 8; v++)
-                s = fmaf((v == 0 ? (float)kFrac : 1.0f) * c_cos16f[(2 * y + 1) * v], s_h[lb][v * 8 + x], s);
-            value = s * 0.25f;
-        }
-        const float c1 = s_c1[lb][0] + s_c1[lb][1];
-        const float near = 0.5f - (c1 * 0x1p-21f + 0x1p-30f);
-        float r;
-        const int32_t v = round_nearest(value, r);
-        if (fabsf(value - r) < near && fabsf(value) < 0x1p22f) {
-            sample = (uint8_t)min(max(v, 0), 255);
-        } else {
-            const double e = mode ? exact_248(s_c[lb], y, x) : exact_88(s_c[lb], y, x);
-            sample = (uint8_t)fmin(fmax(round(e), 0.0), 255.0);
-        }
-    }
+    if (!failed)
+        sample = dv_sample(dv_column_pass(s_h[lb], mode, y, x), s_c1[lb][0] + s_c1[lb][1], s_c[lb], mode, y, x);
     // placement (decoder.rs:432-505)
     uint32_t seg = local_blk / 30, j = local_blk % 30;
     uint32_t sequence = seg / 27, slot = seg % 27, m = j / 6, bi = j % 6;

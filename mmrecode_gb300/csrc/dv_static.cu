@@ -23,6 +23,7 @@
 #include <string>
 
 #include "../../include/mmrecode_gpu.h"
+#include "dv_vlc.h"
 #include "engine.h"
 #include "last_error.h"
 #include "kernels.h"
@@ -37,7 +38,7 @@ constexpr size_t kDvMaxInput = 144000;                   // one 625/50 frame
 constexpr size_t kDvMaxPlanar = 720 * 576 + 2 * 360 * 288;
 constexpr uint32_t kDvMaxSegments = 12 * 27;
 constexpr uint32_t kDvMaxDif = 12 * 150;
-constexpr size_t kVlcMaxEntries = 1024 + 64 * 64;
+constexpr size_t kVlcMaxEntries = kDvVlcMaxEntries;
 
 static __device__ __align__(256) uint8_t g_dv_scratch[kDvStaticScratchBytes];
 
@@ -63,72 +64,28 @@ struct Meta {  // per-call plan and state (lives at kOffMeta)
 };
 static_assert(sizeof(Meta) <= kMetaBytes, "DV static metadata exceeds its region");
 
-// Two-level VLC table with the layout kernels.h documents, from the canonical
-// codes of crates/codecs/dv/src/decoder.rs:319-354; filled into a static host
-// array (no heap use) and copied into the scratch at set-up.
+// The VLC lookup table (dv_vlc.h), filled into a static host array (no heap
+// use) and copied into the scratch at set-up.
 uint32_t g_vlc_host[kVlcMaxEntries];
-
-size_t fill_vlc_table() {
-    struct E {
-        uint32_t code, len, run;
-        int32_t level;
-    };
-    static E entries[746];
-    size_t ne = 0;
-    uint8_t len_of[409];
-    int n = 0;
-    for (auto &r : kDvVlcLenRuns)
-        for (int k = 0; k < r[1]; k++) len_of[n++] = (uint8_t)r[0];
-    uint32_t canonical = 0;
-    for (int i = 0; i < 409; i++) {
-        uint32_t len = len_of[i];
-        uint32_t code = canonical >> (32 - len);
-        canonical += 1u << (32 - len);
-        uint32_t run = i < 153 ? kDvVlcRunHead[i] : 0;
-        int32_t level = i < 153 ? kDvVlcLevelHead[i] : i - 153;
-        if (level == 0) entries[ne++] = {code, len, run, 0};
-        else {
-            entries[ne++] = {code << 1, len + 1, run, level};
-            entries[ne++] = {(code << 1) | 1, len + 1, run, -level};
-        }
-    }
-    const uint32_t l1 = kDvVlcL1Bits, l2 = 16 - kDvVlcL1Bits;
-    size_t size = (size_t)1 << l1;
-    memset(g_vlc_host, 0, sizeof(g_vlc_host));
-    for (size_t k = 0; k < ne; k++) {
-        const E &e = entries[k];
-        uint32_t packed = e.len | (e.run << 5) | ((uint32_t)(e.level + 256) << 12);
-        if (e.len <= l1) {
-            for (uint32_t j = 0; j < (1u << (l1 - e.len)); j++) g_vlc_host[(e.code << (l1 - e.len)) + j] = packed;
-        } else {
-            uint32_t prefix = e.code >> (e.len - l1);
-            if (!(g_vlc_host[prefix] & 0x80000000u)) {
-                if (size + ((size_t)1 << l2) > kVlcMaxEntries) return 0;
-                g_vlc_host[prefix] = 0x80000000u | (uint32_t)size;
-                size += (size_t)1 << l2;
-            }
-            uint32_t off = g_vlc_host[prefix] & 0xffffu, rest = e.code & ((1u << (e.len - l1)) - 1);
-            for (uint32_t j = 0; j < (1u << (16 - e.len)); j++) g_vlc_host[off + (rest << (16 - e.len)) + j] = packed;
-        }
-    }
-    return size;
-}
 
 std::mutex g_setup_mutex;
 uint8_t *g_scratch_ptr[64] = {};  // device address of g_dv_scratch, per device
 
-// Once per device, with that device current.
-cudaError_t setup(int device, uint8_t **ptr) {
+// Once per device, with that device current: looks up the array's device
+// address and writes the VLC table into it. Later calls only confirm the
+// address (a device reset reloads the module, possibly elsewhere); `redo`
+// forces the table to be written again (the caller saw it cleared).
+cudaError_t setup(int device, uint8_t **ptr, bool redo = false) {
     std::lock_guard<std::mutex> lock(g_setup_mutex);
     if (device < 0 || device >= 64) return cudaErrorInvalidDevice;
-    if (g_scratch_ptr[device]) {
-        *ptr = g_scratch_ptr[device];
-        return cudaSuccess;
-    }
     void *p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_dv_scratch);
     if (e != cudaSuccess) return e;
-    size_t entries = fill_vlc_table();
+    if (g_scratch_ptr[device] == (uint8_t *)p && !redo) {
+        *ptr = g_scratch_ptr[device];
+        return cudaSuccess;
+    }
+    size_t entries = fill_dv_vlc(g_vlc_host, kVlcMaxEntries);
     if (entries == 0) return cudaErrorInvalidValue;
     e = cudaMemcpy((uint8_t *)p + kOffVlc, g_vlc_host, entries * 4, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return e;
@@ -147,6 +104,16 @@ mmr_status fail(mmr_gpu_frame_info *info, mmr_status st, const char *m) {
 }  // namespace mmr
 
 using namespace mmr;
+
+namespace {
+
+// One decode of the validated packet with the set-up array at s. *table_word
+// receives the first VLC table entry as the device held it during the call
+// (never 0 once set up: it decodes the two-bit code 00).
+mmr_status run_static(const uint8_t *data, size_t len, uint8_t *out, const Probe &pr, uint8_t *s, uint32_t *table_word,
+                      mmr_gpu_frame_info *info);
+
+}  // namespace
 
 extern "C" MMR_API mmr_status mmr_dv_decode_static(const uint8_t *data, size_t len, uint8_t *out, size_t out_capacity,
                                                    mmr_gpu_frame_info *info) {
@@ -182,6 +149,27 @@ extern "C" MMR_API mmr_status mmr_dv_decode_static(const uint8_t *data, size_t l
         snprintf(msg, sizeof msg, "CUDA device unavailable: %s", cudaGetErrorString(e));
         return fail(info, MMR_STATUS_INTERNAL_ERROR, msg);
     }
+    uint32_t word = 0;
+    mmr_status st = run_static(data, len, out, pr, s, &word, info);
+    if (st != MMR_STATUS_INTERNAL_ERROR && word == 0) {
+        // the table was cleared under us (the device was reset): set up again and redo the call
+        e = setup(device, &s, true);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            snprintf(msg, sizeof msg, "CUDA device unavailable: %s", cudaGetErrorString(e));
+            return fail(info, MMR_STATUS_INTERNAL_ERROR, msg);
+        }
+        st = run_static(data, len, out, pr, s, &word, info);
+    }
+    return st;
+}
+
+namespace {
+
+mmr_status run_static(const uint8_t *data, size_t len, uint8_t *out, const Probe &pr, uint8_t *s, uint32_t *table_word,
+                      mmr_gpu_frame_info *info) {
+    char msg[200];
+    cudaError_t e = cudaSuccess;
     bool pal = pr.format == kYuv420;
     uint32_t seqs = pal ? 12 : 10;
     Meta meta;
@@ -218,7 +206,9 @@ extern "C" MMR_API mmr_status mmr_dv_decode_static(const uint8_t *data, size_t l
     L.vlc = reinterpret_cast<const uint32_t *>(s + kOffVlc);
     L.n_blocks = (uint64_t)seqs * 27 * 30;
     L.item_ok = &dm->item_ok;
-    cudaStream_t st = 0;
+    // the calling thread's default stream: no creation, no allocation, and no
+    // implicit synchronisation with the application's other (blocking) streams
+    cudaStream_t st = cudaStreamPerThread;
     e = cudaMemcpyAsync(s + kOffIn, data, len, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dm, &meta, sizeof(meta), cudaMemcpyHostToDevice, st);
     // the segment decoder writes only non-zero coefficients
@@ -231,6 +221,7 @@ extern "C" MMR_API mmr_status mmr_dv_decode_static(const uint8_t *data, size_t l
     Meta back;
     if (e == cudaSuccess) e = cudaMemcpyAsync(&back, dm, sizeof(back), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(out, s + kOffOut, pr.planar_bytes, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(table_word, s + kOffVlc, 4, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -257,3 +248,5 @@ extern "C" MMR_API mmr_status mmr_dv_decode_static(const uint8_t *data, size_t l
     set_last_error(MMR_STATUS_OK, "");
     return MMR_STATUS_OK;
 }
+
+}  // namespace

@@ -31,13 +31,12 @@
 #include "common.h"
 #include "encode.h"
 #include "encode_gpu.h"
+#include "fdct_core.h"
 #include "tables.h"
 
 namespace mmr {
 namespace {
 
-__constant__ float c_m32[64] = MMR_IDCT_MATRIX_INIT;   // IDCT_MATRIX[x][u] at x * 8 + u, rounded to fp32
-__constant__ double c_m64[64] = MMR_IDCT_MATRIX_INIT;  // the reference's binary64 values
 
 struct EncFrame {
     const uint8_t *plane[3];
@@ -110,36 +109,6 @@ __device__ __forceinline__ uint32_t segment_of_chunk(const EncLaunch &L, uint64_
 
 // ----------------------------------------------------------------- FDCT ---
 
-// The quantised coefficient (v, u) of a block exactly as forward_dct_quantize
-// (transform.rs:111-134) computes it: binary64, every product and sum rounded
-// separately, rows accumulated over x, then the column over y, both from 0.0,
-// the quotient rounded half away from zero.
-__device__ __noinline__ int exact_coefficient(const uint8_t *s, int u, int v, int q) {
-    double value = 0.0;
-    for (int y = 0; y < 8; y++) {
-        double t = 0.0;
-        for (int x = 0; x < 8; x++) t = __dadd_rn(t, __dmul_rn(c_m64[x * 8 + u], (double)s[y * 8 + x] - 128.0));
-        value = __dadd_rn(value, __dmul_rn(c_m64[y * 8 + v], t));
-    }
-    return (int)round(__ddiv_rn(value, (double)q));
-}
-
-// Error bound of the fp32 path, per coefficient. With S = sample - 128 and the
-// coefficient's magnitude sum B = sum_y |M[y][v]| sum_x |M[x][u]| |S[y][x]|, each
-// pass is an 8-term FMA chain (8 roundings of at most 2^-24 of a partial sum
-// bounded by its magnitude sum) on fp32 matrix entries (2^-24 relative each),
-// against the reference's binary64 chains (2^-53 per operation):
-// |V32 - V64| <= (8 + 9 + 1) * 2^-24 * B + 2^-46 * B < 1.08e-6 * B. The fp32
-// quotient is V32 times the rounded reciprocal of q (two roundings of 2^-24 each:
-// within 1.2e-7 |q32| of V32 / q) and the binary64 one is within 2^-53 |V64 / q|, so
-// |q32 - q64| < 1.08e-6 * B / q + 1.2e-7 * |q32| + 1e-12. The guard below takes
-// 1.5e-6, 3.6e-7 and 1e-9 for these (B itself computed in fp32 to within 2^-20
-// relative, B / q as B times the reciprocal): a fp32 quotient farther than that from
-// the nearest half-integer rounds to the reference's integer; the rest are
-// recomputed in binary64. (B <= 1025, so the guard never exceeds 2e-3.)
-__device__ __forceinline__ float tie_guard(float b, float rq, float quot_abs) {
-    return 1.5e-6f * b * rq + 3.6e-7f * quot_abs + 1e-9f;
-}
 constexpr int kEncBlocksPerCta = 32;
 
 __global__ void __launch_bounds__(256) fdct_kernel(EncLaunch L) {
@@ -180,16 +149,7 @@ __global__ void __launch_bounds__(256) fdct_kernel(EncLaunch L) {
     __syncthreads();
     if (valid) {  // row pass: t[r][u] = sum_x M[x][u] S[r][x], and its magnitude sum
 #pragma unroll
-        for (int u = 0; u < 8; u++) {
-            float acc = 0.0f, mag = 0.0f;
-#pragma unroll
-            for (int x = 0; x < 8; x++) {
-                acc = fmaf(c_m32[x * 8 + u], s_in[lb][r][x], acc);
-                mag = fmaf(fabsf(c_m32[x * 8 + u]), fabsf(s_in[lb][r][x]), mag);
-            }
-            s_row[lb][r][u] = acc;
-            s_mag[lb][r][u] = mag;
-        }
+        for (int u = 0; u < 8; u++) fdct_row_pass(s_in[lb][r], u, s_row[lb][r][u], s_mag[lb][r][u]);
     }
     __syncthreads();
     __shared__ __align__(16) int16_t s_out[kEncBlocksPerCta][64];  // the block in zigzag order
@@ -199,23 +159,10 @@ __global__ void __launch_bounds__(256) fdct_kernel(EncLaunch L) {
         const float *rq = L.rq + tq * 64;
 #pragma unroll
         for (int v = 0; v < 8; v++) {
-            float acc = 0.0f, mag = 0.0f;
-#pragma unroll
-            for (int y = 0; y < 8; y++) {
-                acc = fmaf(c_m32[y * 8 + v], s_row[lb][y][u], acc);
-                mag = fmaf(fabsf(c_m32[y * 8 + v]), s_mag[lb][y][u], mag);
-            }
-            const int q = qt[v * 8 + u];
-            const float r_q = rq[v * 8 + u];
-            const float quot = acc * r_q;
-            const float a = fabsf(quot);
-            int k;
-            if (fabsf(a - floorf(a) - 0.5f) < tie_guard(mag * (1.0f + 1.0f / 1048576.0f), r_q, a)) {
-                k = exact_coefficient(s_raw[lb], u, v, q);
-                atomicAdd(L.exact, 1ull);
-            } else {
-                k = (int)rintf(quot);
-            }
+            bool exact;
+            int k = fdct_quantise(&s_row[lb][0][0], &s_mag[lb][0][0], 9, s_raw[lb], u, v, qt[v * 8 + u],
+                                  rq[v * 8 + u], exact);
+            if (exact) atomicAdd(L.exact, 1ull);
             if (v | u) k = min(max(k, -1023), 1023);  // encode_scan (encoder.rs:372-374)
             s_out[lb][L.nat2zz[v * 8 + u]] = (int16_t)k;
         }

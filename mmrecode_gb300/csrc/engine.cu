@@ -11,6 +11,7 @@
 #include <string>
 #include <vector>
 
+#include "dv_vlc.h"
 #include "jpeg_syntax.h"
 #include "kernels.h"
 #include "plan.h"
@@ -431,51 +432,12 @@ DvPlan plan_dv(const uint8_t *in, size_t len) {
     return p;
 }
 
-// Two-level DV VLC table (see kernels.h for the entry layout), built from the
-// canonical codes of decoder.rs:319-354.
+// Two-level DV VLC table (dv_vlc.h).
 std::vector<uint32_t> build_dv_vlc() {
-    struct E {
-        uint32_t code, len, run;
-        int32_t level;
-    };
-    std::vector<E> entries;
-    uint8_t len_of[409];
-    int n = 0;
-    for (auto &r : kDvVlcLenRuns)
-        for (int k = 0; k < r[1]; k++) len_of[n++] = (uint8_t)r[0];
-    uint32_t canonical = 0;
-    for (int i = 0; i < 409; i++) {
-        uint32_t len = len_of[i];
-        uint32_t code = canonical >> (32 - len);
-        canonical += 1u << (32 - len);
-        uint32_t run = i < 153 ? kDvVlcRunHead[i] : 0;
-        int32_t level = i < 153 ? kDvVlcLevelHead[i] : i - 153;
-        if (level == 0) entries.push_back({code, len, run, 0});
-        else {
-            entries.push_back({code << 1, len + 1, run, level});
-            entries.push_back({(code << 1) | 1, len + 1, run, -level});
-        }
-    }
-    const int l1 = kDvVlcL1Bits, l2 = 16 - kDvVlcL1Bits;
-    std::vector<uint32_t> t(1u << l1, 0);
-    for (auto &e : entries) {
-        uint32_t packed = e.len | (e.run << 5) | ((uint32_t)(e.level + 256) << 12);
-        if ((int)e.len <= l1) {
-            uint32_t first = e.code << (l1 - e.len), cnt = 1u << (l1 - e.len);
-            for (uint32_t j = 0; j < cnt; j++) t[first + j] = packed;
-        } else {
-            uint32_t prefix = e.code >> (e.len - l1);
-            if (!(t[prefix] & 0x80000000u)) {
-                uint32_t off = (uint32_t)t.size();
-                t.resize(t.size() + (1u << l2), 0);
-                t[prefix] = 0x80000000u | off;
-            }
-            uint32_t off = t[prefix] & 0xffffu;
-            uint32_t rest = e.code & ((1u << (e.len - l1)) - 1);
-            uint32_t first = rest << (16 - e.len), cnt = 1u << (16 - e.len);
-            for (uint32_t j = 0; j < cnt; j++) t[off + first + j] = packed;
-        }
-    }
+    std::vector<uint32_t> t(kDvVlcMaxEntries);
+    const size_t n = fill_dv_vlc(t.data(), t.size());
+    if (n == 0) throw std::runtime_error("DV VLC table exceeds its two-level layout");
+    t.resize(n);
     return t;
 }
 
@@ -715,6 +677,7 @@ struct Engine::Impl {
     // stage boundaries: start, uploads, scan, entropy, idct, dv, rgb, end
     cudaEvent_t ev[8] = {};
     cudaEvent_t marks[3] = {};  // inside the entropy stage
+    cudaEvent_t dv_mark = nullptr;  // inside the DV stage: segment decode done
     // launch sequences of recent batches, as CUDA graphs once they repeat
     struct GraphEntry {
         std::vector<uintptr_t> key;
@@ -741,6 +704,7 @@ Engine::Engine(int device, int levels) : device_(device), slice_bits_(0), impl_(
     stream_ = streams_[0];
     for (auto &e : impl_->ev) MMR_CUDA(cudaEventCreate(&e));
     for (auto &e : impl_->marks) MMR_CUDA(cudaEventCreate(&e));
+    MMR_CUDA(cudaEventCreate(&impl_->dv_mark));
     impl_->vlc = build_dv_vlc();
     impl_->d_vlc.ensure(impl_->vlc.size() * 4);
     MMR_CUDA(cudaMemcpy(impl_->d_vlc.ptr, impl_->vlc.data(), impl_->vlc.size() * 4, cudaMemcpyHostToDevice));
@@ -753,6 +717,7 @@ Engine::~Engine() {
         if (e) cudaEventDestroy(e);
     for (auto &e : impl_->marks)
         if (e) cudaEventDestroy(e);
+    if (impl_->dv_mark) cudaEventDestroy(impl_->dv_mark);
     for (auto &g : impl_->graphs)
         if (g.exec) cudaGraphExecDestroy(g.exec);
     delete impl_;
@@ -1336,6 +1301,7 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
         DL.item_ok = JL.item_ok;
         if (!dframes.empty()) {
             launch_dv_decode(DL, s);
+            MMR_CUDA(record_event(I.dv_mark, s, capturing));
             launch_dv_idct(DL, s);
             launches_ += 4;
         }
@@ -1386,6 +1352,20 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
         const bool use_graphs = graphs_ && device_resident;
         if (use_graphs) {
             key = {n, (uintptr_t)I.h_blob.ptr, (uintptr_t)I.h_back.ptr, blob.bytes.size()};
+            // the launch shapes (every grid size and per-kernel count the enqueue
+            // derives); the plan image compared below holds them too, but the key
+            // states them so that no change of shape can replay a stale graph
+            for (uintptr_t v : {(uintptr_t)jframes.size(), (uintptr_t)tile_first.back(), (uintptr_t)luts.size(),
+                                (uintptr_t)items_small.size(), (uintptr_t)n_items, (uintptr_t)ranges.size(),
+                                (uintptr_t)idct_cta.back(), (uintptr_t)n_slots, (uintptr_t)scratch_blocks,
+                                (uintptr_t)blocks, (uintptr_t)dframes.size(), (uintptr_t)seg_first.back(),
+                                (uintptr_t)dif_first.back(), (uintptr_t)dv_blocks, (uintptr_t)rgbjobs.size(),
+                                (uintptr_t)rgbcta.back()})
+                key.push_back(v);
+            for (int v = 0; v < kFusedSlots; v++) {
+                key.push_back((uintptr_t)fjobs[v].size());
+                key.push_back((uintptr_t)fcta[v].back());
+            }
             for (const DevBuf *b : {&I.d_in, &I.d_tok, &I.d_blob, &I.d_tile_tok, &I.d_tile_rst, &I.d_rsts,
                                     &I.d_results, &I.d_coef, &I.d_dc, &I.d_planes, &I.d_out, &I.d_dvcoef, &I.d_modes,
                                     &I.d_flags, &I.d_segerr, &I.d_vlc, &I.d_fix, &I.d_slot_item, &I.d_ivs, &I.d_sync,
@@ -1466,6 +1446,12 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
                 MMR_CUDA(cudaEventElapsedTime(&times->slice_decode_ms, I.marks[1], I.marks[2]));
             } else {
                 times->slice_spec_ms = times->slice_sync_ms = times->slice_decode_ms = 0;
+            }
+            if (dv_blocks) {
+                MMR_CUDA(cudaEventElapsedTime(&times->dv_segment_ms, I.ev[4], I.dv_mark));
+                MMR_CUDA(cudaEventElapsedTime(&times->dv_idct_ms, I.dv_mark, I.ev[5]));
+            } else {
+                times->dv_segment_ms = times->dv_idct_ms = 0;
             }
             times->jpeg_blocks = blocks;
             times->graph_replays = graph_replayed_ ? 1 : 0;

@@ -87,6 +87,8 @@ struct EngineTimes {
     // inside entropy_ms: the chunked decoder's speculative pass, its sync passes +
     // block prefix, and its final decode
     float slice_spec_ms = 0, slice_sync_ms = 0, slice_decode_ms = 0;
+    // inside dv_ms: DIF check + segment decode, then the transform and placement
+    float dv_segment_ms = 0, dv_idct_ms = 0;
     uint64_t input_bytes = 0, output_bytes = 0, jpeg_blocks = 0, dv_blocks = 0, rgb_pixels = 0;
     uint64_t idct_exact_samples = 0;  // MJPEG samples recomputed in exact binary64 order
     uint32_t graph_replays = 0;       // batches whose launches replayed a captured CUDA graph

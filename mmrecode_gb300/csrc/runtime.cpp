@@ -18,6 +18,8 @@ void accumulate_times(EngineTimes &a, const EngineTimes &t) {
     a.slice_spec_ms += t.slice_spec_ms;
     a.slice_sync_ms += t.slice_sync_ms;
     a.slice_decode_ms += t.slice_decode_ms;
+    a.dv_segment_ms += t.dv_segment_ms;
+    a.dv_idct_ms += t.dv_idct_ms;
     a.input_bytes += t.input_bytes;
     a.output_bytes += t.output_bytes;
     a.jpeg_blocks += t.jpeg_blocks;
