@@ -10,6 +10,14 @@ import numpy as np
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
+# counts the parity tests report (frames, blocks, near ties, exact-path samples);
+# tests/conftest.py prints them in the terminal summary
+REPORTS: list = []
+
+
+def report(name: str, **counts) -> None:
+    REPORTS.append((name, counts))
+
 
 def fixture(rel: str) -> bytes:
     with open(os.path.join(GOLDEN, rel), "rb") as f:
@@ -176,3 +184,28 @@ def prefixed(status: int, message: str) -> str:
     """The C ABI's message for an oracle (Rust-level) diagnostic (crates/core/src/error.rs:18-27)."""
     prefix = {1: "invalid argument: ", 2: "invalid data: ", 3: "unsupported: ", 4: "invalid state: "}
     return prefix.get(status, "") + message
+
+
+# ---------------------------------------------------------------- oracle pool
+
+def oracle_digest(job):
+    """(kind, packet) -> (status, SHA-256 of the oracle's planar frame, of its RGB24 or None).
+    kind: "mjpeg", "mjpeg-rgb" (also the RGB digest), "dv". Runs in pool workers."""
+    import hashlib
+
+    import oracle
+
+    kind, packet = job
+    r = oracle.dv_decode(packet) if kind == "dv" else oracle.jpeg_decode(packet)
+    if r.status != 0:
+        return r.status, None, None
+    planar = hashlib.sha256(b"".join(p[2] for p in r.frame.planes)).hexdigest()
+    rgb = hashlib.sha256(oracle.rgb24(r.frame)).hexdigest() if kind == "mjpeg-rgb" else None
+    return 0, planar, rgb
+
+
+def oracle_pool():
+    """A process pool for the oracle, started with spawn (safe after CUDA is initialised)."""
+    import multiprocessing as mp
+
+    return mp.get_context("spawn").Pool(os.cpu_count() or 4)

@@ -142,7 +142,19 @@ def test_probe_reports_geometry_from_headers():
     assert (info.format, info.plane_width[1], info.plane_height[1]) == (m.YUV422P8, 960, 1080)
 
 
-REFERENCE_SMOKE = "/root/reference/crates/capi/tests/smoke.c"
+def _reference_smoke() -> str:
+    """The reference's own C smoke program, where the reference checkout is present
+    (its location is the fixture script's, tests/golden/make_fixtures.py)."""
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("make_fixtures", os.path.join(ROOT, "tests", "golden",
+                                                                                "make_fixtures.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return os.path.join(mod.REFERENCE, "crates", "capi", "tests", "smoke.c")
+
+
+REFERENCE_SMOKE = _reference_smoke()
 
 
 @pytest.mark.skipif(not os.path.exists(REFERENCE_SMOKE) or not shutil.which("gcc"), reason="reference smoke.c absent")

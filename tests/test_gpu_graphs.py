@@ -89,3 +89,42 @@ def test_replayed_batches_match_and_read_current_packets(output):
         ctx.set_graphs(False)
         _run(ctx, arr)
         assert ctx.stats()["graph_replays"] == 0
+
+
+def test_same_lengths_and_sizes_different_geometry_never_replay_a_stale_graph():
+    """Two batches in the same buffers with equal packet lengths, output sizes
+    and plan size but transposed frame geometry (64x32 against 32x64 gray): each
+    replays only its own captured graph, and every output equals the oracle's."""
+    torch = pytest.importorskip("torch")
+    import numpy as np
+
+    rng = np.random.default_rng(7)
+
+    def gray(w, h):
+        px = rng.integers(0, 256, (h, w), dtype=np.uint8).tobytes()
+        return m.encode_jpeg(m.VideoFrame(m.GRAY8, w, h, [m.Plane(px, w, w, h)], m.RANGE_FULL), 80)
+
+    a = [gray(64, 32), gray(64, 32)]
+    b = [gray(32, 64), gray(32, 64)]
+    size = max(len(p) for p in a + b)
+    a = [p + bytes(size - len(p)) for p in a]  # bytes after EOI are the reference's trailing data
+    b = [p + bytes(size - len(p)) for p in b]
+    host, dev, offs, outs, arr = _batch(torch, a, m.OUTPUT_PLANAR)
+
+    def load(packets):
+        for i, p in enumerate(packets):
+            host.numpy()[offs[i]:offs[i] + len(p)] = memoryview(p)
+        dev.copy_(host)
+
+    with m.Context(engines=1) as ctx:
+        replays = []
+        for packets in (a, a, a, b, b, b, a, b):
+            load(packets)
+            _run(ctx, arr)
+            replays.append(ctx.stats()["graph_replays"])
+            for i, p in enumerate(packets):
+                st, payload = _expected(p, m.OUTPUT_PLANAR)
+                assert arr[i].status == st == 0, arr[i].message
+                assert (arr[i].width, arr[i].height) == ((64, 32) if packets is a else (32, 64))
+                assert outs[i].cpu().numpy().tobytes() == payload, i
+        assert replays == [0, 1, 1, 0, 1, 1, 1, 1]

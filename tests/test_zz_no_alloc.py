@@ -18,6 +18,7 @@ import ctypes
 import pytest
 
 import mmrecode_gb300 as m
+import oracle
 from mmrecode_gb300 import _lib, synth
 from helpers import DV_FIXTURES, fixture
 
@@ -54,6 +55,28 @@ def test_static_entry_point_matches_mmr_dv_decode_on_two_calls_in_a_row():
             assert (info.format, info.width, info.height, info.plane_count) == (frame.format, frame.width,
                                                                                  frame.height, 3)
             assert got == expect, f"packet {k} call {call}: samples differ from mmr_dv_decode"
+        ref = oracle.dv_decode(packet)  # and directly against the reference algorithm
+        assert ref.status == 0 and expect == b"".join(p[2] for p in ref.frame.planes), f"packet {k}: oracle"
+
+
+def _device_free_bytes() -> int:
+    """Free device memory as the driver reports it for the current context."""
+    cuda = ctypes.CDLL("libcuda.so.1")
+    free, total = ctypes.c_size_t(0), ctypes.c_size_t(0)
+    assert cuda.cuMemGetInfo_v2(ctypes.byref(free), ctypes.byref(total)) == 0
+    return free.value
+
+
+def test_calls_after_set_up_allocate_no_device_memory():
+    packets = [fixture(r) for r in DV_FIXTURES] + synth.dv_stream(117, 3)
+    st, _, _ = static_decode(packets[0])  # the first call on the device sets it up
+    assert st == 0
+    before = _device_free_bytes()
+    for _ in range(3):
+        for p in packets:
+            st, _, _ = static_decode(p)
+            assert st == 0
+    assert _device_free_bytes() == before
 
 
 def test_static_entry_point_errors_match_and_do_not_leak_into_the_next_call():
