@@ -14,8 +14,9 @@
 // both round (half away from zero) and clamp alike; the rest are recomputed in
 // the reference order.
 //
-// Used by dv_idct_kernel (one thread per sample) and, with the same functions,
-// by the block-level transform tests.
+// Used by dv_idct_kernel (eight threads per block, the row-parallel form at the
+// end of this file) and, with the same functions, by the block-level transform
+// tests.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -76,46 +77,6 @@ __device__ __noinline__ double exact_248(const int32_t *c, int y, int x) {
     return sum / 2.0;
 }
 
-// Horizontal pass for output (row, x) of a block of int32 coefficients c
-// (natural order): the 8-8 row sum, or for 2-4-8 the row sum over the
-// butterfly of the row pair, halved.
-__device__ __forceinline__ float dv_row_pass(const int32_t *c, bool mode248, int row, int x) {
-    float h = 0.0f;
-    if (mode248) {
-        const int pair = row >> 1;
-#pragma unroll
-        for (int u = 0; u < 8; u++) {
-            const float first = (float)c[pair * 16 + u], second = (float)c[pair * 16 + 8 + u];
-            const float b = (row & 1) ? first - second : first + second;  // exact: |c| < 2^23
-            h = fmaf((u == 0 ? (float)kFrac : 1.0f) * c_cos16f[(2 * x + 1) * u], b, h);
-        }
-        h *= 0.5f;
-    } else {
-#pragma unroll
-        for (int u = 0; u < 8; u++)
-            h = fmaf((u == 0 ? (float)kFrac : 1.0f) * c_cos16f[(2 * x + 1) * u], (float)c[row * 8 + u], h);
-    }
-    return h;
-}
-
-// Vertical pass for sample (y, x) from the 64 row-pass outputs h: the 8-8 column
-// sum / 4, or the 2-4-8 four-term field sum / 2.
-__device__ __forceinline__ float dv_column_pass(const float *h, bool mode248, int y, int x) {
-    if (mode248) {
-        const int field = y & 1, yy = y >> 1;
-        float s = 0.0f;
-#pragma unroll
-        for (int v = 0; v < 4; v++)
-            s = fmaf((v == 0 ? (float)kFrac : 1.0f) * c_cos16f[2 * (2 * yy + 1) * v], h[(v * 2 + field) * 8 + x], s);
-        return s * 0.5f;
-    }
-    float s = 0.0f;
-#pragma unroll
-    for (int v = 0; v < 8; v++)
-        s = fmaf((v == 0 ? (float)kFrac : 1.0f) * c_cos16f[(2 * y + 1) * v], h[v * 8 + x], s);
-    return s * 0.25f;
-}
-
 // The sample: the fp32 value's rounding when no half-integer lies within delta of
 // it (c1 = sum |c| of the block), else the reference's binary64 value rounded
 // half away from zero; clamped to 0..255.
@@ -126,6 +87,129 @@ __device__ __forceinline__ uint8_t dv_sample(float value, float c1, const int32_
     if (fabsf(value - r) < near && fabsf(value) < 0x1p22f) return (uint8_t)min(max(v, 0), 255);
     const double e = mode248 ? exact_248(c, y, x) : exact_88(c, y, x);
     return (uint8_t)fmin(fmax(round(e), 0.0), 255.0);
+}
+
+// The sample of every position of a block whose only nonzero coefficient is the
+// DC: all 64 are equal (cos16[0] = cos8[0] = 1.0, and only the u = v = 0 terms
+// are nonzero), so the reference-order value of position (0, 0) is computed once
+// per block. These blocks are common in smooth content, and with an odd DC level
+// their exact value is a half-integer: every sample would go to the binary64
+// pass one by one.
+__device__ __forceinline__ uint8_t dv_flat_sample(const int32_t *c, bool mode248) {
+    const double e = mode248 ? exact_248(c, 0, 0) : exact_88(c, 0, 0);
+    return (uint8_t)fmin(fmax(round(e), 0.0), 255.0);
+}
+
+// ---------------------------------------------------------------------------
+// Row-parallel form: eight threads per block, thread r producing output row r.
+// The factors are fp32 products of the fp32 roundings, W[u][x] = (u ? 1 : FRAC)
+// * cos16f[(2x+1)u] (transposed: a thread reads the eight x of one u as two
+// 16-byte loads) and V4[yy][v] = (v ? 1 : FRAC) * cos16f[2(2yy+1)v]. Pass 1 is an
+// FMA chain over u per output, pass 2 one over v, the 2-4-8 butterfly and the
+// halvings exact: the evaluation the bound above describes.
+
+// Fills the tables (64 + 16 floats) cooperatively; callers synchronise before use.
+__device__ __forceinline__ void dv_fill_tables(float *wt, float *v4) {
+    for (int i = threadIdx.x; i < 80; i += blockDim.x) {
+        if (i < 64) {
+            const int u = i >> 3, x = i & 7;
+            wt[i] = (u == 0 ? (float)kFrac : 1.0f) * c_cos16f[(2 * x + 1) * u];
+        } else {
+            const int yy = (i - 64) >> 2, v = (i - 64) & 3;
+            v4[i - 64] = (v == 0 ? (float)kFrac : 1.0f) * c_cos16f[2 * (2 * yy + 1) * v];
+        }
+    }
+}
+
+// Pass 1 for row r: h[r][0..7] into hrow (16-byte aligned). c: the block's 64
+// coefficients (natural order).
+__device__ __forceinline__ void dv_row_pass8(const int32_t *c, const float *wt, bool mode248, int r, float *hrow) {
+    float b[8];
+    if (mode248) {
+        const int pair = r >> 1;
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            const float first = (float)c[pair * 16 + u], second = (float)c[pair * 16 + 8 + u];
+            b[u] = (r & 1) ? first - second : first + second;  // exact: |c| < 2^23
+        }
+    } else {
+#pragma unroll
+        for (int u = 0; u < 8; u++) b[u] = (float)c[r * 8 + u];
+    }
+    float h[8];
+#pragma unroll
+    for (int x = 0; x < 8; x++) h[x] = 0.0f;
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+        const float4 w0 = reinterpret_cast<const float4 *>(wt + u * 8)[0];
+        const float4 w1 = reinterpret_cast<const float4 *>(wt + u * 8)[1];
+        const float w[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+#pragma unroll
+        for (int x = 0; x < 8; x++) h[x] = fmaf(w[x], b[u], h[x]);
+    }
+    if (mode248) {
+#pragma unroll
+        for (int x = 0; x < 8; x++) h[x] *= 0.5f;
+    }
+    reinterpret_cast<float4 *>(hrow)[0] = make_float4(h[0], h[1], h[2], h[3]);
+    reinterpret_cast<float4 *>(hrow)[1] = make_float4(h[4], h[5], h[6], h[7]);
+}
+
+// Pass 2 for output row y: value[0..7] from the block's 64 pass-1 outputs h
+// (row-major, 16-byte aligned rows).
+__device__ __forceinline__ void dv_column_pass8(const float *h, const float *wt, const float *v4, bool mode248, int y,
+                                                float *value) {
+    float s[8];
+#pragma unroll
+    for (int x = 0; x < 8; x++) s[x] = 0.0f;
+    if (mode248) {
+        const int field = y & 1, yy = y >> 1;
+#pragma unroll
+        for (int v = 0; v < 4; v++) {
+            const float wv = v4[yy * 4 + v];
+            const float4 h0 = reinterpret_cast<const float4 *>(h + (v * 2 + field) * 8)[0];
+            const float4 h1 = reinterpret_cast<const float4 *>(h + (v * 2 + field) * 8)[1];
+            const float hv[8] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z, h1.w};
+#pragma unroll
+            for (int x = 0; x < 8; x++) s[x] = fmaf(wv, hv[x], s[x]);
+        }
+#pragma unroll
+        for (int x = 0; x < 8; x++) value[x] = s[x] * 0.5f;
+    } else {
+#pragma unroll
+        for (int v = 0; v < 8; v++) {
+            const float wv = wt[v * 8 + y];  // V[y][v] = W[v][y]
+            const float4 h0 = reinterpret_cast<const float4 *>(h + v * 8)[0];
+            const float4 h1 = reinterpret_cast<const float4 *>(h + v * 8)[1];
+            const float hv[8] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z, h1.w};
+#pragma unroll
+            for (int x = 0; x < 8; x++) s[x] = fmaf(wv, hv[x], s[x]);
+        }
+#pragma unroll
+        for (int x = 0; x < 8; x++) value[x] = s[x] * 0.25f;
+    }
+}
+
+// The eight samples of row y of a block, row-parallel: c (the block's
+// coefficients) and h (its pass-1 outputs) in shared memory, c1 = sum |c|, flat
+// = no nonzero AC coefficient (then lane `flat_src` of the warp computes the one
+// reference-order value and broadcasts it; all eight lanes of the group call this
+// together). Returns the samples packed little-endian (x = 0 in the low byte).
+__device__ __forceinline__ unsigned long long dv_row_samples(const int32_t *c, const float *h, const float *wt,
+                                                             const float *v4, bool mode248, int y, float c1,
+                                                             bool flat, int flat_src, unsigned group_mask) {
+    if (flat) {
+        uint32_t v = 0;
+        if ((int)(threadIdx.x & 31) == flat_src) v = dv_flat_sample(c, mode248);
+        v = __shfl_sync(group_mask, v, flat_src);
+        return 0x0101010101010101ull * v;
+    }
+    float value[8];
+    dv_column_pass8(h, wt, v4, mode248, y, value);
+    unsigned long long out = 0;
+#pragma unroll
+    for (int x = 0; x < 8; x++) out |= (unsigned long long)dv_sample(value[x], c1, c, mode248, y, x) << (8 * x);
+    return out;
 }
 
 }  // namespace

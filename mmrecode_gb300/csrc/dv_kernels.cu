@@ -317,98 +317,128 @@ __device__ __forceinline__ void mb_coords(bool pal, uint32_t seqs, uint32_t sequ
     }
 }
 
-constexpr int kIdctThreads = 256;  // 4 blocks x 64 samples
+constexpr int kIdctBlocks = 32;                  // blocks per CTA
+constexpr int kIdctThreads = kIdctBlocks * 8;    // eight threads (rows) per block
 
-// One thread per sample, four blocks per CTA: the fp32 transform and its exact
-// fallback (dv_idct_core.h), then placement.
+// Stores the eight bytes of `row` at dst (any alignment).
+__device__ __forceinline__ void store_row8(uint8_t *dst, unsigned long long row) {
+    const uintptr_t a = reinterpret_cast<uintptr_t>(dst);
+    if ((a & 7) == 0) {
+        *reinterpret_cast<uint2 *>(dst) = make_uint2((uint32_t)row, (uint32_t)(row >> 32));
+    } else if ((a & 3) == 0) {
+        reinterpret_cast<uint32_t *>(dst)[0] = (uint32_t)row;
+        reinterpret_cast<uint32_t *>(dst)[1] = (uint32_t)(row >> 32);
+    } else {
+#pragma unroll
+        for (int x = 0; x < 8; x++) dst[x] = (uint8_t)(row >> (8 * x));
+    }
+}
+
+__device__ __forceinline__ void store_row4(uint8_t *dst, uint32_t row) {
+    if ((reinterpret_cast<uintptr_t>(dst) & 3) == 0) {
+        *reinterpret_cast<uint32_t *>(dst) = row;
+    } else {
+#pragma unroll
+        for (int x = 0; x < 4; x++) dst[x] = (uint8_t)(row >> (8 * x));
+    }
+}
+
+// Eight threads per block, thread r producing row r: the fp32 row and column
+// passes with the exact fallback (dv_idct_core.h), then placement
+// (decoder.rs:432-505) with 8-byte row stores. A warp holds four blocks of one
+// frame (frames start at multiples of 4 blocks: 8100 and 9720 blocks per frame),
+// so one search per warp finds it; the eight threads of a block synchronise
+// through their warp only.
 __global__ void __launch_bounds__(kIdctThreads) dv_idct_kernel(DvLaunch L) {
-    __shared__ int32_t s_c[4][64];
-    __shared__ float s_h[4][64];
-    __shared__ float s_c1[4][2];
-    int lb = threadIdx.x >> 6, px = threadIdx.x & 63;
-    uint64_t gb = (uint64_t)blockIdx.x * 4 + lb;
+    __shared__ __align__(16) int32_t s_c[kIdctBlocks][64];
+    __shared__ __align__(16) float s_h[kIdctBlocks][64];
+    __shared__ __align__(16) float s_wt[64];
+    __shared__ __align__(16) float s_v4[16];
+    dv_fill_tables(s_wt, s_v4);
+    __syncthreads();
+    const int lane = threadIdx.x & 31, lb = threadIdx.x >> 3, r = threadIdx.x & 7;
+    const unsigned group_mask = 0xffu << (lane & 24);
+    const uint64_t gb = (uint64_t)blockIdx.x * kIdctBlocks + lb;
     bool valid = gb < L.n_blocks;
-    uint32_t f = 0, local_blk = 0;
-    const DvFrame *F = nullptr;
-    bool failed = false, mode = false;
-    int32_t cval = 0;
-    if (valid) {
-        // frame from block index: blocks of frame f are [blk_off, blk_off + sequences*27*30)
+    uint32_t f = 0;
+    if (lane == 0 && valid) {
         uint32_t lo = 0, hi = L.n_frames;
         while (hi - lo > 1) {
-            uint32_t mid = (lo + hi) >> 1;
+            const uint32_t mid = (lo + hi) >> 1;
             if (L.frames[mid].blk_off <= gb) lo = mid;
             else hi = mid;
         }
         f = lo;
-        F = &L.frames[f];
+    }
+    f = __shfl_sync(0xffffffffu, f, 0);
+    const DvFrame *F = &L.frames[f];
+    bool failed = false, mode = false;
+    uint32_t local_blk = 0;
+    int4 lv = make_int4(0, 0, 0, 0);
+    if (valid) {
         local_blk = (uint32_t)(gb - F->blk_off);
         valid = L.item_ok[F->item] != 0;
         if (valid) {
             failed = L.seg_err[F->seg_first + local_blk / 30] != 0;
             mode = L.modes[gb] != 0;
-            cval = failed ? 0 : (int32_t)L.coef[gb * 64 + px];
+            if (!failed) lv = reinterpret_cast<const int4 *>(L.coef + gb * 64)[r];  // row r: 8 int16
         }
     }
-    s_c[lb][px] = cval;
-    // C1 of the block: 64 threads = two warps
-    float a = fabsf((float)cval);
+    int32_t *c = s_c[lb];
+    {
+        const int16_t *q = reinterpret_cast<const int16_t *>(&lv);
+        int32_t row[8];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-    if ((px & 31) == 0) s_c1[lb][px >> 5] = a;
-    __syncthreads();
-    const int y = px >> 3, x = px & 7;
-    // pass 1: h[row][x]
-    if (valid && !failed) s_h[lb][y * 8 + x] = dv_row_pass(s_c[lb], mode, y, x);
-    __syncthreads();
+        for (int u = 0; u < 8; u++) row[u] = q[u];
+        reinterpret_cast<int4 *>(c + r * 8)[0] = make_int4(row[0], row[1], row[2], row[3]);
+        reinterpret_cast<int4 *>(c + r * 8)[1] = make_int4(row[4], row[5], row[6], row[7]);
+    }
+    // C1 of the block and whether any AC coefficient is nonzero, over its eight threads
+    float a = 0.0f;
+    bool ac = false;
+    {
+        const int16_t *q = reinterpret_cast<const int16_t *>(&lv);
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            a += fabsf((float)q[u]);
+            ac |= (r | u) != 0 && q[u] != 0;
+        }
+    }
+#pragma unroll
+    for (int o = 1; o < 8; o <<= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    const bool flat = (__ballot_sync(0xffffffffu, ac) & group_mask) == 0;
+    __syncwarp();
+    if (valid && !failed && !flat) dv_row_pass8(c, s_wt, mode, r, s_h[lb] + r * 8);
+    __syncwarp();
     if (!valid) return;
-    uint8_t sample = 0;
-    if (!failed)
-        sample = dv_sample(dv_column_pass(s_h[lb], mode, y, x), s_c1[lb][0] + s_c1[lb][1], s_c[lb], mode, y, x);
+    unsigned long long row;
     // placement (decoder.rs:432-505)
-    uint32_t seg = local_blk / 30, j = local_blk % 30;
-    uint32_t sequence = seg / 27, slot = seg % 27, m = j / 6, bi = j % 6;
+    const uint32_t seg = local_blk / 30, j = local_blk % 30;
+    const uint32_t sequence = seg / 27, slot = seg % 27, m = j / 6, bi = j % 6;
     uint32_t mbx, mby;
     mb_coords(F->pal != 0, F->sequences, sequence, slot, m, &mbx, &mby);
-    uint32_t X = mbx * 8, Y = mby * 8;
-    uint32_t W = F->width, H = F->height, cw = F->cw, ch = F->ch;
+    const uint32_t X = mbx * 8, Y = mby * 8;
+    const uint32_t W = F->width, H = F->height, cw = F->cw, ch = F->ch;
     uint8_t *yp = F->planes, *cbp = F->planes + (size_t)W * H, *crp = cbp + (size_t)cw * ch;
-    uint32_t bx, by;
-    uint8_t *plane;
-    uint32_t pw;
-    bool chroma = bi >= 4;
+    const bool chroma = bi >= 4;
+    if (failed) row = 0x0101010101010101ull * (chroma ? 128u : 16u);
+    else row = dv_row_samples(c, s_h[lb], s_wt, s_v4, mode, r, a, flat, lane & 24, group_mask);
     if (F->pal || mbx >= 88) {
         if (!chroma) {
-            bx = X + (bi & 1) * 8;
-            by = Y + (bi >> 1) * 8;
-            plane = yp;
-            pw = W;
+            store_row8(yp + (size_t)(Y + (bi >> 1) * 8 + r) * W + X + (bi & 1) * 8, row);
         } else {
-            plane = bi == 4 ? crp : cbp;
-            pw = cw;
+            uint8_t *plane = bi == 4 ? crp : cbp;
             if (F->pal) {
-                bx = X / 2;
-                by = Y / 2;
+                store_row8(plane + (size_t)(Y / 2 + r) * cw + X / 2, row);
             } else {  // put_split_chroma: columns 0-3 to rows y.., 4-7 to rows y+8..
-                bx = X / 4 - (x >= 4 ? 4 : 0);
-                by = Y + (x >= 4 ? 8 : 0);
+                store_row4(plane + (size_t)(Y + r) * cw + X / 4, (uint32_t)row);
+                store_row4(plane + (size_t)(Y + 8 + r) * cw + X / 4, (uint32_t)(row >> 32));
             }
         }
     } else {
-        if (!chroma) {
-            bx = X + bi * 8;
-            by = Y;
-            plane = yp;
-            pw = W;
-        } else {
-            plane = bi == 4 ? crp : cbp;
-            pw = cw;
-            bx = X / 4;
-            by = Y;
-        }
+        if (!chroma) store_row8(yp + (size_t)(Y + r) * W + X + bi * 8, row);
+        else store_row8((bi == 4 ? crp : cbp) + (size_t)(Y + r) * cw + X / 4, row);
     }
-    if (failed) sample = chroma ? 128 : 16;
-    plane[(size_t)(by + y) * pw + bx + x] = sample;
 }
 
 }  // namespace
@@ -421,7 +451,7 @@ void launch_dv_decode(const DvLaunch &L, cudaStream_t s) {
 
 void launch_dv_idct(const DvLaunch &L, cudaStream_t s) {
     if (L.n_blocks == 0) return;
-    uint64_t grid = (L.n_blocks + 3) / 4;
+    const uint64_t grid = (L.n_blocks + kIdctBlocks - 1) / kIdctBlocks;
     dv_idct_kernel<<<(unsigned)grid, kIdctThreads, 0, s>>>(L);
 }
 

@@ -128,6 +128,8 @@ def lib():
         vp = ctypes.c_void_p
         for name in ("orc_jpeg_idct_many", "orc_dv_idct88_many", "orc_dv_idct248_many"):
             getattr(L, name).argtypes = [vp, ctypes.c_size_t, vp]
+        L.orc_dv_coefficients.argtypes = [u8p, ctypes.c_size_t, vp, vp, ctypes.c_size_t]
+        L.orc_dv_coefficients.restype = ctypes.c_size_t
         L.orc_jpeg_fdct_quantize_many.argtypes = [vp, vp, ctypes.c_size_t, vp]
         L.orc_jpeg_write_levels.argtypes = [ctypes.POINTER(_JpegLayout), vp, ctypes.c_size_t, vp, ctypes.c_size_t,
                                             ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(_Result)]
@@ -340,3 +342,16 @@ def jpeg_encode(fmt, width, height, planes, quality, annex_k=False, restart_inte
     if st != OK:
         raise ValueError(res.message.decode())
     return bytes(out[:n.value])
+
+
+def dv_coefficients(data: bytes):
+    """(coefficients int32 (n, 64), modes uint8 (n,)) of every block of a DV frame,
+    as decode_segment hands them to the transforms (segment order)."""
+    import numpy as np
+
+    cap = 12 * 27 * 30
+    coef = np.zeros((cap, 64), np.int32)
+    modes = np.zeros(cap, np.uint8)
+    arr, n = _buf(data)
+    got = lib().orc_dv_coefficients(arr, n, coef.ctypes.data, modes.ctypes.data, cap)
+    return coef[:got], modes[:got]

@@ -544,6 +544,12 @@ static void free_blocks(dctblock_t *b, size_t n) {
     for (size_t i = 0; i < n; i++) bits_free(&b[i].partial);
 }
 
+/* Coefficient capture for the transform tests (orc_dv_coefficients): every
+ * decoded block's coefficients and DCT mode, in segment order. */
+static int32_t *g_cap_coef;
+static uint8_t *g_cap_mode;
+static size_t g_cap_n, g_cap_cap;
+
 /* decoder.rs:152-191 decode_segment */
 static int decode_segment(const uint8_t *data, const profile_t *p, const uint8_t *issue_flags, orc_plane planes[3],
                           size_t sequence, size_t slot, orc_result *res) {
@@ -579,6 +585,11 @@ static int decode_segment(const uint8_t *data, const profile_t *p, const uint8_t
                     sequence);
             st = ORC_INVALID_DATA;
             goto done;
+        }
+    if (g_cap_coef)
+        for (int i = 0; i < 30 && g_cap_n < g_cap_cap; i++, g_cap_n++) {
+            memcpy(g_cap_coef + 64 * g_cap_n, blocks[i].coefficients, 64 * sizeof(int32_t));
+            g_cap_mode[g_cap_n] = (uint8_t)(blocks[i].dct_mode != 0);
         }
     {
         size_t xy[5][2];
@@ -642,4 +653,24 @@ int orc_dv_decode(const uint8_t *data, size_t len, int conceal, orc_frame *out, 
     out->plane_count = 3;
     for (int i = 0; i < 3; i++) out->planes[i] = planes[i];
     return ORC_OK;
+}
+
+/* The dequantised coefficients (natural order) and DCT modes of every block of a
+ * frame, as decode_segment hands them to the transforms, in segment order (30
+ * blocks per segment). Returns the number of blocks written (at most cap), or 0
+ * when the frame fails. Not thread-safe (test infrastructure). */
+size_t orc_dv_coefficients(const uint8_t *data, size_t len, int32_t *coef, uint8_t *modes, size_t cap) {
+    orc_frame fr;
+    orc_result res;
+    g_cap_coef = coef;
+    g_cap_mode = modes;
+    g_cap_n = 0;
+    g_cap_cap = cap;
+    int st = orc_dv_decode(data, len, 0, &fr, NULL, 0, NULL, &res);
+    size_t n = g_cap_n;
+    g_cap_coef = NULL;
+    g_cap_mode = NULL;
+    if (st) return 0;
+    orc_frame_free(&fr);
+    return n;
 }

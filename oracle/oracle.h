@@ -116,6 +116,9 @@ int orc_dv_decode(const uint8_t *data, size_t len, int conceal, orc_frame *out,
 int orc_dv_issue_count(const uint8_t *data, size_t len, size_t *count, size_t *first_offset,
                        orc_result *res);
 
+/* Dequantised coefficients and DCT modes of every block of a frame (segment order). */
+size_t orc_dv_coefficients(const uint8_t *data, size_t len, int32_t *coef, uint8_t *modes, size_t cap);
+
 /* decoder.rs:520-548 and 555-602 on one block. */
 void orc_dv_idct88(const int32_t coefficients[64], uint8_t out[64]);
 void orc_dv_idct248(const int32_t coefficients[64], uint8_t out[64]);

@@ -64,27 +64,41 @@ __global__ void __launch_bounds__(kJBlocks * 4) jpeg_idct_blocks(const int32_t *
     if (n_exact) atomicAdd(exact, (unsigned long long)n_exact);
 }
 
-__global__ void __launch_bounds__(256) dv_idct_blocks(const int32_t *c, const uint8_t *modes, uint64_t n,
+// DV: the decode kernel's row-parallel form (dv_idct_kernel), eight threads per
+// block, output in natural order.
+__global__ void __launch_bounds__(256) dv_idct_blocks(const int32_t *coef, const uint8_t *modes, uint64_t n,
                                                       uint8_t *out) {
-    __shared__ int32_t s_c[4][64];
-    __shared__ float s_h[4][64];
-    __shared__ float s_c1[4][2];
-    const int lb = threadIdx.x >> 6, px = threadIdx.x & 63;
-    const uint64_t b = (uint64_t)blockIdx.x * 4 + lb;
+    __shared__ __align__(16) int32_t s_c[32][64];
+    __shared__ __align__(16) float s_h[32][64];
+    __shared__ __align__(16) float s_wt[64];
+    __shared__ __align__(16) float s_v4[16];
+    dv_fill_tables(s_wt, s_v4);
+    __syncthreads();
+    const int lane = threadIdx.x & 31, lb = threadIdx.x >> 3, r = threadIdx.x & 7;
+    const unsigned group_mask = 0xffu << (lane & 24);
+    const uint64_t b = (uint64_t)blockIdx.x * 32 + lb;
     const bool valid = b < n;
-    const int32_t cval = valid ? c[b * 64 + px] : 0;
     const bool mode = valid && modes[b] != 0;
-    s_c[lb][px] = cval;
-    float a = fabsf((float)cval);
+    int32_t *c = s_c[lb];
+    float a = 0.0f;
+    bool ac = false;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-    if ((px & 31) == 0) s_c1[lb][px >> 5] = a;
-    __syncthreads();
-    const int y = px >> 3, x = px & 7;
-    if (valid) s_h[lb][y * 8 + x] = dv_row_pass(s_c[lb], mode, y, x);
-    __syncthreads();
+    for (int u = 0; u < 8; u++) {
+        const int32_t v = valid ? coef[b * 64 + r * 8 + u] : 0;
+        c[r * 8 + u] = v;
+        a += fabsf((float)v);
+        ac |= (r | u) != 0 && v != 0;
+    }
+#pragma unroll
+    for (int o = 1; o < 8; o <<= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    const bool flat = (__ballot_sync(0xffffffffu, ac) & group_mask) == 0;
+    __syncwarp();
+    if (valid && !flat) dv_row_pass8(c, s_wt, mode, r, s_h[lb] + r * 8);
+    __syncwarp();
     if (!valid) return;
-    out[b * 64 + px] = dv_sample(dv_column_pass(s_h[lb], mode, y, x), s_c1[lb][0] + s_c1[lb][1], s_c[lb], mode, y, x);
+    const unsigned long long row = dv_row_samples(c, s_h[lb], s_wt, s_v4, mode, r, a, flat, lane & 24, group_mask);
+#pragma unroll
+    for (int x = 0; x < 8; x++) out[b * 64 + r * 8 + x] = (uint8_t)(row >> (8 * x));
 }
 
 constexpr int kFBlocks = 32;  // FDCT blocks per CTA (8 threads each)
@@ -167,7 +181,7 @@ extern "C" int harness_dv_idct(const int32_t *c, const uint8_t *modes, uint64_t 
     if (e == cudaSuccess) e = upload(&dm, modes, n);
     if (e == cudaSuccess) e = cudaMalloc((void **)&dout, n * 64);
     if (e == cudaSuccess && n) {
-        dv_idct_blocks<<<(unsigned)((n + 3) / 4), 256>>>(dc, dm, n, dout);
+        dv_idct_blocks<<<(unsigned)((n + 31) / 32), 256>>>(dc, dm, n, dout);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaMemcpy(out, dout, n * 64, cudaMemcpyDeviceToHost);
