@@ -22,6 +22,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "exact_fixed.h"
 #include "rounding.h"
 
 namespace mmr {
@@ -77,14 +78,22 @@ __device__ __noinline__ double exact_248(const int32_t *c, int y, int x) {
     return sum / 2.0;
 }
 
-// The sample: the fp32 value's rounding when no half-integer lies within delta of
-// it (c1 = sum |c| of the block), else the reference's binary64 value rounded
-// half away from zero; clamped to 0..255.
-__device__ __forceinline__ uint8_t dv_sample(float value, float c1, const int32_t *c, bool mode248, int y, int x) {
-    const float near = 0.5f - (c1 * 0x1p-21f + 0x1p-30f);
+// The fp32 value's sample when it is certain: no half-integer within delta of
+// the value (c1 = sum |c| of the block), or the value so far beyond 255.5 or
+// below -0.5 that the reference clamps it whatever its rounding (the comparison
+// constants leave room for the fp32 rounding of 256 + delta). -1: undecided.
+__device__ __forceinline__ int dv_decide32(float value, float c1) {
+    const float delta = c1 * 0x1p-21f + 0x1p-30f;
     float r;
     const int32_t v = round_nearest(value, r);
-    if (fabsf(value - r) < near && fabsf(value) < 0x1p22f) return (uint8_t)min(max(v, 0), 255);
+    if (fabsf(value - r) < 0.5f - delta && fabsf(value) < 0x1p22f) return min(max(v, 0), 255);
+    if (value > 256.0f + delta) return 255;
+    if (value < -1.0f - delta) return 0;
+    return -1;
+}
+
+// The reference order for sample (y, x), rounded and clamped.
+__device__ __forceinline__ uint8_t dv_exact_sample(const int32_t *c, bool mode248, int y, int x) {
     const double e = mode248 ? exact_248(c, y, x) : exact_88(c, y, x);
     return (uint8_t)fmin(fmax(round(e), 0.0), 255.0);
 }
@@ -96,8 +105,7 @@ __device__ __forceinline__ uint8_t dv_sample(float value, float c1, const int32_
 // their exact value is a half-integer: every sample would go to the binary64
 // pass one by one.
 __device__ __forceinline__ uint8_t dv_flat_sample(const int32_t *c, bool mode248) {
-    const double e = mode248 ? exact_248(c, 0, 0) : exact_88(c, 0, 0);
-    return (uint8_t)fmin(fmax(round(e), 0.0), 255.0);
+    return dv_exact_sample(c, mode248, 0, 0);
 }
 
 // ---------------------------------------------------------------------------
@@ -190,26 +198,62 @@ __device__ __forceinline__ void dv_column_pass8(const float *h, const float *wt,
     }
 }
 
-// The eight samples of row y of a block, row-parallel: c (the block's
-// coefficients) and h (its pass-1 outputs) in shared memory, c1 = sum |c|, flat
-// = no nonzero AC coefficient (then lane `flat_src` of the warp computes the one
-// reference-order value and broadcasts it; all eight lanes of the group call this
-// together). Returns the samples packed little-endian (x = 0 in the low byte).
-__device__ __forceinline__ unsigned long long dv_row_samples(const int32_t *c, const float *h, const float *wt,
-                                                             const float *v4, bool mode248, int y, float c1,
-                                                             bool flat, int flat_src, unsigned group_mask) {
+// The samples of row y that the fp32 evaluation decides, packed little-endian
+// (x = 0 in the low byte) into *row; returns the undecided ones as bits (x).
+// For a flat block (no nonzero AC coefficient) lane `flat_src` of the warp
+// computes the one reference-order value and broadcasts it (all eight lanes of
+// the block's group call this together).
+__device__ __forceinline__ uint32_t dv_row_fp32(const int32_t *c, const float *h, const float *wt, const float *v4,
+                                                bool mode248, int y, float c1, bool flat, int flat_src,
+                                                unsigned group_mask, unsigned long long *row) {
     if (flat) {
         uint32_t v = 0;
         if ((int)(threadIdx.x & 31) == flat_src) v = dv_flat_sample(c, mode248);
         v = __shfl_sync(group_mask, v, flat_src);
-        return 0x0101010101010101ull * v;
+        *row = 0x0101010101010101ull * v;
+        return 0;
     }
     float value[8];
     dv_column_pass8(h, wt, v4, mode248, y, value);
     unsigned long long out = 0;
+    uint32_t und = 0;
 #pragma unroll
-    for (int x = 0; x < 8; x++) out |= (unsigned long long)dv_sample(value[x], c1, c, mode248, y, x) << (8 * x);
-    return out;
+    for (int x = 0; x < 8; x++) {
+        const int d = dv_decide32(value[x], c1);
+        if (d < 0) und |= 1u << x;
+        else out |= (unsigned long long)d << (8 * x);
+    }
+    *row = out;
+    return und;
+}
+
+// Settles the undecided samples of every lane of the warp (all 32 lanes call
+// this; und = 0 for lanes with none): one sample at a time the whole warp forms
+// its exact fixed-point value (exact_fixed.h), and the owner lane takes it, or
+// the reference order when that value is too close to a half-integer.
+// c: the lane's block coefficients (shared), c1i = sum |c| exactly, fix: the
+// 8-8 table followed by the 2-4-8 table.
+__device__ __forceinline__ void dv_resolve_row(uint32_t und, unsigned long long &row, const int32_t *c,
+                                               bool mode248, int y, int32_t c1i, const long long *fix) {
+    const int lane = threadIdx.x & 31;
+    uint32_t m;
+    while ((m = __ballot_sync(0xffffffffu, und != 0)) != 0) {
+        const int src = __ffs(m) - 1;
+        const uint32_t sund = __shfl_sync(0xffffffffu, und, src);
+        const int x = __ffs(sund) - 1;
+        const int sy = __shfl_sync(0xffffffffu, y, src);
+        const int smode = __shfl_sync(0xffffffffu, mode248 ? 1 : 0, src);
+        const int32_t sc1 = __shfl_sync(0xffffffffu, c1i, src);
+        const int32_t *sc = reinterpret_cast<const int32_t *>(
+            __shfl_sync(0xffffffffu, (unsigned long long)reinterpret_cast<uintptr_t>(c), src));
+        int smp = -1;
+        if (sc1 < kFixMaxC1) smp = fixed_round(fixed_sum(fix + smode * kFixEntries + (sy * 8 + x) * 64, sc), sc1, 0);
+        if (lane == src) {
+            if (smp < 0) smp = dv_exact_sample(c, mode248, y, x);
+            row |= (unsigned long long)smp << (8 * x);
+            und &= und - 1;
+        }
+    }
 }
 
 }  // namespace

@@ -393,25 +393,35 @@ __global__ void __launch_bounds__(kIdctThreads) dv_idct_kernel(DvLaunch L) {
         reinterpret_cast<int4 *>(c + r * 8)[0] = make_int4(row[0], row[1], row[2], row[3]);
         reinterpret_cast<int4 *>(c + r * 8)[1] = make_int4(row[4], row[5], row[6], row[7]);
     }
-    // C1 of the block and whether any AC coefficient is nonzero, over its eight threads
+    // C1 of the block (fp32 for the first decision, exact for the second) and
+    // whether any AC coefficient is nonzero, over its eight threads
     float a = 0.0f;
+    int32_t ai = 0;
     bool ac = false;
     {
         const int16_t *q = reinterpret_cast<const int16_t *>(&lv);
 #pragma unroll
         for (int u = 0; u < 8; u++) {
             a += fabsf((float)q[u]);
+            ai += abs((int32_t)q[u]);
             ac |= (r | u) != 0 && q[u] != 0;
         }
     }
 #pragma unroll
-    for (int o = 1; o < 8; o <<= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    for (int o = 1; o < 8; o <<= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        ai += __shfl_xor_sync(0xffffffffu, ai, o);
+    }
     const bool flat = (__ballot_sync(0xffffffffu, ac) & group_mask) == 0;
+    const bool active = valid && !failed;
     __syncwarp();
-    if (valid && !failed && !flat) dv_row_pass8(c, s_wt, mode, r, s_h[lb] + r * 8);
+    if (active && !flat) dv_row_pass8(c, s_wt, mode, r, s_h[lb] + r * 8);
     __syncwarp();
+    unsigned long long row = 0;
+    uint32_t und = 0;
+    if (active) und = dv_row_fp32(c, s_h[lb], s_wt, s_v4, mode, r, a, flat, lane & 24, group_mask, &row);
+    dv_resolve_row(und, row, c, mode, r, ai, L.fixw);  // every lane of the warp takes part
     if (!valid) return;
-    unsigned long long row;
     // placement (decoder.rs:432-505)
     const uint32_t seg = local_blk / 30, j = local_blk % 30;
     const uint32_t sequence = seg / 27, slot = seg % 27, m = j / 6, bi = j % 6;
@@ -422,7 +432,6 @@ __global__ void __launch_bounds__(kIdctThreads) dv_idct_kernel(DvLaunch L) {
     uint8_t *yp = F->planes, *cbp = F->planes + (size_t)W * H, *crp = cbp + (size_t)cw * ch;
     const bool chroma = bi >= 4;
     if (failed) row = 0x0101010101010101ull * (chroma ? 128u : 16u);
-    else row = dv_row_samples(c, s_h[lb], s_wt, s_v4, mode, r, a, flat, lane & 24, group_mask);
     if (F->pal || mbx >= 88) {
         if (!chroma) {
             store_row8(yp + (size_t)(Y + (bi >> 1) * 8 + r) * W + X + (bi & 1) * 8, row);

@@ -24,6 +24,7 @@
 
 #include "../../include/mmrecode_gpu.h"
 #include "dv_vlc.h"
+#include "exact_fixed.h"
 #include "engine.h"
 #include "last_error.h"
 #include "kernels.h"
@@ -51,7 +52,8 @@ constexpr size_t kOffSegErr = kOffFlags + a256(kDvMaxDif);
 constexpr size_t kOffModes = kOffSegErr + a256(kDvMaxSegments);
 constexpr size_t kOffCoef = kOffModes + a256(kDvMaxSegments * 30);
 constexpr size_t kOffVlc = kOffCoef + a256((size_t)kDvMaxSegments * 30 * 128);
-constexpr size_t kOffMeta = kOffVlc + a256(kVlcMaxEntries * 4);
+constexpr size_t kOffFix = kOffVlc + a256(kVlcMaxEntries * 4);  // DV fixed-point weights (exact_fixed.h)
+constexpr size_t kOffMeta = kOffFix + a256(2 * kFixEntries * sizeof(long long));
 constexpr size_t kMetaBytes = 1024;
 static_assert(kOffMeta + kMetaBytes <= kDvStaticScratchBytes, "DV static scratch layout exceeds the array");
 
@@ -64,9 +66,11 @@ struct Meta {  // per-call plan and state (lives at kOffMeta)
 };
 static_assert(sizeof(Meta) <= kMetaBytes, "DV static metadata exceeds its region");
 
-// The VLC lookup table (dv_vlc.h), filled into a static host array (no heap
-// use) and copied into the scratch at set-up.
+// The VLC lookup table (dv_vlc.h) and the fixed-point transform weights
+// (exact_fixed.h), filled into static host arrays (no heap use) and copied into
+// the scratch at set-up.
 uint32_t g_vlc_host[kVlcMaxEntries];
+long long g_fix_host[2 * kFixEntries];
 
 std::mutex g_setup_mutex;
 uint8_t *g_scratch_ptr[64] = {};  // device address of g_dv_scratch, per device
@@ -88,6 +92,9 @@ cudaError_t setup(int device, uint8_t **ptr, bool redo = false) {
     size_t entries = fill_dv_vlc(g_vlc_host, kVlcMaxEntries);
     if (entries == 0) return cudaErrorInvalidValue;
     e = cudaMemcpy((uint8_t *)p + kOffVlc, g_vlc_host, entries * 4, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return e;
+    build_dv_fixed(g_fix_host, g_fix_host + kFixEntries);
+    e = cudaMemcpy((uint8_t *)p + kOffFix, g_fix_host, sizeof(g_fix_host), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return e;
     g_scratch_ptr[device] = (uint8_t *)p;
     *ptr = (uint8_t *)p;
@@ -204,6 +211,7 @@ mmr_status run_static(const uint8_t *data, size_t len, uint8_t *out, const Probe
     L.coef = reinterpret_cast<int16_t *>(s + kOffCoef);
     L.modes = s + kOffModes;
     L.vlc = reinterpret_cast<const uint32_t *>(s + kOffVlc);
+    L.fixw = reinterpret_cast<const long long *>(s + kOffFix);
     L.n_blocks = (uint64_t)seqs * 27 * 30;
     L.item_ok = &dm->item_ok;
     // the calling thread's default stream: no creation, no allocation, and no

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "dv_vlc.h"
+#include "exact_fixed.h"
 #include "jpeg_syntax.h"
 #include "kernels.h"
 #include "plan.h"
@@ -671,7 +672,8 @@ Probe probe_packet(uint32_t codec, const uint8_t *data, size_t len) {
 struct Engine::Impl {
     DevBuf d_in, d_tok, d_blob, d_tile_tok, d_tile_rst, d_rsts, d_results, d_coef, d_dc, d_planes, d_out, d_dvcoef,
         d_modes, d_flags, d_segerr, d_vlc, d_fix, d_slot_item, d_ivs, d_sync, d_spec, d_prefix, d_events, d_ivkey,
-        d_own, d_match, d_redo, d_scratch, d_scratch_dc, d_blkmap;
+        d_own, d_match, d_redo, d_scratch, d_scratch_dc, d_blkmap,
+        d_fixtab;  // fixed-point transform weights: MJPEG, DV 8-8, DV 2-4-8 (exact_fixed.h)
     PinBuf h_blob, h_back;
     std::vector<uint32_t> vlc;
     // stage boundaries: start, uploads, scan, entropy, idct, dv, rgb, end
@@ -708,6 +710,13 @@ Engine::Engine(int device, int levels) : device_(device), slice_bits_(0), impl_(
     impl_->vlc = build_dv_vlc();
     impl_->d_vlc.ensure(impl_->vlc.size() * 4);
     MMR_CUDA(cudaMemcpy(impl_->d_vlc.ptr, impl_->vlc.data(), impl_->vlc.size() * 4, cudaMemcpyHostToDevice));
+    {
+        std::vector<long long> fix(3 * (size_t)kFixEntries);
+        build_jpeg_fixed(fix.data());
+        build_dv_fixed(fix.data() + kFixEntries, fix.data() + 2 * kFixEntries);
+        impl_->d_fixtab.ensure(fix.size() * sizeof(long long));
+        MMR_CUDA(cudaMemcpy(impl_->d_fixtab.ptr, fix.data(), fix.size() * sizeof(long long), cudaMemcpyHostToDevice));
+    }
 }
 
 Engine::~Engine() {
@@ -1258,6 +1267,7 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
         JL.scratch_blocks = (uint32_t)scratch_blocks;
         JL.scratch_next = reinterpret_cast<unsigned long long *>(db + o_scratch_next);
         JL.blk_map = I.d_blkmap.as<uint32_t>();
+        JL.fixw = I.d_fixtab.as<long long>();
         if (!jframes.empty()) {
             if (n_slots) MMR_CUDA(cudaMemsetAsync(I.d_redo.ptr, 0, n_slots * 4, s));
             if (blocks) MMR_CUDA(cudaMemsetAsync(I.d_blkmap.ptr, 0xff, blocks * 4, s));
@@ -1297,6 +1307,7 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
         DL.coef = I.d_dvcoef.as<int16_t>();
         DL.modes = I.d_modes.as<uint8_t>();
         DL.vlc = I.d_vlc.as<uint32_t>();
+        DL.fixw = I.d_fixtab.as<long long>() + kFixEntries;
         DL.n_blocks = dv_blocks;
         DL.item_ok = JL.item_ok;
         if (!dframes.empty()) {

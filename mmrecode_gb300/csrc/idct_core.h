@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "exact_fixed.h"
 #include "kernels.h"
 #include "rounding.h"
 #include "tables.h"
@@ -70,6 +71,26 @@ __device__ __forceinline__ uint8_t exact_sample(const int32_t *c, int stride, in
     return exact_finish(t, y);
 }
 
+// Settles the samples in `mask` of one block whose exact dequantised coefficients
+// are in c (shared memory; all 32 lanes of the warp call this together): per
+// sample the warp forms the exact fixed-point value (exact_fixed.h, offset +128),
+// and when that is too close to a half-integer lane 0 takes the reference order.
+// put(y, x, sample) runs on lane 0.
+template <class Put>
+__device__ __forceinline__ void settle_samples(const long long *fixw, const int32_t *c, unsigned long long mask,
+                                               Put put) {
+    const int lane = threadIdx.x & 31;
+    long long c1 = llabs((long long)c[lane]) + llabs((long long)c[lane + 32]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c1 += __shfl_xor_sync(0xffffffffu, c1, o);
+    for (; mask; mask &= mask - 1) {
+        const int b = __ffsll((long long)mask) - 1, y = b >> 3, x = b & 7;
+        int smp = -1;
+        if (c1 < kFixMaxC1) smp = fixed_round(fixed_sum(fixw + (y * 8 + x) * 64, c), (int32_t)c1, 128);
+        if (lane == 0) put(y, x, smp >= 0 ? (uint8_t)smp : exact_sample(c, 8, y, x));
+    }
+}
+
 // The 64 levels of block g: in the speculative decode's scratch arena when the
 // block map points there, else in the coefficient arena (any map value past the
 // arena, the reset value included, means in place).
@@ -119,11 +140,25 @@ __device__ __forceinline__ float stage_rows(const int16_t *levels, const int32_t
 // round_nearest (rounding.h) avoids conversion instructions and is exact for
 // |acc| < 2^22. Larger values need no check of their own: |s| <= C1/4 and
 // |acc - s| <= delta give C1 > 2^24 for |acc| >= 2^22, so near < 0 and the
-// sample is unsure already. Returns the unclamped integer sample (+128).
+// rounding is unsure already. A value that far beyond the clamp limits
+// (s + 128 > 255.5 or < -0.5 whatever the rounding; 129 and -130 leave room for
+// the fp32 rounding of the bounds) is decided by the clamp. Returns the
+// unclamped integer sample (+128), or one far outside 0..255 for a clamped one.
 __device__ __forceinline__ int32_t round_sample(float acc, float near, bool &unsure) {
     float r;
     const int32_t v = round_nearest(acc, r) + 128;
     unsure = !(fabsf(acc - r) < near);
+    if (unsure) {
+        const float delta = 0.5f - near;
+        if (acc > 129.0f + delta) {
+            unsure = false;
+            return 1 << 20;
+        }
+        if (acc < -130.0f - delta) {
+            unsure = false;
+            return -(1 << 20);
+        }
+    }
     return v;
 }
 

@@ -10,9 +10,9 @@
 // straight from coefficients into RGB: no planar samples go through HBM.
 //
 // A CTA: NM consecutive MCUs of one MCU row, four threads per block. Samples the
-// fp32 transform cannot decide (idct_core.h) are recomputed in the reference's
-// binary64 order inside the CTA, eight threads per sample (one per pass-1 row),
-// before the colour conversion reads them.
+// fp32 transform cannot decide (idct_core.h) are settled inside the CTA, a warp
+// per block: the exact fixed-point value, or the reference's binary64 order for
+// genuine near-ties (settle_samples), before the colour conversion reads them.
 #include <cuda_runtime.h>
 
 #include "idct_core.h"
@@ -59,11 +59,12 @@ struct FusedSmem {
     __align__(16) float q[3][64];
     unsigned long long mask[Sh::NB];  // samples left to the exact pass, per block
     unsigned long long blk[Sh::NB];
+    int32_t cx[Sh::THREADS / 32][64];  // per warp: exact coefficients of the block it settles
     uint32_t n;
 };
 
 // Converts MCUs mx0 .. mx0+NM-1 of MCU row my of job J to RGB; undecided samples
-// are recomputed in the reference order first, eight threads each.
+// are settled first, a warp per block (settle_samples).
 template <int HM, int VM, int NM>
 __device__ __forceinline__ void fused_tile(const JpegLaunch &L, const FusedLaunch &FL, uint32_t job, uint32_t my,
                                            uint32_t mx0, FusedSmem<HM, VM, NM> &S) {
@@ -115,31 +116,25 @@ __device__ __forceinline__ void fused_tile(const JpegLaunch &L, const FusedLaunc
     __syncthreads();
     const uint32_t n_exact = S.n;
     if (threadIdx.x == 0 && n_exact) atomicAdd(L.fix_count + 1, n_exact);
-    if (n_exact) {
-        const uint32_t grp = threadIdx.x >> 3, v = threadIdx.x & 7, ngrp = blockDim.x >> 3;
-        const unsigned gmask = 0xffu << (threadIdx.x & 24);
-        for (uint32_t b = grp; b < (uint32_t)Sh::NB; b += ngrp) {
-            for (unsigned long long bits = S.mask[b]; bits; bits &= bits - 1) {
-                const uint32_t smp_i = __ffsll((long long)bits) - 1, y = smp_i >> 3, x = smp_i & 7;
-                const uint32_t bm = b / Sh::BPM, bi = b % Sh::BPM;
-                const uint32_t bc = bi < HM * VM ? 0 : bi - HM * VM + 1;
-                const uint64_t bg = S.blk[b];
-                const uint16_t *Q = L.quant + F.quant_off + comps[bc].q * 64;
-                const int16_t *lv = block_levels(L, bg);
-                int32_t crow[8];
-#pragma unroll
-                for (int u = 0; u < 8; u++) crow[u] = (int32_t)lv[v * 8 + u] * (int32_t)Q[v * 8 + u];
-                if (v == 0) crow[0] = L.dc[bg];
-                const double tv = exact_row(crow, (int)x);
-                double t[8];
-#pragma unroll
-                for (int j = 0; j < 8; j++) t[j] = __shfl_sync(gmask, tv, (threadIdx.x & 24) + j);
-                if (v == 0) {
-                    const uint8_t smp = exact_finish(t, (int)y);
-                    if (bc == 0) S.y[((bi / HM) * 8 + y) * Sh::YW + (bm * HM + bi % HM) * 8 + x] = smp;
-                    else S.c[bc - 1][y * Sh::CW + bm * 8 + x] = smp;
-                }
-            }
+    if (n_exact) {  // a warp per block with undecided samples (settle_samples)
+        const uint32_t w = threadIdx.x >> 5, nw = blockDim.x >> 5, lane = threadIdx.x & 31;
+        int32_t *cx = S.cx[w];
+        for (uint32_t b = w; b < (uint32_t)Sh::NB; b += nw) {
+            const unsigned long long bits = S.mask[b];
+            if (!bits) continue;
+            const uint32_t bm = b / Sh::BPM, bi = b % Sh::BPM;
+            const uint32_t bc = bi < HM * VM ? 0 : bi - HM * VM + 1;
+            const uint64_t bg = S.blk[b];
+            const uint16_t *Q = L.quant + F.quant_off + comps[bc].q * 64;
+            const int16_t *lv = block_levels(L, bg);
+            cx[lane] = lane == 0 ? L.dc[bg] : (int32_t)lv[lane] * (int32_t)Q[lane];
+            cx[lane + 32] = (int32_t)lv[lane + 32] * (int32_t)Q[lane + 32];
+            __syncwarp();
+            settle_samples(L.fixw, cx, bits, [&](int y, int x, uint8_t smp) {
+                if (bc == 0) S.y[((bi / HM) * 8 + y) * Sh::YW + (bm * HM + bi % HM) * 8 + x] = smp;
+                else S.c[bc - 1][y * Sh::CW + bm * 8 + x] = smp;
+            });
+            __syncwarp();
         }
     }
     __syncthreads();

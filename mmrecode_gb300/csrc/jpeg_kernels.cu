@@ -575,33 +575,32 @@ __global__ void __launch_bounds__(kIdctThreads, 4) idct_kernel(JpegLaunch L) {
     }
 }
 
-// Exact reference-order recomputation of the queued samples.
+// The queued samples the fp32 transform could not decide, a warp per queued
+// block: its exact coefficients into shared memory, then settle_samples
+// (fixed-point value, or the reference order for genuine near-ties).
 __global__ void __launch_bounds__(256) idct_fixup_kernel(JpegLaunch L) {
+    __shared__ int32_t s_c[8][64];
     const uint32_t n = *L.fix_count;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int32_t *c = s_c[w];
+    for (uint32_t i = blockIdx.x * 8 + w; i < n; i += gridDim.x * 8) {
         const ulonglong2 e = L.fix[i];
         const uint64_t g = e.x;
         const uint32_t r = find_range(L, g);
         const JFrame *F = &L.frames[L.ranges[r].frame];
         const JComp *C = &L.comps[F->comp_off + L.ranges[r].comp];
         const uint16_t *Q = L.quant + F->quant_off + C->q * 64;
-        int32_t c[64];
-        const int4 *src = reinterpret_cast<const int4 *>(block_levels(L, g));
-#pragma unroll
-        for (int k = 0; k < 8; k++) {
-            int4 v = src[k];
-            const int16_t *lv = reinterpret_cast<const int16_t *>(&v);
-#pragma unroll
-            for (int j = 0; j < 8; j++) c[k * 8 + j] = (int32_t)lv[j] * (int32_t)Q[k * 8 + j];
-        }
-        c[0] = L.dc[g];
+        const int16_t *lv = block_levels(L, g);
+        c[lane] = lane == 0 ? L.dc[g] : (int32_t)lv[lane] * (int32_t)Q[lane];
+        c[lane + 32] = (int32_t)lv[lane + 32] * (int32_t)Q[lane + 32];
+        __syncwarp();
         const uint32_t local = (uint32_t)(g - L.ranges[r].first);
         const uint32_t gx = local % C->bw, gy = local / C->bw;
         uint8_t *plane = F->planes + C->out_off;
-        for (unsigned long long m = e.y; m; m &= m - 1) {
-            const int b = __ffsll((long long)m) - 1, y = b >> 3, x = b & 7;
-            plane[(uint64_t)(gy * 8 + y) * C->plane_w + gx * 8 + x] = exact_sample(c, 8, y, x);
-        }
+        settle_samples(L.fixw, c, e.y, [&](int y, int x, uint8_t v) {
+            plane[(uint64_t)(gy * 8 + y) * C->plane_w + gx * 8 + x] = v;
+        });
+        __syncwarp();
     }
 }
 

@@ -63,6 +63,7 @@ struct JpegLaunch {
     uint32_t scratch_blocks;
     unsigned long long *scratch_next;
     uint32_t *blk_map;           // per block (all 0xff per batch); nullptr: levels in place
+    const long long *fixw;       // fixed-point IDCT weights (exact_fixed.h)
 };
 
 constexpr int kSyncPasses = 2;
@@ -116,6 +117,7 @@ struct DvLaunch {
     int16_t *coef;               // 64 per block, natural order
     uint8_t *modes;              // per block: 1 = 2-4-8
     const uint32_t *vlc;         // two-level VLC table
+    const long long *fixw;       // fixed-point transform weights: 8-8 then 2-4-8 (exact_fixed.h)
     uint64_t n_blocks;
     uint32_t *item_ok;
 };

@@ -21,8 +21,8 @@ namespace {
 constexpr int kJBlocks = 32;  // MJPEG blocks per CTA (4 threads each)
 constexpr int kJStride = 68;
 
-__global__ void __launch_bounds__(kJBlocks * 4) jpeg_idct_blocks(const int32_t *c, uint64_t n, uint8_t *out,
-                                                                  unsigned long long *exact) {
+__global__ void __launch_bounds__(kJBlocks * 4) jpeg_idct_blocks(const int32_t *c, uint64_t n, const long long *fixw,
+                                                                  uint8_t *out, unsigned long long *exact) {
     __shared__ __align__(16) float s_f[kJBlocks * kJStride];
     __shared__ __align__(16) uint8_t s_o[kJBlocks * 64];
     const int lb = threadIdx.x >> 2, q = threadIdx.x & 3;
@@ -49,25 +49,36 @@ __global__ void __launch_bounds__(kJBlocks * 4) jpeg_idct_blocks(const int32_t *
 #pragma unroll
     for (int o = 1; o < 4; o <<= 1) mask |= __shfl_xor_sync(0xffffffffu, mask, o);
     __syncwarp();
-    if (!valid) return;
+    // a warp settles the undecided samples of its eight blocks one block at a time,
+    // as the decode kernels do (settle_samples)
+    __shared__ int32_t s_cx[kJBlocks / 8][64];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     uint32_t n_exact = 0;
+    for (int k = 0; k < 8; k++) {
+        const unsigned long long bm = __shfl_sync(0xffffffffu, mask, k * 4);
+        if (!bm) continue;
+        const int blb = w * 8 + k;
+        const uint64_t bb = (uint64_t)blockIdx.x * kJBlocks + blb;
+        s_cx[w][lane] = (int32_t)c[bb * 64 + lane];
+        s_cx[w][lane + 32] = (int32_t)c[bb * 64 + lane + 32];
+        __syncwarp();
+        settle_samples(fixw, s_cx[w], bm, [&](int y, int x, uint8_t v) { s_o[blb * 64 + y * 8 + x] = v; });
+        __syncwarp();
+        n_exact += __popcll(bm);
+    }
+    if (!valid) return;
     for (int row = 0; row < 8; row++)
         for (int side = 0; side < 2; side++) {
             const int col = side ? 7 - q : q;
-            uint8_t v = s_o[lb * 64 + row * 8 + col];
-            if ((mask >> (row * 8 + col)) & 1) {
-                v = exact_sample(c + b * 64, 8, row, col);
-                n_exact++;
-            }
-            out[b * 64 + row * 8 + col] = v;
+            out[b * 64 + row * 8 + col] = s_o[lb * 64 + row * 8 + col];
         }
-    if (n_exact) atomicAdd(exact, (unsigned long long)n_exact);
+    if (lane == 0 && n_exact) atomicAdd(exact, (unsigned long long)n_exact);
 }
 
 // DV: the decode kernel's row-parallel form (dv_idct_kernel), eight threads per
 // block, output in natural order.
 __global__ void __launch_bounds__(256) dv_idct_blocks(const int32_t *coef, const uint8_t *modes, uint64_t n,
-                                                      uint8_t *out) {
+                                                      const long long *fix, uint8_t *out) {
     __shared__ __align__(16) int32_t s_c[32][64];
     __shared__ __align__(16) float s_h[32][64];
     __shared__ __align__(16) float s_wt[64];
@@ -81,22 +92,30 @@ __global__ void __launch_bounds__(256) dv_idct_blocks(const int32_t *coef, const
     const bool mode = valid && modes[b] != 0;
     int32_t *c = s_c[lb];
     float a = 0.0f;
+    int32_t ai = 0;
     bool ac = false;
 #pragma unroll
     for (int u = 0; u < 8; u++) {
         const int32_t v = valid ? coef[b * 64 + r * 8 + u] : 0;
         c[r * 8 + u] = v;
         a += fabsf((float)v);
+        ai += abs(v);
         ac |= (r | u) != 0 && v != 0;
     }
 #pragma unroll
-    for (int o = 1; o < 8; o <<= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    for (int o = 1; o < 8; o <<= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        ai += __shfl_xor_sync(0xffffffffu, ai, o);
+    }
     const bool flat = (__ballot_sync(0xffffffffu, ac) & group_mask) == 0;
     __syncwarp();
     if (valid && !flat) dv_row_pass8(c, s_wt, mode, r, s_h[lb] + r * 8);
     __syncwarp();
+    unsigned long long row = 0;
+    uint32_t und = 0;
+    if (valid) und = dv_row_fp32(c, s_h[lb], s_wt, s_v4, mode, r, a, flat, lane & 24, group_mask, &row);
+    dv_resolve_row(und, row, c, mode, r, ai, fix);
     if (!valid) return;
-    const unsigned long long row = dv_row_samples(c, s_h[lb], s_wt, s_v4, mode, r, a, flat, lane & 24, group_mask);
 #pragma unroll
     for (int x = 0; x < 8; x++) out[b * 64 + r * 8 + x] = (uint8_t)(row >> (8 * x));
 }
@@ -158,17 +177,22 @@ extern "C" int harness_jpeg_idct(const int32_t *c, uint64_t n, uint8_t *out, uns
     int32_t *dc = nullptr;
     uint8_t *dout = nullptr;
     unsigned long long *dex = nullptr;
+    long long *dfix = nullptr;
+    static long long fix[kFixEntries];
+    build_jpeg_fixed(fix);
     cudaError_t e = upload(&dc, c, n * 64);
+    if (e == cudaSuccess) e = upload(&dfix, fix, (size_t)kFixEntries);
     if (e == cudaSuccess) e = cudaMalloc((void **)&dout, n * 64);
     if (e == cudaSuccess) e = cudaMalloc((void **)&dex, 8);
     if (e == cudaSuccess) e = cudaMemset(dex, 0, 8);
     if (e == cudaSuccess && n) {
-        jpeg_idct_blocks<<<(unsigned)((n + kJBlocks - 1) / kJBlocks), kJBlocks * 4>>>(dc, n, dout, dex);
+        jpeg_idct_blocks<<<(unsigned)((n + kJBlocks - 1) / kJBlocks), kJBlocks * 4>>>(dc, n, dfix, dout, dex);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaMemcpy(out, dout, n * 64, cudaMemcpyDeviceToHost);
     if (e == cudaSuccess) e = cudaMemcpy(exact, dex, 8, cudaMemcpyDeviceToHost);
     cudaFree(dc);
+    cudaFree(dfix);
     cudaFree(dout);
     cudaFree(dex);
     return (int)e;
@@ -177,16 +201,21 @@ extern "C" int harness_jpeg_idct(const int32_t *c, uint64_t n, uint8_t *out, uns
 extern "C" int harness_dv_idct(const int32_t *c, const uint8_t *modes, uint64_t n, uint8_t *out) {
     int32_t *dc = nullptr;
     uint8_t *dm = nullptr, *dout = nullptr;
+    long long *dfix = nullptr;
+    static long long fix[2 * kFixEntries];
+    build_dv_fixed(fix, fix + kFixEntries);
     cudaError_t e = upload(&dc, c, n * 64);
     if (e == cudaSuccess) e = upload(&dm, modes, n);
+    if (e == cudaSuccess) e = upload(&dfix, fix, 2 * (size_t)kFixEntries);
     if (e == cudaSuccess) e = cudaMalloc((void **)&dout, n * 64);
     if (e == cudaSuccess && n) {
-        dv_idct_blocks<<<(unsigned)((n + 31) / 32), 256>>>(dc, dm, n, dout);
+        dv_idct_blocks<<<(unsigned)((n + 31) / 32), 256>>>(dc, dm, n, dfix, dout);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaMemcpy(out, dout, n * 64, cudaMemcpyDeviceToHost);
     cudaFree(dc);
     cudaFree(dm);
+    cudaFree(dfix);
     cudaFree(dout);
     return (int)e;
 }
