@@ -354,6 +354,12 @@ void build_lut(const uint8_t *key, size_t key_len, uint32_t sym_off, bool ac, Hu
                     size = sym;
                     ok = size <= 11;
                 }
+                if (ok && l + size > FB) {  // the code alone: the magnitude follows it
+                    const uint32_t e = (size << 16) | kFastCode | (adv << 5) | (uint32_t)l;
+                    const uint32_t base = code << (FB - l);
+                    for (uint32_t j = 0; j < (1u << (FB - l)); j++)
+                        if (!lut->fastv[base + j]) lut->fastv[base + j] = e;
+                }
                 if (ok && l + size <= FB) {
                     const uint32_t rest = FB - l - size;  // bits after the magnitude
                     for (uint32_t m = 0; m < (1u << size); m++) {

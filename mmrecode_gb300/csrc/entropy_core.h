@@ -82,11 +82,20 @@ __device__ __forceinline__ bool decode_symbol(Bits &r, uint32_t avail, const Huf
                                               uint16_t &err, uint32_t &errbit) {
     refill(r);
     const uint32_t fv = __ldg(&T->fastv[r.buf >> (64 - kHuffFastBits)]);
-    const uint32_t total = fv & 31;
+    const uint32_t fl = fv & 31;
     const int kn = (fv & kFastEob) ? 64 : k + (int)((fv >> 5) & 127);
-    if (total - 1u < avail && kn <= 64) {
+    if (fv & kFastCode) {  // code resolved, magnitude after it (receive_extend, entropy.rs:168-182)
+        const uint32_t size = (fv >> 16) & 15, total = fl + size;
+        if (total - 1u < avail && kn <= 64) {
+            const int32_t v = (int32_t)((r.buf << fl) >> (64 - size));
+            val = v < (1 << (size - 1)) ? v + 1 - (1 << size) : v;
+            take(r, (int)total);
+            k = kn;
+            return true;
+        }
+    } else if (fl - 1u < avail && kn <= 64) {
         val = (int32_t)fv >> 16;
-        take(r, (int)total);
+        take(r, (int)fl);
         k = kn;
         return true;
     }

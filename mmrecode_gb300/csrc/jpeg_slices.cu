@@ -49,6 +49,9 @@ constexpr unsigned long long kStGuess = ~0ull - 1;  // start not yet derived fro
 constexpr int kSliceThreads = 128;
 constexpr int kStride = 72;  // int16 per staged block (144 B: conflict-free 16 B rows)
 constexpr int kKeyBits = 26;
+#ifndef MMR_SPEC_CTAS_PER_SM
+#define MMR_SPEC_CTAS_PER_SM 8
+#endif
 
 __device__ __forceinline__ unsigned long long pack_state(unsigned long long p, uint32_t si, uint32_t k) {
     return (p << 16) | (si << 8) | k;
@@ -227,7 +230,7 @@ __device__ __forceinline__ TabIdx tab_idx(const JpegLaunch &L, const JFrame &F, 
 
 // 8 CTAs per SM (64 registers): the pass is latency-bound, so resident warps are
 // what it runs on (at 9 it spills and runs slower)
-__global__ void __launch_bounds__(kSliceThreads, 8) slice_spec_kernel(JpegLaunch L) {
+__global__ void __launch_bounds__(kSliceThreads, MMR_SPEC_CTAS_PER_SM) slice_spec_kernel(JpegLaunch L) {
     __shared__ __align__(16) int16_t s_stage[kSliceThreads * kStride];
     __shared__ uint8_t s_zz[64];
     int16_t *stage = s_stage + threadIdx.x * kStride;

@@ -13,14 +13,17 @@ namespace mmr {
 // code as the reference's length-by-length search.
 constexpr int kHuffFastBits = 11;
 constexpr uint32_t kFastEob = 1u << 12;
+constexpr uint32_t kFastCode = 1u << 13;
 
 struct HuffLut {
     uint16_t fast[512];    // (length << 8) | symbol; 0 when the code is longer than 9 bits or absent
     // Whole symbols within the next 11 bits: value << 16 | eob << 12 | advance << 5 |
     // total bits (code + magnitude). advance moves the coefficient index k: 1 for a
     // DC difference (size 0..11), run + 1 for an AC level (size 1..10), 16 for ZRL;
-    // EOB sets k to 64. 0: slow path (longer symbols, and every symbol the
-    // reference rejects).
+    // EOB sets k to 64. Codes of at most 11 bits whose magnitude bits reach past
+    // them: size << 16 | kFastCode | advance << 5 | code length (the magnitude is
+    // read from the bits after the code). 0: slow path (codes longer than 11 bits,
+    // and every symbol the reference rejects).
     uint32_t fastv[1 << kHuffFastBits];
     int32_t maxcode[18];   // largest code of each length 1..16, -1 if none
     int32_t valptr[18];    // symbol index of a length's first code, minus that code
