@@ -72,10 +72,13 @@ __device__ __forceinline__ uint8_t exact_sample(const int32_t *c, int stride, in
 }
 
 // Settles the samples in `mask` of one block whose exact dequantised coefficients
-// are in c (shared memory; all 32 lanes of the warp call this together): per
-// sample the warp forms the exact fixed-point value (exact_fixed.h, offset +128),
-// and when that is too close to a half-integer lane 0 takes the reference order.
-// put(y, x, sample) runs on lane 0.
+// are in c (shared memory; all 32 lanes of the warp call this together). First
+// the warp forms each sample's exact fixed-point value (exact_fixed.h, offset
+// +128); the samples still too close to a half-integer take the reference
+// order: once for the whole block when it has no nonzero AC coefficient (every
+// M[x][0] is the same literal, so all 64 reference samples are equal: DC-only
+// blocks whose value is a half-integer leave all 64 undecided), else one sample
+// per lane in parallel. put(y, x, sample) may run on any lane.
 template <class Put>
 __device__ __forceinline__ void settle_samples(const long long *fixw, const int32_t *c, unsigned long long mask,
                                                Put put) {
@@ -83,11 +86,37 @@ __device__ __forceinline__ void settle_samples(const long long *fixw, const int3
     long long c1 = llabs((long long)c[lane]) + llabs((long long)c[lane + 32]);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) c1 += __shfl_xor_sync(0xffffffffu, c1, o);
-    for (; mask; mask &= mask - 1) {
-        const int b = __ffsll((long long)mask) - 1, y = b >> 3, x = b & 7;
+    const bool flat = __ballot_sync(0xffffffffu, (lane != 0 && c[lane] != 0) || c[lane + 32] != 0) == 0;
+    unsigned long long left = 0;  // samples for the reference order
+    for (unsigned long long m = mask; m; m &= m - 1) {
+        const int b = __ffsll((long long)m) - 1, y = b >> 3, x = b & 7;
         int smp = -1;
         if (c1 < kFixMaxC1) smp = fixed_round(fixed_sum(fixw + (y * 8 + x) * 64, c), (int32_t)c1, 128);
-        if (lane == 0) put(y, x, smp >= 0 ? (uint8_t)smp : exact_sample(c, 8, y, x));
+        if (smp >= 0) {
+            if (lane == 0) put(y, x, (uint8_t)smp);
+        } else {
+            left |= 1ull << b;
+        }
+    }
+    if (!left) return;
+    if (flat) {
+        uint8_t v = 0;
+        if (lane == 0) v = exact_sample(c, 8, 0, 0);
+        v = (uint8_t)__shfl_sync(0xffffffffu, (uint32_t)v, 0);
+        for (unsigned long long m = left; m; m &= m - 1) {
+            const int b = __ffsll((long long)m) - 1;
+            if (((b ^ lane) & 31) == 0) put(b >> 3, b & 7, v);  // lanes b and b - 32 share the stores
+        }
+        return;
+    }
+    while (left) {  // lane i takes the i-th remaining sample
+        unsigned long long m = left;
+        for (int i = 0; i < lane && m; i++) m &= m - 1;
+        if (m) {
+            const int b = __ffsll((long long)m) - 1;
+            put(b >> 3, b & 7, exact_sample(c, 8, b >> 3, b & 7));
+        }
+        for (int i = 0; i < 32 && left; i++) left &= left - 1;
     }
 }
 
