@@ -689,6 +689,12 @@ def _cpu_leg(pool, jobs, cores, single_seconds):
                            f"(oracle restating the reference decoder)"}
 
 
+def _traffic(figures, kernel, blocks):
+    """ncu DRAM bytes per block of a kernel (profiles/) scaled to the blocks of a launch."""
+    tpb = figures.get(("traffic_bytes_per_block", kernel))
+    return tpb * blocks if tpb else None
+
+
 def small_legs(args, local, pool, cores, m, _lib, peak, peak_kind, figures):
     """Configuration 1 (30 VGA 4:2:0 q75 frames without restart markers, planar) and
     configuration 3 (1000 NTSC DV25 frames, planar): frames/s device-resident and
@@ -773,12 +779,14 @@ def small_legs(args, local, pool, cores, m, _lib, peak, peak_kind, figures):
                                "peak_kind": peak_kind, "unit": "GB/s",
                                "frac": idct_bytes / (st["dv_idct"] / 1e3) / 1e9 / peak,
                                "algorithmic_bytes_per_launch": idct_bytes, "ms_per_launch": st["dv_idct"],
+                               "traffic": _traffic(figures, "dv_idct_kernel", blocks),
                                "issue_active_pct_ncu": figures.get(("issue_active_pct", "dv_idct_kernel"))}
             leg["roofline_segment"] = {"bound": "issue", "kernel": "segment_kernel",
                                        "achieved": seg_bytes / (st["dv_segment"] / 1e3) / 1e9, "peak": peak,
                                        "peak_kind": peak_kind, "unit": "GB/s",
                                        "frac": seg_bytes / (st["dv_segment"] / 1e3) / 1e9 / peak,
                                        "algorithmic_bytes_per_launch": seg_bytes, "ms_per_launch": st["dv_segment"],
+                                       "traffic": _traffic(figures, "segment_kernel", blocks),
                                        "issue_active_pct_ncu": figures.get(("issue_active_pct", "segment_kernel"))}
         if pool is not None:
             ctx.decode_raw(resident)
