@@ -123,6 +123,8 @@ typedef struct mmr_gpu_batch_stats {
     uint64_t slices, slices_redone;
     /* inside dv_ms: DIF identifier check + segment (VLC) decode, then transform + placement */
     double dv_segment_ms, dv_idct_ms;
+    /* of slices_redone, those the final decode redid from their start */
+    uint64_t slices_redone_whole;
 } mmr_gpu_batch_stats;
 
 /*

@@ -86,7 +86,8 @@ class BatchStats(ctypes.Structure):
         ("launches", ctypes.c_uint32)] + [
         (n, ctypes.c_double) for n in ("slice_spec_ms", "slice_sync_ms", "slice_decode_ms")] + [
         ("graph_replays", ctypes.c_uint32), ("slices", ctypes.c_uint64), ("slices_redone", ctypes.c_uint64),
-        ("dv_segment_ms", ctypes.c_double), ("dv_idct_ms", ctypes.c_double)]
+        ("dv_segment_ms", ctypes.c_double), ("dv_idct_ms", ctypes.c_double),
+        ("slices_redone_whole", ctypes.c_uint64)]
 
 
 class TuneEntry(ctypes.Structure):

@@ -586,6 +586,7 @@ MMR_API mmr_status mmr_gpu_last_batch_stats(const mmr_gpu_context *context, mmr_
     stats->slices_redone = t.slices_redone;
     stats->dv_segment_ms = t.dv_segment_ms;
     stats->dv_idct_ms = t.dv_idct_ms;
+    stats->slices_redone_whole = t.slices_redone_whole;
     return finish(MMR_STATUS_OK, "");
 }
 

@@ -678,7 +678,7 @@ Probe probe_packet(uint32_t codec, const uint8_t *data, size_t len) {
 struct Engine::Impl {
     DevBuf d_in, d_tok, d_blob, d_tile_tok, d_tile_rst, d_rsts, d_results, d_coef, d_dc, d_planes, d_out, d_dvcoef,
         d_modes, d_flags, d_segerr, d_vlc, d_fix, d_slot_item, d_ivs, d_sync, d_spec, d_prefix, d_events, d_ivkey,
-        d_own, d_match, d_redo, d_scratch, d_scratch_dc, d_blkmap,
+        d_own, d_match, d_redo, d_work, d_scratch, d_scratch_dc, d_blkmap,
         d_fixtab;  // fixed-point transform weights: MJPEG, DV 8-8, DV 2-4-8 (exact_fixed.h)
     PinBuf h_blob, h_back;
     std::vector<uint32_t> vlc;
@@ -1145,6 +1145,7 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
         I.d_own.ensure(std::max<size_t>(n_slots * sizeof(SliceOwn), 256));
         I.d_match.ensure(std::max<size_t>(n_slots * sizeof(SliceMatch), 256));
         I.d_redo.ensure(std::max<size_t>(n_slots * 4, 256));
+        I.d_work.ensure(std::max<size_t>(n_slots * 4, 256));
         I.d_scratch.ensure(std::max<size_t>(scratch_blocks * 128, 256));
         I.d_scratch_dc.ensure(std::max<size_t>(scratch_blocks * 2, 256));
         I.d_blkmap.ensure(std::max<size_t>(blocks * 4, 256));
@@ -1190,7 +1191,9 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
             o_fcta[v] = blob.add_vec(fcta[v]);
         }
 
-        uint32_t zero_counters[4] = {0, 0, 0, 0};  // fixup entries, exact samples, slices redone, slices
+        // fixup entries, exact samples, slices redone, slices, short redos listed for
+        // the final decode, slices redone whole
+        uint32_t zero_counters[8] = {};
         size_t o_fixcount = blob.add(zero_counters, sizeof(zero_counters));
         uint32_t zero_dirty[2 * kSyncPasses] = {};  // changed-exit counts, then work counters
         size_t o_dirty = blob.add(zero_dirty, sizeof(zero_dirty));
@@ -1207,7 +1210,7 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
         size_t back_ok = n * 4, back_seg = seg_first.back();
         size_t o_b1 = 0, o_b2 = align_up(back_j, 16), o_b3 = align_up(o_b2 + back_d, 16),
                o_b4 = align_up(o_b3 + back_ok, 16), o_b5 = align_up(o_b4 + back_seg, 16);
-        I.h_back.ensure(std::max<size_t>(o_b5 + 12, 256));
+        I.h_back.ensure(std::max<size_t>(o_b5 + 20, 256));
         uint8_t *hb = reinterpret_cast<uint8_t *>(I.h_back.ptr);
 
         // ------------------------------------------------------- launches
@@ -1268,6 +1271,7 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
         JL.own = I.d_own.as<SliceOwn>();
         JL.match = I.d_match.as<SliceMatch>();
         JL.redo = I.d_redo.as<uint32_t>();
+        JL.work = I.d_work.as<uint32_t>();
         JL.scratch = I.d_scratch.as<int16_t>();
         JL.scratch_dc = I.d_scratch_dc.as<int16_t>();
         JL.scratch_blocks = (uint32_t)scratch_blocks;
@@ -1341,7 +1345,7 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
         if (back_d) MMR_CUDA(cudaMemcpyAsync(hb + o_b2, db + o_dstates, back_d, cudaMemcpyDeviceToHost, s));
         if (back_ok) MMR_CUDA(cudaMemcpyAsync(hb + o_b3, db + o_itemok, back_ok, cudaMemcpyDeviceToHost, s));
         if (back_seg) MMR_CUDA(cudaMemcpyAsync(hb + o_b4, I.d_segerr.ptr, back_seg, cudaMemcpyDeviceToHost, s));
-        MMR_CUDA(cudaMemcpyAsync(hb + o_b5, db + o_fixcount + 4, 12, cudaMemcpyDeviceToHost, s));
+        MMR_CUDA(cudaMemcpyAsync(hb + o_b5, db + o_fixcount + 4, 20, cudaMemcpyDeviceToHost, s));
         for (size_t i = 0; i < n; i++) {
             Item &it = items[i];
             if (it.status != kOk || it.out_on_device || !it.out_bytes) continue;
@@ -1387,7 +1391,7 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
                                     &I.d_results, &I.d_coef, &I.d_dc, &I.d_planes, &I.d_out, &I.d_dvcoef, &I.d_modes,
                                     &I.d_flags, &I.d_segerr, &I.d_vlc, &I.d_fix, &I.d_slot_item, &I.d_ivs, &I.d_sync,
                                     &I.d_spec, &I.d_prefix, &I.d_events, &I.d_ivkey, &I.d_own, &I.d_match, &I.d_redo,
-                                    &I.d_scratch, &I.d_scratch_dc, &I.d_blkmap})
+                                    &I.d_work, &I.d_scratch, &I.d_scratch_dc, &I.d_blkmap})
                 key.push_back((uintptr_t)b->ptr);
             for (size_t i = 0; i < n; i++) {
                 const Item &it = items[i];
@@ -1475,6 +1479,7 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
             times->idct_exact_samples = *reinterpret_cast<const uint32_t *>(hb + o_b5);
             times->slices_redone = *reinterpret_cast<const uint32_t *>(hb + o_b5 + 4);
             times->slices = *reinterpret_cast<const uint32_t *>(hb + o_b5 + 8);
+            times->slices_redone_whole = *reinterpret_cast<const uint32_t *>(hb + o_b5 + 16);
             times->dv_blocks = dv_blocks;
             times->rgb_pixels = rgbfirst.back();
             times->input_bytes = 0;

@@ -94,6 +94,7 @@ struct EngineTimes {
     uint32_t graph_replays = 0;       // batches whose launches replayed a captured CUDA graph
     uint64_t slices = 0;              // slices of the chunked entropy decoder
     uint64_t slices_redone = 0;       // of which the final decode pass redid (the rest were placed)
+    uint64_t slices_redone_whole = 0; // of those, redone from their start (no usable speculative part)
 };
 
 class Engine {

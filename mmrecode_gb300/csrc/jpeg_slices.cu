@@ -632,16 +632,16 @@ __device__ __forceinline__ void report(const JpegLaunch &L, const SliceRef &s, u
 // failed, or it is the interval's last slice
 // (its decode reports the interval's completion; a placed last block reports it
 // here). A DC overflow among the placed blocks also sends the whole slice there
-// (reported with its position). Returns true when the final decode pass has
-// work in the slice.
-__device__ bool place_slice(const JpegLaunch &L, uint32_t slot, const SliceRef &s) {
+// (reported with its position). Returns the final decode pass's work in the
+// slice: the leading blocks it writes (0: none, UINT32_MAX: all).
+__device__ uint32_t place_slice(const JpegLaunch &L, uint32_t slot, const SliceRef &s) {
     const SliceSync y = L.sync[slot];
-    if (y.start == kStErr || y.start == kStGuess) return false;  // not reached: nothing to decode
+    if (y.start == kStErr || y.start == kStGuess) return 0;  // not reached: nothing to decode
     const SlicePrefix P = L.prefix[slot];
     const uint32_t B = s.v.blocks;
-    if (P.base >= B) return false;
+    if (P.base >= B) return 0;
     const uint32_t nown = s.last ? B - P.base : min(y.blocks, B - P.base);
-    if (nown == 0) return false;
+    if (nown == 0) return 0;
     const SliceOwn *O = L.own + slot;
     const SliceMatch M = L.match[slot];
     uint32_t spec_first = 0;
@@ -693,7 +693,7 @@ __device__ bool place_slice(const JpegLaunch &L, uint32_t slot, const SliceRef &
     }
     const uint32_t redo = usable ? M.blocks : 0xffffffffu;
     L.redo[slot] = redo;
-    return redo != 0;
+    return redo;
 }
 
 // Adds the lanes' flags to a counter, one atomic per warp.
@@ -702,14 +702,26 @@ __device__ __forceinline__ void count_lanes(uint32_t *counter, bool flag) {
     if ((threadIdx.x & 31) == 0 && m) atomicAdd(counter, (uint32_t)__popc(m));
 }
 
+// Also lists the slots with short work for the final decode (leading blocks, or an
+// interval's last slice, at most kSliceTail bits), so that its warps take those
+// tasks packed and lanes without work do not ride along. Whole slices redone from
+// their start stay in slot order: few and long, they run best spread over the
+// warps (a packed warp of them waits on 32 lanes' loads per step).
 __global__ void __launch_bounds__(kSliceThreads) slice_place_kernel(JpegLaunch L) {
     const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
     SliceRef s;
     const bool valid = slice_ref(L, slot, s);
     count_lanes(L.fix_count + 3, valid);
-    bool redo = false;
+    uint32_t redo = 0;
     if (valid) redo = place_slice(L, slot, s);
-    count_lanes(L.fix_count + 2, redo);
+    count_lanes(L.fix_count + 2, redo != 0);
+    count_lanes(L.fix_count + 5, redo == 0xffffffffu);
+    const uint32_t lane = threadIdx.x & 31;
+    const unsigned shrt = __ballot_sync(0xffffffffu, redo != 0 && (redo != 0xffffffffu || s.last));
+    uint32_t base = 0;
+    if (lane == 0 && shrt) base = atomicAdd(L.fix_count + 4, (uint32_t)__popc(shrt));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (shrt & (1u << lane)) L.work[base + __popc(shrt & ((1u << lane) - 1u))] = slot;
 }
 
 
@@ -725,11 +737,22 @@ __global__ void __launch_bounds__(kSliceThreads) slice_decode_kernel(JpegLaunch 
     for (int q = 0; q < 8; q++) stage4[q] = make_int4(0, 0, 0, 0);
     if (threadIdx.x < 64) s_zz[threadIdx.x] = c_slice_zz[threadIdx.x];
     __syncthreads();
-    const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+    // The first half of the grid takes the short tasks, packed from the work list
+    // (slice_place_kernel); the second half the whole slices redone from their
+    // start, in slot order.
+    const uint32_t half = gridDim.x >> 1;
+    uint32_t slot;
+    if (blockIdx.x < half) {
+        const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+        if (t >= L.fix_count[4]) return;
+        slot = L.work[t];
+    } else {
+        slot = (blockIdx.x - half) * blockDim.x + threadIdx.x;
+    }
     SliceRef s;
     if (!slice_ref(L, slot, s)) return;
     const uint32_t redo = L.redo[slot];  // leading blocks to write; the rest are placed
-    if (!redo) return;
+    if (!redo || (blockIdx.x >= half && (redo != 0xffffffffu || s.last))) return;
     const unsigned long long from = L.sync[slot].start;
     if (from == kStErr || from == kStGuess) return;
     const SlicePrefix P = L.prefix[slot];
@@ -926,7 +949,7 @@ void launch_jpeg_slices(const JpegLaunch &L, cudaStream_t s, cudaEvent_t *marks,
     mark(1);
     if (run) {
         slice_place_kernel<<<grid, kSliceThreads, 0, s>>>(L);
-        slice_decode_kernel<<<grid, kSliceThreads, 0, s>>>(L);
+        slice_decode_kernel<<<2 * grid, kSliceThreads, 0, s>>>(L);
     }
     mark(2);
     if (run) slice_resolve_kernel<<<(L.n_items_small + 127) / 128, 128, 0, s>>>(L);

@@ -38,7 +38,8 @@ struct JpegLaunch {
     uint64_t n_blocks;
     uint32_t *item_ok;           // per batch item: 1 while decoding has not failed
     ulonglong2 *fix;             // blocks the fp32 IDCT could not fully decide: (block, sample mask)
-    uint32_t *fix_count;         // entries, then samples; zero-initialised per batch
+    uint32_t *fix_count;         // entries, samples, slices redone, slices, short redos listed, slices
+                                 // redone whole (8 counters, zeroed per batch)
     uint32_t fixup_grid;         // CTAs of the grid-stride fixup pass
     // chunked entropy decoder (frames with <= 4 components; items [0, n_items_small))
     uint32_t n_slots;
@@ -58,6 +59,7 @@ struct JpegLaunch {
     SliceMatch *match;           // per slot (written by the speculative and sync passes)
     uint32_t *redo;              // per slot: leading owned blocks the final decode pass writes
                                  // (0: none, UINT32_MAX: all; zeroed per batch)
+    uint32_t *work;              // n_slots: slots with short work for the final decode (count in fix_count[4])
     int16_t *scratch;            // 64 levels per scratch block
     int16_t *scratch_dc;         // DC difference per scratch block
     uint32_t scratch_blocks;

@@ -29,6 +29,7 @@ void accumulate_times(EngineTimes &a, const EngineTimes &t) {
     a.graph_replays += t.graph_replays;
     a.slices += t.slices;
     a.slices_redone += t.slices_redone;
+    a.slices_redone_whole += t.slices_redone_whole;
 }
 
 // ------------------------------------------------------------------ pool ---
