@@ -21,21 +21,28 @@ struct Bits {
     int nbits;      // bits held in buf (>= 32 after refill)
     uint64_t buf;   // next bits, MSB first
     uint32_t used;  // bits consumed, counted from the reader's base position
+    uint32_t pf;    // the word after buf's bits, loaded one refill ahead (byte order as stored)
 };
 
 // Reader at token-stream bit `bit`; `used` is the base-relative position there.
+// The token stream has a word of padding past its end, so the one-ahead load of
+// the last word stays inside the buffer.
 __device__ __forceinline__ void bits_init(Bits &r, const uint8_t *tok, unsigned long long bit, uint32_t used) {
     r.words = reinterpret_cast<const uint32_t *>(tok);
     const uint32_t w0 = (uint32_t)(bit >> 5), skip = (uint32_t)bit & 31;
     r.buf = (uint64_t)bswap32(__ldg(r.words + w0)) << (32 + skip);
+    r.pf = __ldg(r.words + w0 + 1);
     r.nbits = 32 - (int)skip;
-    r.wpos = w0 + 1;
+    r.wpos = w0 + 2;
     r.used = used;
 }
 
+// Tops buf up to at least 33 bits from the prefetched word and starts the load
+// of the next one, which the refill after this one uses (about 32 bits later).
 __device__ __forceinline__ void refill(Bits &r) {
     if (r.nbits <= 32) {
-        r.buf |= (uint64_t)bswap32(__ldg(r.words + r.wpos)) << (32 - r.nbits);
+        r.buf |= (uint64_t)bswap32(r.pf) << (32 - r.nbits);
+        r.pf = __ldg(r.words + r.wpos);
         r.wpos++;
         r.nbits += 32;
     }
