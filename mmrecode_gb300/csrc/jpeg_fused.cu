@@ -138,15 +138,60 @@ __device__ __forceinline__ void fused_tile(const JpegLaunch &L, const FusedLaunc
         }
     }
     __syncthreads();
-    // colour conversion (terminal_preview.rs:7308-7330, full range), four pixels per
-    // thread: one 32-bit luma load, three 32-bit words of RGB. Rows whose bytes
-    // start 4-aligned (width a multiple of 4, aligned output) are stored straight
-    // from registers, consecutive threads writing consecutive words; others go
-    // through a shared-memory tile and a byte-exact copy. Pixels past the visible
-    // width are computed from padding and never stored.
+    // colour conversion (terminal_preview.rs:7308-7330, full range). When every row
+    // starts 16-byte aligned (width a multiple of 16, aligned output; x0 is a
+    // multiple of 64 pixels) a thread converts 16 pixels from one 16-byte luma
+    // load and stores them as three 16-byte vectors, consecutive threads writing
+    // consecutive 48-byte runs. Otherwise four pixels per thread: one 32-bit luma
+    // load, three 32-bit words of RGB, stored straight from registers when rows
+    // start 4-aligned, else through a shared-memory tile and a byte-exact copy.
+    // Pixels past the visible width are computed from padding and never stored.
     const uint32_t x0 = mx0 * HM * 8, y0 = my * VM * 8;
     const uint32_t vis_w = min((uint32_t)(nm * HM * 8), J.width - x0);
     const uint32_t vis_h = min((uint32_t)Sh::YH, J.height - y0);
+    if ((((reinterpret_cast<uintptr_t>(J.out) | J.width | vis_w) & 15) == 0)) {  // uniform over the CTA
+        for (uint32_t p = threadIdx.x; p < vis_h * (Sh::YW / 16); p += blockDim.x) {
+            const uint32_t ly = p / (Sh::YW / 16), lx = (p - ly * (Sh::YW / 16)) * 16;
+            if (lx >= vis_w) continue;
+            const uint4 yv = *reinterpret_cast<const uint4 *>(S.y + ly * Sh::YW + lx);
+            const uint8_t *cbr = S.c[0] + (ly / VM) * Sh::CW + lx / HM;
+            const uint8_t *crr = S.c[1] + (ly / VM) * Sh::CW + lx / HM;
+            uint32_t cb[4], cr[4];  // the 16 / HM chroma bytes of the 16 pixels
+            if (HM == 2) {
+                const uint2 a = *reinterpret_cast<const uint2 *>(cbr), b = *reinterpret_cast<const uint2 *>(crr);
+                cb[0] = a.x, cb[1] = a.y, cr[0] = b.x, cr[1] = b.y;
+                cb[2] = cb[3] = cr[2] = cr[3] = 0;
+            } else {
+                const uint4 a = *reinterpret_cast<const uint4 *>(cbr), b = *reinterpret_cast<const uint4 *>(crr);
+                cb[0] = a.x, cb[1] = a.y, cb[2] = a.z, cb[3] = a.w;
+                cr[0] = b.x, cr[1] = b.y, cr[2] = b.z, cr[3] = b.w;
+            }
+            const uint32_t ys[4] = {yv.x, yv.y, yv.z, yv.w};
+            uint32_t word[12];
+#pragma unroll
+            for (int g = 0; g < 4; g++) {
+                int32_t ch[12];
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    const int px = 4 * g + k, ci = px / HM;
+                    const int32_t Y = (int32_t)((ys[g] >> (8 * k)) & 0xff);
+                    const int32_t u = (int32_t)((cb[ci >> 2] >> (8 * (ci & 3))) & 0xff) - 128;
+                    const int32_t w = (int32_t)((cr[ci >> 2] >> (8 * (ci & 3))) & 0xff) - 128;
+                    ch[3 * k + 0] = Y + ((359 * w + 128) >> 8);
+                    ch[3 * k + 1] = Y - ((88 * u + 183 * w + 128) >> 8);
+                    ch[3 * k + 2] = Y + ((454 * u + 128) >> 8);
+                }
+#pragma unroll
+                for (int j = 0; j < 3; j++)
+                    word[3 * g + j] = pack4_sat_u8(ch[4 * j], ch[4 * j + 1], ch[4 * j + 2], ch[4 * j + 3]);
+            }
+            uint4 *o = reinterpret_cast<uint4 *>(J.out + ((uint64_t)(y0 + ly) * J.width + x0 + lx) * 3);
+            o[0] = make_uint4(word[0], word[1], word[2], word[3]);
+            o[1] = make_uint4(word[4], word[5], word[6], word[7]);
+            o[2] = make_uint4(word[8], word[9], word[10], word[11]);
+        }
+        return;
+    }
     const bool direct = ((reinterpret_cast<uintptr_t>(J.out) | J.width) & 3) == 0;
     for (uint32_t p = threadIdx.x; p < vis_h * (Sh::YW / 4); p += blockDim.x) {
         const uint32_t ly = p / (Sh::YW / 4), lx = (p - ly * (Sh::YW / 4)) * 4;

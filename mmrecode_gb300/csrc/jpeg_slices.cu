@@ -268,8 +268,8 @@ __global__ void __launch_bounds__(kSliceThreads, MMR_SPEC_CTAS_PER_SM) slice_spe
     unsigned long long nominal;
     uint32_t S;  // this slice's length
     slice_span(s, F.slice_bits, nominal, S);
-    // a guessed decode starts up to kSpecLead bits early; positions below are from p0
-    const uint32_t lead = guess ? (uint32_t)min((unsigned long long)kSpecLead, nominal) : 0;
+    // a guessed decode starts up to spec_lead(S) bits early; positions below are from p0
+    const uint32_t lead = guess ? (uint32_t)min((unsigned long long)spec_lead(F.slice_bits), nominal) : 0;
     const unsigned long long p0 = nominal - lead;
     const uint32_t end = S + lead;
     auto mark_at = [&](uint32_t qq) {

@@ -134,14 +134,19 @@ struct SlicePoint {
 };
 
 // Checkpoints 64, 128, 256, 512, 768, 1024, 1536 and 2048 bits into a slice
-// (those inside it). The speculative decode of a slice starts kSpecLead bits
+// (those inside it). The speculative decode of a slice starts spec_lead(S) bits
 // before the slice: the synchronisation distance of Huffman-coded JPEG data is a
-// few hundred bits, so it has usually met the true decode by the first
-// checkpoint, and a re-decode from the predecessor's exit matches there after a
-// few symbols; the later ones bound how far the final decode pass must redo a
-// slice whose speculative decode met the true one late.
+// few hundred bits (longer where the MCU's block phase must also fall into
+// place), so it has usually met the true decode by the first checkpoint, and a
+// re-decode from the predecessor's exit matches there after a few symbols; the
+// later ones bound how far the final decode pass must redo a slice whose
+// speculative decode met the true one late. Short slices take a longer lead
+// relative to their length: their sync passes and serial fix-up cost more than
+// the extra decoding (measured: 1024-bit slices of 4:2:0 VGA frames 512 -> 1024
+// bits, 1.29 -> 1.14 ms per 30 frames; 4096-bit slices of 4:2:2 1080p frames
+// 512 -> 768 bits, 5.71 -> 5.68 ms of entropy decode per 300 frames).
 constexpr int kSliceCheckpoints = 8;
-constexpr uint32_t kSpecLead = 512;
+__host__ __device__ constexpr uint32_t spec_lead(uint32_t slice_bits) { return slice_bits <= 2048 ? 1024u : 768u; }
 
 struct SliceSpec {
     SlicePoint exit;                      // end of the speculative decode
