@@ -508,6 +508,9 @@ __device__ bool resync_slice(const JpegLaunch &L, uint32_t slot, const SliceRef 
 // lanes that reach the counter together take consecutive slots with one atomic
 // (one per slot serialised on the counter's address).
 __global__ void __launch_bounds__(kSliceThreads) slice_sync_kernel(JpegLaunch L, uint32_t pass) {
+    // a pass after one that changed no exit state has nothing to do: every start
+    // then equals its predecessor's exit
+    if (pass > 0 && *(volatile const uint32_t *)&L.sync_dirty[pass - 1] == 0) return;
     uint32_t *next = L.sync_dirty + kSyncPasses + pass;
     const uint32_t lane = threadIdx.x & 31;
     for (;;) {

@@ -68,7 +68,11 @@ struct JpegLaunch {
     const long long *fixw;       // fixed-point IDCT weights (exact_fixed.h)
 };
 
-constexpr int kSyncPasses = 2;
+// Parallel sync passes before the serial fix-up walk; a pass after one that changed
+// nothing returns at once (measured: 4 passes take VGA 4:2:0 restart-less frames
+// from 0.49 to 0.42 ms of sync per 30 frames and cost 1080p batches nothing; 6 are
+// slower again)
+constexpr int kSyncPasses = 4;
 
 void launch_jpeg_scan(const JpegLaunch &L, cudaStream_t s);
 void launch_jpeg_entropy(const JpegLaunch &L, cudaStream_t s);   // frames with > 4 components
