@@ -2,10 +2,11 @@
 //
 //   dif_check  one thread per 80-byte DIF block: identifier vs canonical layout
 //              (crates/codecs/dv/src/dif.rs:181-253).
-//   segment    one thread per video segment (5 macroblocks, 30 blocks):
+//   segment    a CTA per four video segments (5 macroblocks, 30 blocks each):
 //              DC/mode/class fields, VLC decode and the three-level spill of
-//              unused bits -- block region, macroblock pool, segment pool
-//              (dv/src/decoder.rs:152-317); writes dequantised coefficients.
+//              unused bits -- block region (a thread per block), macroblock pool
+//              (a thread per macroblock), segment pool (a thread per segment)
+//              (dv/src/decoder.rs:152-317); writes every dequantised coefficient.
 //   resolve    first failing segment per frame (sequential semantics).
 //   idct       one thread per sample: fp32 separable 8-8 / 2-4-8 transform with
 //              a proven error bound; samples within it of a rounding boundary
@@ -182,98 +183,174 @@ __device__ void consume_ac(DvBlock &b, const uint32_t *buf, uint32_t &pos, uint3
     }
 }
 
-constexpr int kSegThreads = 64;
+// A CTA per four video segments (dv/src/decoder.rs:152-317), in the reference's
+// three levels, each level's independent parts in parallel:
+//   1. a thread per block (120): DC/mode/class and the AC codes inside the
+//      block's own region of its macroblock's payload;
+//   2. a thread per macroblock (20): the leftover bits of its complete blocks, in
+//      block order, make the macroblock pool, which its incomplete blocks
+//      consume in order (decode_macroblock, decoder.rs:193-243);
+//   3. a thread per segment (4): the macroblock pools' leftovers, in macroblock
+//      order, make the segment pool, which the segment's incomplete blocks
+//      consume in order (consume_pool_for_macroblocks, decoder.rs:225-233).
+// Payload, pools and dequantised coefficients stay in shared memory; every
+// block's 64 coefficients (zeros included) then leave as 16-byte stores.
+constexpr int kSegPerCta = 4;
+constexpr int kSegBlocks = kSegPerCta * 30;
+constexpr int kSegThreads = 128;
+
+struct SegSmem {
+    __align__(16) int16_t coef[kSegBlocks][64];
+    uint32_t pay[kSegPerCta][5 * 19 + 1];  // payload words of the five macroblocks (+1: reads past the end)
+    uint32_t mbpool[kSegPerCta * 5][20];
+    uint32_t segpool[kSegPerCta][5 * 19 + 2];
+    DvBlock blk[kSegBlocks];
+    uint16_t left_start[kSegBlocks], left_len[kSegBlocks];  // unused bits of a complete block's region
+    uint16_t mb_pos[kSegPerCta * 5], mb_len[kSegPerCta * 5];
+    uint32_t dif_off[kSegPerCta * 5];  // byte offset of each macroblock's DIF block in the frame
+    uint32_t frame[kSegPerCta], local[kSegPerCta];
+    uint8_t qno[kSegPerCta * 5];
+    uint8_t bad[kSegBlocks];
+    uint16_t kind[kSegPerCta];
+};
 
 __global__ void __launch_bounds__(kSegThreads) segment_kernel(DvLaunch L) {
-    uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= L.n_segments) return;
-    uint32_t f = upper_index32(L.seg_first, L.n_frames, g);
-    const DvFrame &F = L.frames[f];
-    uint32_t local = g - L.seg_first[f];
-    uint32_t sequence = local / 27, slot = local % 27;
-    uint16_t kind = kDiagNone;
-
-    uint32_t dif[5];
-    for (int m = 0; m < 5; m++) {
-        uint32_t vn = slot * 5 + m;
-        dif[m] = sequence * 150 + 7 + (vn / 15) * 16 + vn % 15;
-        if (kind == kDiagNone && L.flags[F.dif_first + dif[m]]) kind = kDvDamagedId;
+    __shared__ SegSmem S;
+    const uint32_t t = threadIdx.x;
+    const uint32_t g0 = blockIdx.x * kSegPerCta;
+    // segment records: frame, segment in frame, DIF blocks, damaged identifiers
+    if (t < (uint32_t)kSegPerCta) {
+        const uint32_t g = g0 + t;
+        uint16_t kind = 0xffff;  // no segment
+        if (g < L.n_segments) {
+            const uint32_t f = upper_index32(L.seg_first, L.n_frames, g);
+            const DvFrame &F = L.frames[f];
+            const uint32_t local = g - L.seg_first[f];
+            const uint32_t sequence = local / 27, slot = local % 27;
+            kind = kDiagNone;
+            for (int m = 0; m < 5; m++) {
+                const uint32_t vn = slot * 5 + m;
+                const uint32_t dif = sequence * 150 + 7 + (vn / 15) * 16 + vn % 15;
+                if (kind == kDiagNone && L.flags[F.dif_first + dif]) kind = kDvDamagedId;
+                S.dif_off[t * 5 + m] = dif * 80;
+                S.qno[t * 5 + m] = F.in[(size_t)dif * 80 + 3] & 0x0f;
+            }
+            S.frame[t] = f;
+            S.local[t] = local;
+        }
+        S.kind[t] = kind;
     }
-    if (kind == kDiagNone) {
-        // payload words of the 5 macroblocks (bytes 4..80 of each DIF block)
-        uint32_t pay[5 * 19 + 1];
-        for (int m = 0; m < 5; m++) {
-            const uint8_t *src = F.in + (size_t)dif[m] * 80 + 4;
-            for (int i = 0; i < 19; i++)
-                pay[m * 19 + i] = ((uint32_t)src[4 * i] << 24) | ((uint32_t)src[4 * i + 1] << 16) |
-                                  ((uint32_t)src[4 * i + 2] << 8) | (uint32_t)src[4 * i + 3];
+    __syncthreads();
+    // payload words (bytes 4..80 of each DIF block), big-endian
+    for (uint32_t i = t; i < (uint32_t)kSegPerCta * 96; i += kSegThreads) {
+        const uint32_t sg = i / 96, wi = i % 96;
+        uint32_t v = 0;
+        if (wi < 95 && S.kind[sg] == kDiagNone) {
+            const uint32_t m = wi / 19;
+            const uint8_t *src = L.frames[S.frame[sg]].in + S.dif_off[sg * 5 + m] + 4 + (wi % 19) * 4;
+            v = ((uint32_t)src[0] << 24) | ((uint32_t)src[1] << 16) | ((uint32_t)src[2] << 8) | (uint32_t)src[3];
         }
-        pay[95] = 0;
-        uint32_t segpool[5 * 19 + 2];
-        for (int i = 0; i < 97; i++) segpool[i] = 0;
+        S.pay[sg][wi] = v;
+    }
+    for (uint32_t i = t; i < (uint32_t)kSegBlocks * 8; i += kSegThreads)
+        reinterpret_cast<int4 *>(&S.coef[0][0])[i] = make_int4(0, 0, 0, 0);
+    for (uint32_t i = t; i < (uint32_t)kSegPerCta * 5 * 20; i += kSegThreads) (&S.mbpool[0][0])[i] = 0;
+    for (uint32_t i = t; i < (uint32_t)kSegPerCta * 97; i += kSegThreads) (&S.segpool[0][0])[i] = 0;
+    __syncthreads();
+    // 1. a thread per block: its own region
+    if (t < (uint32_t)kSegBlocks) {
+        const uint32_t sg = t / 30, b = t % 30, m = b / 6, bi = b % 6;
+        DvBlock &B = S.blk[t];
+        B.position = 0;
+        B.complete = 0;
+        B.mode = 0;
+        B.cls = 0;
+        B.pval = 0;
+        B.plen = 0;
+        B.pad = 0;
+        uint16_t ls = 0, ll = 0;
+        bool bad = false;
+        if (S.kind[sg] == kDiagNone) {
+            const uint32_t *w = S.pay[sg] + m * 19;
+            const uint32_t r0 = bi < 4 ? bi * 112 : 448 + (bi - 4) * 80, bits = bi < 4 ? 112 : 80;
+            const uint32_t head = get32(w, r0) >> 20;  // 12 bits: dc(9) mode(1) class(2)
+            int32_t dc = (int32_t)(head >> 3);
+            if (dc & 0x100) dc -= 512;
+            B.mode = (head >> 2) & 1;
+            B.cls = head & 3;
+            S.coef[t][0] = (int16_t)(dc * 4 + 1024);
+            uint32_t pos = r0 + 12;
+            const uint32_t end = r0 + bits;
+            consume_ac(B, w, pos, end, S.coef[t], S.qno[sg * 5 + m], L.vlc, bad);
+            if (B.complete) {
+                ls = (uint16_t)pos;
+                ll = (uint16_t)(end - pos);
+            }
+        }
+        S.left_start[t] = ls;
+        S.left_len[t] = ll;
+        S.bad[t] = bad ? 1 : 0;
+    }
+    __syncthreads();
+    // 2. a thread per macroblock: its pool
+    if (t < (uint32_t)kSegPerCta * 5) {
+        const uint32_t sg = t / 5, m = t % 5;
+        uint32_t pos = 0, mbn = 0;
+        if (S.kind[sg] == kDiagNone) {
+            const uint32_t *w = S.pay[sg] + m * 19;
+            const uint32_t j0 = sg * 30 + m * 6;
+            for (uint32_t j = j0; j < j0 + 6; j++)
+                if (S.blk[j].complete) append_bits(S.mbpool[t], mbn, w, S.left_start[j], S.left_len[j]);
+            bool bad = false;
+            for (uint32_t j = j0; j < j0 + 6; j++)
+                if (!S.blk[j].complete && pos < mbn)
+                    consume_ac(S.blk[j], S.mbpool[t], pos, mbn, S.coef[j], S.qno[t], L.vlc, bad);
+            if (bad) S.bad[j0] = 1;
+        }
+        S.mb_pos[t] = (uint16_t)pos;
+        S.mb_len[t] = (uint16_t)mbn;
+    }
+    __syncthreads();
+    // 3. a thread per segment: its pool, then its result
+    if (t < (uint32_t)kSegPerCta && S.kind[t] == kDiagNone) {
         uint32_t segn = 0;
-        DvBlock blk[30];
-        int16_t *coef = L.coef + (F.blk_off + (uint64_t)local * 30) * 64;
-        bool bad_vlc = false;
-        const uint32_t kRegion[6] = {0, 112, 224, 336, 448, 528};
-        const uint32_t kBits[6] = {112, 112, 112, 112, 80, 80};
-        for (int m = 0; m < 5; m++) {
-            // decode_macroblock (decoder.rs:193-223)
-            uint32_t qno = F.in[(size_t)dif[m] * 80 + 3] & 0x0f;
-            const uint32_t *w = pay + m * 19;
-            uint32_t mbpool[20];
-            for (int i = 0; i < 20; i++) mbpool[i] = 0;
-            uint32_t mbn = 0;
-            for (int j = 0; j < 6; j++) {
-                DvBlock &b = blk[m * 6 + j];
-                uint32_t r0 = kRegion[j];
-                uint32_t head = get32(w, r0) >> 20;  // 12 bits: dc(9) mode(1) class(2)
-                int32_t dc = (int32_t)(head >> 3);
-                if (dc & 0x100) dc -= 512;
-                b.position = 0;
-                b.complete = 0;
-                b.mode = (head >> 2) & 1;
-                b.cls = head & 3;
-                b.pval = 0;
-                b.plen = 0;
-                int16_t *bc = coef + (m * 6 + j) * 64;
-                bc[0] = (int16_t)(dc * 4 + 1024);
-                uint32_t pos = r0 + 12, end = r0 + kBits[j];
-                consume_ac(b, w, pos, end, bc, qno, L.vlc, bad_vlc);
-                if (b.complete) append_bits(mbpool, mbn, w, pos, end - pos);
-            }
-            // consume_pool over the macroblock (decoder.rs:235-243)
-            uint32_t pos = 0;
-            for (int j = 0; j < 6; j++) {
-                DvBlock &b = blk[m * 6 + j];
-                if (!b.complete && pos < mbn)
-                    consume_ac(b, mbpool, pos, mbn, coef + (m * 6 + j) * 64, qno, L.vlc, bad_vlc);
-            }
-            if (pos < mbn) append_bits(segpool, segn, mbpool, pos, mbn - pos);
+        for (uint32_t m = 0; m < 5; m++) {
+            const uint32_t k = t * 5 + m;
+            if (S.mb_pos[k] < S.mb_len[k])
+                append_bits(S.segpool[t], segn, S.mbpool[k], S.mb_pos[k], S.mb_len[k] - S.mb_pos[k]);
         }
-        // consume_pool_for_macroblocks (decoder.rs:225-233)
         uint32_t pos = 0;
-        for (int j = 0; j < 30; j++) {
-            DvBlock &b = blk[j];
-            if (!b.complete && pos < segn) {
-                uint32_t qno = F.in[(size_t)dif[j / 6] * 80 + 3] & 0x0f;
-                consume_ac(b, segpool, pos, segn, coef + j * 64, qno, L.vlc, bad_vlc);
-            }
+        bool bad = false;
+        for (uint32_t j = 0; j < 30; j++) {
+            const uint32_t jj = t * 30 + j;
+            if (!S.blk[jj].complete && pos < segn)
+                consume_ac(S.blk[jj], S.segpool[t], pos, segn, S.coef[jj], S.qno[t * 5 + j / 6], L.vlc, bad);
         }
-        if (bad_vlc) kind = kDvBadVlc;
+        for (uint32_t j = 0; j < 30; j++) bad |= S.bad[t * 30 + j] != 0;
+        uint16_t kind = kDiagNone;
+        if (bad) kind = kDvBadVlc;
         else
-            for (int j = 0; j < 30; j++)
-                if (!blk[j].complete) {
+            for (uint32_t j = 0; j < 30; j++)
+                if (!S.blk[t * 30 + j].complete) {
                     kind = kDvIncomplete;
                     break;
                 }
-        uint8_t *modes = L.modes + F.blk_off + (uint64_t)local * 30;
-        for (int j = 0; j < 30; j++) modes[j] = blk[j].mode;
+        S.kind[t] = kind;
     }
-    L.seg_err[g] = (uint8_t)kind;
-    if (kind != kDiagNone) {
-        atomicMin(&L.states[f].bad_segment, local);
-        atomicAdd(&L.states[f].failed, 1u);
+    __syncthreads();
+    // coefficients out (the CTA's segments are consecutive: blocks g0 * 30 ..), modes, results
+    const uint32_t n_seg = min((uint32_t)kSegPerCta, L.n_segments - g0);
+    int4 *dst = reinterpret_cast<int4 *>(L.coef + (uint64_t)g0 * 30 * 64);
+    const int4 *src = reinterpret_cast<const int4 *>(&S.coef[0][0]);
+    for (uint32_t i = t; i < n_seg * 30 * 8; i += kSegThreads) dst[i] = src[i];
+    if (t < n_seg * 30) L.modes[(uint64_t)g0 * 30 + t] = S.blk[t].mode;
+    if (t < n_seg) {
+        const uint16_t kind = S.kind[t];
+        L.seg_err[g0 + t] = (uint8_t)kind;
+        if (kind != kDiagNone) {
+            atomicMin(&L.states[S.frame[t]].bad_segment, S.local[t]);
+            atomicAdd(&L.states[S.frame[t]].failed, 1u);
+        }
     }
 }
 
@@ -454,7 +531,7 @@ __global__ void __launch_bounds__(kIdctThreads) dv_idct_kernel(DvLaunch L) {
 
 void launch_dv_decode(const DvLaunch &L, cudaStream_t s) {
     if (L.n_dif) dif_check_kernel<<<(L.n_dif + 255) / 256, 256, 0, s>>>(L);
-    if (L.n_segments) segment_kernel<<<(L.n_segments + kSegThreads - 1) / kSegThreads, kSegThreads, 0, s>>>(L);
+    if (L.n_segments) segment_kernel<<<(L.n_segments + kSegPerCta - 1) / kSegPerCta, kSegThreads, 0, s>>>(L);
     if (L.n_frames) dv_resolve_kernel<<<(L.n_frames + 127) / 128, 128, 0, s>>>(L);
 }
 

@@ -219,8 +219,7 @@ mmr_status run_static(const uint8_t *data, size_t len, uint8_t *out, const Probe
     cudaStream_t st = cudaStreamPerThread;
     e = cudaMemcpyAsync(s + kOffIn, data, len, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dm, &meta, sizeof(meta), cudaMemcpyHostToDevice, st);
-    // the segment decoder writes only non-zero coefficients
-    if (e == cudaSuccess) e = cudaMemsetAsync(s + kOffCoef, 0, L.n_blocks * 128, st);
+    // (the segment decoder writes every coefficient of every block)
     if (e == cudaSuccess) {
         launch_dv_decode(L, st);
         launch_dv_idct(L, st);

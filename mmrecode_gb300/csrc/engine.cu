@@ -1224,7 +1224,6 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
             if (planned && !items[i].dev_data && items[i].len)
                 MMR_CUDA(cudaMemcpyAsync(d_in + in_off[i], items[i].data, items[i].len, cudaMemcpyHostToDevice, s));
         }
-        if (dv_blocks) MMR_CUDA(cudaMemsetAsync(I.d_dvcoef.ptr, 0, dv_blocks * 128, s));
         MMR_CUDA(record_event(I.ev[1], s, capturing));
 
         JpegLaunch JL;
