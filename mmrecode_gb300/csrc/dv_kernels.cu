@@ -394,7 +394,7 @@ __device__ __forceinline__ void mb_coords(bool pal, uint32_t seqs, uint32_t sequ
     }
 }
 
-constexpr int kIdctBlocks = 32;                  // blocks per CTA
+constexpr int kIdctBlocks = 16;                  // blocks per CTA
 constexpr int kIdctThreads = kIdctBlocks * 8;    // eight threads (rows) per block
 
 // Stores the eight bytes of `row` at dst (any alignment).
