@@ -380,6 +380,24 @@ void build_lut(const uint8_t *key, size_t key_len, uint32_t sym_off, bool ac, Hu
         }
         code <<= 1;
     }
+    // pairs: an AC symbol whose bits leave room for the whole next one
+    for (uint32_t x = 0; x < (1u << FB); x++) {
+        const uint32_t e1 = lut->fastv[x];
+        lut->fastp[x] = e1;
+        if (!ac || !e1 || (e1 & (kFastCode | kFastEob))) continue;
+        const uint32_t l1 = e1 & 31, adv1 = (e1 >> 5) & 127;
+        const int32_t v1 = (int32_t)e1 >> 16;
+        if (l1 + 2 > FB || v1 < -64 || v1 > 63) continue;
+        const uint32_t e2 = lut->fastv[(x << l1) & ((1u << FB) - 1)];
+        if (!e2 || (e2 & kFastCode)) continue;
+        const uint32_t l2 = e2 & 31;  // the entry depends only on its first l2 bits
+        if (l2 > FB - l1) continue;
+        const int32_t v2 = (int32_t)e2 >> 16;
+        const uint32_t adv2 = (e2 & kFastEob) ? 0 : (e2 >> 5) & 127;
+        if (v2 < -32 || v2 > 31) continue;
+        lut->fastp[x] = ((uint32_t)v2 << 26) | (((uint32_t)v1 & 127) << 19) | (adv2 << 14) | kFastPair | (adv1 << 5) |
+                        (l1 + l2);
+    }
     lut->sym_off = sym_off;
     lut->nsym = (uint32_t)(key_len - 16);
 }

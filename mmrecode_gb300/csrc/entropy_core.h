@@ -77,34 +77,54 @@ __device__ __forceinline__ int slow_symbol(const HuffLut *__restrict__ T, const 
 
 constexpr uint16_t kBarrierErr = 0xffff;  // the symbol runs into the interval's barrier
 
-// Decodes one symbol for coefficient index k (0: the DC symbol), in the
-// reference's order of checks (decoder.rs:501-546). On success returns true,
+// Decodes one symbol for coefficient index k (0: the DC symbol) (with kPairs, a
+// pair where HuffLut::fastp has one; see decode_step), in the reference's order of checks (decoder.rs:501-546). On success returns true,
 // moves k (1 after the DC difference, past an AC level, 16 on for ZRL, 64 at
 // EOB) and sets val: the DC difference or the AC level, 0 for EOB and ZRL, to be
 // stored at zigzag index k - 1 (a zero stored past the last level changes
 // nothing). On failure returns false with err (kBarrierErr when the symbol runs
 // into the barrier) and errbit, the reader position the reference reports.
-__device__ __forceinline__ bool decode_symbol(Bits &r, uint32_t avail, const HuffLut *__restrict__ T,
-                                              const uint8_t *__restrict__ symbols, int &k, int32_t &val,
-                                              uint16_t &err, uint32_t &errbit) {
+template <bool kPairs>
+__device__ __forceinline__ bool decode_symbol_t(Bits &r, uint32_t avail, uint32_t stop, const HuffLut *__restrict__ T,
+                                                const uint8_t *__restrict__ symbols, int &k, int32_t &val,
+                                                int32_t &val2, int &k_mid, uint16_t &err, uint32_t &errbit) {
     refill(r);
-    const uint32_t fv = __ldg(&T->fastv[r.buf >> (64 - kHuffFastBits)]);
+    const uint32_t fv = __ldg(kPairs ? &T->fastp[r.buf >> (64 - kHuffFastBits)] : &T->fastv[r.buf >> (64 - kHuffFastBits)]);
     const uint32_t fl = fv & 31;
-    const int kn = (fv & kFastEob) ? 64 : k + (int)((fv >> 5) & 127);
-    if (fv & kFastCode) {  // code resolved, magnitude after it (receive_extend, entropy.rs:168-182)
-        const uint32_t size = (fv >> 16) & 15, total = fl + size;
-        if (total - 1u < avail && kn <= 64) {
-            const int32_t v = (int32_t)((r.buf << fl) >> (64 - size));
-            val = v < (1 << (size - 1)) ? v + 1 - (1 << size) : v;
-            take(r, (int)total);
+    if (kPairs) {
+        k_mid = 0;
+        val2 = 0;
+    }
+    if (kPairs && (fv & kFastPair) == kFastPair) {
+        const int k1 = k + (int)((fv >> 5) & 127);
+        const uint32_t adv2 = (fv >> 14) & 31;
+        const int k2 = adv2 ? k1 + (int)adv2 : 64;
+        if (fl - 1u < avail && fl <= stop && k1 < 64 && k2 <= 64) {
+            val = (int32_t)(fv << 6) >> 25;
+            val2 = (int32_t)fv >> 26;
+            take(r, (int)fl);
+            k_mid = k1;
+            k = k2;
+            return true;
+        }
+        // otherwise the first symbol alone, by the canonical search below
+    } else {
+        const int kn = (fv & kFastEob) ? 64 : k + (int)((fv >> 5) & 127);
+        if (fv & kFastCode) {  // code resolved, magnitude after it (receive_extend, entropy.rs:168-182)
+            const uint32_t size = (fv >> 16) & 15, total = fl + size;
+            if (total - 1u < avail && kn <= 64) {
+                const int32_t v = (int32_t)((r.buf << fl) >> (64 - size));
+                val = v < (1 << (size - 1)) ? v + 1 - (1 << size) : v;
+                take(r, (int)total);
+                k = kn;
+                return true;
+            }
+        } else if (fl - 1u < avail && kn <= 64) {
+            val = (int32_t)fv >> 16;
+            take(r, (int)fl);
             k = kn;
             return true;
         }
-    } else if (fl - 1u < avail && kn <= 64) {
-        val = (int32_t)fv >> 16;
-        take(r, (int)fl);
-        k = kn;
-        return true;
     }
     uint32_t sym;
     const int l = slow_symbol(T, symbols, r.buf, &sym);
@@ -173,6 +193,29 @@ __device__ __forceinline__ bool decode_symbol(Bits &r, uint32_t avail, const Huf
     val = v;
     k += run + 1;
     return true;
+}
+
+// Decodes one symbol, or two AC symbols from one pair entry (HuffLut::fastp) when
+// both lie within the next 11 bits and end at most `stop` bits on, the first
+// leaves k below 64 and the second keeps it at most 64: the same steps one
+// symbol at a time would take. The pair's inner boundary lies before `stop`, so
+// a decode that records or compares states at the first symbol boundary at or
+// past some position (a checkpoint, the slice end) passing that position as
+// stop meets exactly the boundaries a one-symbol decode meets there. On a pair
+// val is the first level (at zigzag index k_mid - 1) and val2 the second (at
+// k - 1; 0 for EOB, with k 64); otherwise k_mid is 0 and val2 0.
+__device__ __forceinline__ bool decode_step(Bits &r, uint32_t avail, uint32_t stop, const HuffLut *__restrict__ T,
+                                            const uint8_t *__restrict__ symbols, int &k, int32_t &val,
+                                            int32_t &val2, int &k_mid, uint16_t &err, uint32_t &errbit) {
+    return decode_symbol_t<true>(r, avail, stop, T, symbols, k, val, val2, k_mid, err, errbit);
+}
+
+__device__ __forceinline__ bool decode_symbol(Bits &r, uint32_t avail, const HuffLut *__restrict__ T,
+                                              const uint8_t *__restrict__ symbols, int &k, int32_t &val,
+                                              uint16_t &err, uint32_t &errbit) {
+    int32_t v2;
+    int km;
+    return decode_symbol_t<false>(r, avail, 0, T, symbols, k, val, v2, km, err, errbit);
 }
 
 }  // namespace mmr

@@ -480,10 +480,14 @@ __device__ bool resync_slice(const JpegLaunch &L, uint32_t slot, const SliceRef 
         }
         const int k0 = k;
         blocks += k0 == 0;
-        int32_t val;
+        int32_t val, val2;
+        int km;
         uint16_t err;
         uint32_t eb;
-        if (!decode_symbol(r, lim - pr, k0 == 0 ? tb.dc : tb.ac, L.symbols, k, val, err, eb)) break;
+        // two symbols per lookup where both end before the next checkpoint or the
+        // slice end (the speculative decode's boundaries there are one-symbol ones)
+        const uint32_t stop = min(next_mark, S) - pn;
+        if (!decode_step(r, lim - pr, stop, k0 == 0 ? tb.dc : tb.ac, L.symbols, k, val, val2, km, err, eb)) break;
         dcv = k0 == 0 ? val : dcv;
         if (k < 64) continue;
         add_dc(dc, tb.comp, dcv);

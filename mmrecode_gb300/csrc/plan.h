@@ -14,6 +14,7 @@ namespace mmr {
 constexpr int kHuffFastBits = 11;
 constexpr uint32_t kFastEob = 1u << 12;
 constexpr uint32_t kFastCode = 1u << 13;
+constexpr uint32_t kFastPair = kFastEob | kFastCode;  // (no single entry has both)
 
 struct HuffLut {
     uint16_t fast[512];    // (length << 8) | symbol; 0 when the code is longer than 9 bits or absent
@@ -25,6 +26,11 @@ struct HuffLut {
     // read from the bits after the code). 0: slow path (codes longer than 11 bits,
     // and every symbol the reference rejects).
     uint32_t fastv[1 << kHuffFastBits];
+    // fastv with two AC symbols in one entry where both lie whole within the next
+    // 11 bits, the first not EOB, with levels in -64..63 and -32..31:
+    //   level2 << 26 | level1 << 19 | advance2 << 14 | kFastPair | advance1 << 5 | total bits
+    // (advance2 0: the second is EOB). The same as fastv for DC tables.
+    uint32_t fastp[1 << kHuffFastBits];
     int32_t maxcode[18];   // largest code of each length 1..16, -1 if none
     int32_t valptr[18];    // symbol index of a length's first code, minus that code
     uint32_t sym_off;      // first symbol in the symbol pool
