@@ -948,8 +948,14 @@ def main():
     ms_per_step = 1000 * dt / args.steps
 
     hostbuf = items(False)
-    edt, _, _, _ = run(hostbuf, args.steps, args.warmup)
-    edt = _max_over_ranks(world, edt)
+    # three runs of the same K steps, the median reported: a host thread that the OS
+    # holds back for tens of ms now and then (seen with this build and earlier ones
+    # alike) lands in one run, not in the figure; every run's time is reported
+    e2e_runs = []
+    for _ in range(3):
+        edt, _, _, _ = run(hostbuf, args.steps, args.warmup)
+        e2e_runs.append(_max_over_ranks(world, edt))
+    edt = sorted(e2e_runs)[1]
     e2e = total_frames / edt
 
     # the host link this run had: one device-to-host copy of a step's outputs and
@@ -1140,6 +1146,8 @@ def main():
                            "served_p99_at_80pct": served80["p99_ms"] if served80 else None},
             "e2e": {"value": e2e, "unit": "frames/s", "h2d_bytes_per_step": in_bytes,
                     "d2h_bytes_per_step": n * rgb_bytes,
+                    "statistic": "median of 3 runs of the timed steps",
+                    "runs_ms_per_step": [1000 * t / args.steps for t in e2e_runs],
                     # the link alone: the frame rate the device-to-host copy of the outputs caps e2e at
                     "link_d2h_GBps": d2h_gbs, "link_cap_frames_per_s": d2h_gbs * 1e9 / rgb_bytes},
             "bit_exact": bit_exact, "bit_exact_frames": bit_exact_frames,
