@@ -152,7 +152,7 @@ struct SlicePoint {
 // bits, 1.29 -> 1.14 ms per 30 frames; 4096-bit slices of 4:2:2 1080p frames
 // 512 -> 768 bits, 5.71 -> 5.68 ms of entropy decode per 300 frames).
 constexpr int kSliceCheckpoints = 8;
-__host__ __device__ constexpr uint32_t spec_lead(uint32_t slice_bits) { return slice_bits <= 2048 ? 1024u : 768u; }
+MMR_HD constexpr uint32_t spec_lead(uint32_t slice_bits) { return slice_bits <= 2048 ? 1024u : 768u; }
 
 struct SliceSpec {
     SlicePoint exit;                      // end of the speculative decode
