@@ -9,20 +9,25 @@
 // symbol boundary with the same state, and from there both are identical.
 //
 //   slice_plan     per frame: interval token ranges, slice counts, slot -> interval map
-//   slice_spec     every slice decoded from a guessed state 512 bits before it (the
-//                  first slice from the true one) up to its end; keeps the state 64,
-//                  256, 1024 and 2048 bits into the slice
-//   slice_sync     (twice) each slice whose start no longer equals its predecessor's
-//                  exit state re-decodes from that state until it meets one of its own
+//   slice_spec     every slice decoded from a guessed state spec_lead(S) bits before it
+//                  (the first slice from the true one) up to its end; keeps the state
+//                  at eight checkpoints (64 .. 2048 bits into the slice) and stores
+//                  the levels of the blocks it owns
+//   slice_sync     (kSyncPasses passes; one after a pass that changed nothing returns
+//                  at once) each slice whose start no longer equals its predecessor's
+//                  exit state re-decodes from that state, two symbols per lookup where
+//                  both end before the next checkpoint, until it meets one of its own
 //                  checkpoints (then the rest is known) or its end
 //   slice_fix      per interval, only when the last sync pass still changed a state:
 //                  walks the slices in order until every start equals the previous
 //                  exit. Then slice 0 starts in the true state and each exit is the
 //                  true state at that point, so every start is the true one.
 //   slice_prefix   per interval: block index and DC predictors at each slice start
-//   slice_decode   the final decode from true states: quantised AC levels, dequantised
-//                  DC, and each slice's first event (an error, or the interval's last
-//                  block completed)
+//   slice_place    the owned blocks past each slice's match point placed (DC
+//                  predictors, block map); the slots with short work listed
+//   slice_decode   the final decode from true states of what was not placed: quantised
+//                  AC levels, dequantised DC, and each slice's first event (an error,
+//                  or the interval's last block completed)
 //   slice_resolve  per interval: the earliest event in stream order becomes the
 //                  interval's result, or the restart-marker check (entropy.rs:111-134)
 //
