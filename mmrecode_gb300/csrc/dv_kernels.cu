@@ -8,10 +8,12 @@
 //              (a thread per macroblock), segment pool (a thread per segment)
 //              (dv/src/decoder.rs:152-317); writes every dequantised coefficient.
 //   resolve    first failing segment per frame (sequential semantics).
-//   idct       one thread per sample: fp32 separable 8-8 / 2-4-8 transform with
-//              a proven error bound; samples within it of a rounding boundary
-//              get the reference's binary64 sum in its exact operation order
-//              (decoder.rs:520-602); then placement (decoder.rs:395-505).
+//   idct       eight threads per block (one per output row), 16 blocks per CTA:
+//              fp32 separable 8-8 / 2-4-8 transform with a proven error bound;
+//              samples within it of a rounding boundary are settled by the warp in
+//              exact fixed point, or in the reference's binary64 order for genuine
+//              near-ties (decoder.rs:520-602, dv_idct_core.h); then placement
+//              (decoder.rs:395-505).
 #include <cuda_runtime.h>
 
 #include "dv_idct_core.h"
