@@ -9,9 +9,11 @@
 //       levels (natural order) and the dequantised DC of every block, and the
 //       interval's restart-marker check (entropy.rs:111-134).
 //   resolve  picks each frame's first failing interval (sequential semantics).
-//   idct     dequantisation + the reference's binary64 IDCT (transform.rs:86-109)
-//       in its exact operation order, +128, round-half-away, clamp, clipped
-//       block write (decoder.rs:550-565).
+//   idct     planar output: dequantisation + the IDCT in fp32 with a proven error
+//       bound (idct_core.h), +128, round-half-away, clamp, clipped block write
+//       (decoder.rs:550-565); idct_fixup settles the samples the bound leaves
+//       undecided, a warp per block, in exact fixed point or the reference's
+//       binary64 order (transform.rs:86-109).
 #include <cuda_runtime.h>
 
 #include "entropy_core.h"
