@@ -92,6 +92,8 @@ __device__ __forceinline__ void add_dc(int32_t (&dc)[4], uint32_t comp, int32_t 
         if (comp == (uint32_t)c) dc[c] += v;
 }
 
+__device__ __forceinline__ void add_dc_at(int32_t *dc, uint32_t comp, int32_t v) { dc[comp] += v; }
+
 struct SliceRef {
     uint32_t item, j;
     IvInfo v;
@@ -238,6 +240,10 @@ __device__ __forceinline__ TabIdx tab_idx(const JpegLaunch &L, const JFrame &F, 
 __global__ void __launch_bounds__(kSliceThreads, MMR_SPEC_CTAS_PER_SM) slice_spec_kernel(JpegLaunch L) {
     __shared__ __align__(16) int16_t s_stage[kSliceThreads * kStride];
     __shared__ uint8_t s_zz[64];
+    // per thread: DC sums per component, the scratch chunk and the end of the last
+    // stored block, touched once per block (kept out of registers for occupancy)
+    __shared__ int32_t s_dc[kSliceThreads][4];
+    __shared__ uint32_t s_chunk[kSliceThreads], s_end[kSliceThreads];
     int16_t *stage = s_stage + threadIdx.x * kStride;
     int4 *stage4 = reinterpret_cast<int4 *>(stage);
 #pragma unroll
@@ -289,7 +295,9 @@ __global__ void __launch_bounds__(kSliceThreads, MMR_SPEC_CTAS_PER_SM) slice_spe
     uint32_t si = 0;
     TabIdx tb = tab_idx(L, F, si);
     uint32_t blocks = 0;
-    int32_t dc[4] = {0, 0, 0, 0};
+    int32_t *dc = s_dc[threadIdx.x];
+#pragma unroll
+    for (int c = 0; c < 4; c++) dc[c] = 0;
     int32_t dcv = 0;  // DC difference of the block in progress (0 before its DC symbol)
     uint32_t q = 0, recorded = 0;
     uint32_t next_mark = guess ? mark_at(0) : 0xffffffffu;
@@ -297,8 +305,11 @@ __global__ void __launch_bounds__(kSliceThreads, MMR_SPEC_CTAS_PER_SM) slice_spe
     bool entered = false;  // at or past the slice start
     bool own_blk = false;  // the block in progress is owned
     bool own_ok = true;    // the owned blocks so far are stored
-    uint32_t own_n = 0, chunk_base = 0;
-    uint32_t own_end = 0;  // position (from p0) after the last stored one
+    uint32_t own_n = 0;
+    uint32_t &chunk_base = s_chunk[threadIdx.x];
+    uint32_t &own_end = s_end[threadIdx.x];  // position (from p0) after the last stored one
+    chunk_base = 0;
+    own_end = 0;
     for (;;) {
         const uint32_t pr = r.used;
         if (pr >= end) {
@@ -359,7 +370,7 @@ __global__ void __launch_bounds__(kSliceThreads, MMR_SPEC_CTAS_PER_SM) slice_spe
             own_end = r.used;
         }
         own_blk = false;
-        add_dc(dc, tb.comp, dcv);
+        add_dc_at(dc, tb.comp, dcv);
         dcv = 0;
         k = 0;
         si = si + 1 == F.sched_len ? 0 : si + 1;
@@ -387,7 +398,7 @@ __global__ void __launch_bounds__(kSliceThreads, MMR_SPEC_CTAS_PER_SM) slice_spe
     own->last_end = p0 + own_end;
     own->n = own_n;
     own->ok = own_ok && exit_state != kStErr;
-    add_dc(dc, tb.comp, dcv);  // the block in progress is counted, with its DC if decoded
+    add_dc_at(dc, tb.comp, dcv);  // the block in progress is counted, with its DC if decoded
     if (guess) {
         for (uint32_t x = 0; x < (uint32_t)kSliceCheckpoints; x++)
             if (!(recorded & (1u << x))) L.spec[slot].cp[x].state = kStErr;
