@@ -368,24 +368,26 @@ __global__ void dv_resolve_kernel(DvLaunch L) {
     }
 }
 
-// decoder.rs:395-422 macroblock_coordinates (in 8-sample units)
+// decoder.rs:395-422 macroblock_coordinates (in 8-sample units); the per-macroblock
+// offsets in constant memory (indexed per lane, as local arrays they went to the stack)
+__constant__ uint32_t c_mb_off[5] = {2, 6, 8, 0, 4};
+__constant__ uint32_t c_mb_shuf3[5] = {18, 9, 27, 0, 36};
+__constant__ uint32_t c_mb_lstart[5] = {9, 4, 13, 0, 18};
+
 __device__ __forceinline__ void mb_coords(bool pal, uint32_t seqs, uint32_t sequence, uint32_t slot, uint32_t m,
                                           uint32_t *mbx, uint32_t *mby) {
-    const uint32_t OFF[5] = {2, 6, 8, 0, 4};
-    const uint32_t SHUF3[5] = {18, 9, 27, 0, 36};
-    const uint32_t LSTART[5] = {9, 4, 13, 0, 18};
     if (pal) {
         // SERPENT1[slot] = 0,1,2,2,1,0 repeating
         uint32_t s6 = slot % 6;
         uint32_t serp1 = s6 < 3 ? s6 : 5 - s6;
-        uint32_t x = SHUF3[m] + slot / 3;
-        uint32_t y = serp1 + ((sequence + OFF[m]) % seqs) * 3;
+        uint32_t x = c_mb_shuf3[m] + slot / 3;
+        uint32_t y = serp1 + ((sequence + c_mb_off[m]) % seqs) * 3;
         *mbx = x * 2;
         *mby = y * 2;
     } else {
-        uint32_t row = (sequence + OFF[m]) % seqs;
+        uint32_t row = (sequence + c_mb_off[m]) % seqs;
         uint32_t k = slot + ((m == 1 || m == 2) ? 3 : 0);
-        uint32_t x = LSTART[m] + k / 6;
+        uint32_t x = c_mb_lstart[m] + k / 6;
         // SERPENT2[k] = 0..5,5..0 repeating
         uint32_t k12 = k % 12;
         uint32_t serp2 = k12 < 6 ? k12 : 11 - k12;
