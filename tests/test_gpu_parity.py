@@ -18,7 +18,7 @@ import mmrecode_gb300 as m
 import oracle
 from mmrecode_gb300 import _lib, synth
 from helpers import (DV_FIXTURES, GOLDEN, JPEG_FIXTURES, SIMPLE_AC, SIMPLE_DC, BitWriter, assert_same_decode,
-                     encode_blocks, fixture, frame_planes_gpu, jpeg, prefixed, stuff)
+                     encode_blocks, fixture, frame_planes_gpu, jpeg, prefixed, stuff, report)
 
 pytestmark = pytest.mark.gpu
 
@@ -134,6 +134,58 @@ def test_dv_synthetic_88_and_248(ctx, pal):
     packets = synth.dv_stream(103, 3, pal=pal)
     check_batch(ctx, m.CODEC_DV, packets, "dv")
     check_batch(ctx, m.CODEC_DV, packets[:1], "dv rgb", m.OUTPUT_RGB24)
+
+
+def _dv_content(kind: str, pal: bool, seed: int):
+    """Frames that push the DV encoder's bits through every spill level: noise as
+    strong as the encoder still fits (blocks overflow into the macroblock and segment
+    pools), flat (nothing spills), one-sample checkerboards and 8-sample stripes
+    (every block dense or one-sided)."""
+    w, h = 720, (576 if pal else 480)
+    cw, ch = (360, 288) if pal else (180, 480)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    yy, xx = np.mgrid[0:h, 0:w]
+    cy, cx = np.mgrid[0:ch, 0:cw]
+    if kind == "noise":
+        planes = [128 + rng.integers(-12, 13, (h, w)), 128 + rng.integers(-12, 13, (ch, cw)),
+                  128 + rng.integers(-12, 13, (ch, cw))]
+    elif kind == "flat":
+        planes = [np.full((h, w), 120), np.full((ch, cw), 100), np.full((ch, cw), 150)]
+    elif kind == "checker":
+        planes = [16 + 219 * ((yy + xx) & 1), 16 + 224 * ((cy + cx) & 1), 240 - 224 * ((cy + cx) & 1)]
+    else:  # stripes
+        planes = [16 + 219 * ((xx >> 3) & 1), 16 + 224 * ((cy >> 3) & 1), 128 + 0 * cx]
+    planes = [np.asarray(p, dtype=np.uint8) for p in planes]
+    fmt = m.YUV420P8 if pal else m.YUV411P8
+    return m.VideoFrame(fmt, w, h, [m.Plane(planes[0].tobytes(), w, w, h), m.Plane(planes[1].tobytes(), cw, cw, ch),
+                                    m.Plane(planes[2].tobytes(), cw, cw, ch)], m.RANGE_LIMITED)
+
+
+@pytest.mark.parametrize("pal", [False, True])
+def test_dv_spill_levels_extreme_content(ctx, pal):
+    packets = []
+    for i, kind in enumerate(("noise", "flat", "checker", "stripes")):
+        frame = _dv_content(kind, pal, 120 + i)
+        for mode in (m.DV_MODE_88, m.DV_MODE_ACTIVITY):
+            try:
+                packets.append(m.encode_dv(frame, mode))
+            except m.MmrError:  # the encoder's own limit (a segment over its budget): no stream
+                pass
+    assert len(packets) >= 6
+    check_batch(ctx, m.CODEC_DV, packets, "dv extreme")
+    # the same with damaged payload bytes: errors inside the pools, with and without concealment
+    rng = np.random.Generator(np.random.PCG64(130 + pal))
+    bad = []
+    for pkt in packets[:4]:
+        b = bytearray(pkt)
+        for _ in range(40):
+            dif = int(rng.integers(0, len(b) // 80))
+            if (dif % 150) >= 6:  # video DIF blocks keep their headers intact
+                b[dif * 80 + int(rng.integers(4, 80))] ^= 1 << int(rng.integers(0, 8))
+        bad.append(bytes(b))
+    check_batch(ctx, m.CODEC_DV, bad, "dv extreme damaged")
+    check_batch(ctx, m.CODEC_DV, bad, "dv extreme damaged conceal", conceal=True)
+    report("dv spill levels", frames=len(packets) + 2 * len(bad))
 
 
 def test_mixed_sizes_subsampling_quality_restart(ctx):
