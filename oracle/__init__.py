@@ -130,6 +130,8 @@ def lib():
             getattr(L, name).argtypes = [vp, ctypes.c_size_t, vp]
         L.orc_dv_coefficients.argtypes = [u8p, ctypes.c_size_t, vp, vp, ctypes.c_size_t]
         L.orc_dv_coefficients.restype = ctypes.c_size_t
+        L.orc_dv_vlc_entries.argtypes = [vp, vp, vp, vp, ctypes.c_size_t]
+        L.orc_dv_vlc_entries.restype = ctypes.c_size_t
         L.orc_jpeg_fdct_quantize_many.argtypes = [vp, vp, ctypes.c_size_t, vp]
         L.orc_jpeg_write_levels.argtypes = [ctypes.POINTER(_JpegLayout), vp, ctypes.c_size_t, vp, ctypes.c_size_t,
                                             ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(_Result)]
@@ -355,3 +357,16 @@ def dv_coefficients(data: bytes):
     arr, n = _buf(data)
     got = lib().orc_dv_coefficients(arr, n, coef.ctypes.data, modes.ctypes.data, cap)
     return coef[:got], modes[:got]
+
+
+def dv_vlc_entries():
+    """[(code, length, run, level)] of the DV VLC (decoder.rs:319-354), sorted by length."""
+    import numpy as np
+
+    cap = 1024
+    code = np.zeros(cap, np.uint16)
+    ln = np.zeros(cap, np.uint8)
+    run = np.zeros(cap, np.uint8)
+    level = np.zeros(cap, np.int16)
+    n = lib().orc_dv_vlc_entries(code.ctypes.data, ln.ctypes.data, run.ctypes.data, level.ctypes.data, cap)
+    return [(int(code[i]), int(ln[i]), int(run[i]), int(level[i])) for i in range(n)]

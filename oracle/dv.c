@@ -544,6 +544,18 @@ static void free_blocks(dctblock_t *b, size_t n) {
     for (size_t i = 0; i < n; i++) bits_free(&b[i].partial);
 }
 
+size_t orc_dv_vlc_entries(uint16_t *code, uint8_t *len, uint8_t *run, int16_t *level, size_t cap) {
+    build_vlc();
+    size_t n = 0;
+    for (int i = 0; i < VLC_COUNT && n < cap; i++, n++) {
+        code[n] = VLC[i].code;
+        len[n] = VLC[i].len;
+        run[n] = VLC[i].run;
+        level[n] = VLC[i].level;
+    }
+    return n;
+}
+
 /* Coefficient capture for the transform tests (orc_dv_coefficients): every
  * decoded block's coefficients and DCT mode, in segment order. */
 static int32_t *g_cap_coef;

@@ -116,6 +116,10 @@ int orc_dv_decode(const uint8_t *data, size_t len, int conceal, orc_frame *out,
 int orc_dv_issue_count(const uint8_t *data, size_t len, size_t *count, size_t *first_offset,
                        orc_result *res);
 
+/* The DV VLC codes (decoder.rs:319-354 vlc_entries, sign bits appended, sorted by
+ * length): up to cap (code, length, run, level) entries; returns the number. */
+size_t orc_dv_vlc_entries(uint16_t *code, uint8_t *len, uint8_t *run, int16_t *level, size_t cap);
+
 /* Dequantised coefficients and DCT modes of every block of a frame (segment order). */
 size_t orc_dv_coefficients(const uint8_t *data, size_t len, int32_t *coef, uint8_t *modes, size_t cap);
 
