@@ -149,10 +149,11 @@ struct SlicePoint {
 // speculative decode met the true one late. Short slices take a longer lead
 // relative to their length: their sync passes and serial fix-up cost more than
 // the extra decoding (measured: 1024-bit slices of 4:2:0 VGA frames 512 -> 1024
-// bits, 1.29 -> 1.14 ms per 30 frames; 4096-bit slices of 4:2:2 1080p frames
-// 512 -> 768 bits, 5.71 -> 5.68 ms of entropy decode per 300 frames).
+// -> 1536 bits, 1.29 -> 1.14 -> 1.13 ms per 30 frames, 2048 bits no better;
+// 4096-bit slices of 4:2:2 1080p frames 512 -> 768 bits, 5.71 -> 5.68 ms of
+// entropy decode per 300 frames).
 constexpr int kSliceCheckpoints = 8;
-MMR_HD constexpr uint32_t spec_lead(uint32_t slice_bits) { return slice_bits <= 2048 ? 1024u : 768u; }
+MMR_HD constexpr uint32_t spec_lead(uint32_t slice_bits) { return slice_bits <= 1024 ? 1536u : slice_bits <= 2048 ? 1024u : 768u; }
 
 struct SliceSpec {
     SlicePoint exit;                      // end of the speculative decode
