@@ -25,8 +25,9 @@ struct Bits {
 };
 
 // Reader at token-stream bit `bit`; `used` is the base-relative position there.
-// The token stream has a word of padding past its end, so the one-ahead load of
-// the last word stays inside the buffer.
+// Every frame's token stream is followed by padding (256-byte aligned frames and 64
+// bytes past the last), so the one-ahead load of the last word stays inside the
+// buffer.
 __device__ __forceinline__ void bits_init(Bits &r, const uint8_t *tok, unsigned long long bit, uint32_t used) {
     r.words = reinterpret_cast<const uint32_t *>(tok);
     const uint32_t w0 = (uint32_t)(bit >> 5), skip = (uint32_t)bit & 31;
@@ -77,13 +78,14 @@ __device__ __forceinline__ int slow_symbol(const HuffLut *__restrict__ T, const 
 
 constexpr uint16_t kBarrierErr = 0xffff;  // the symbol runs into the interval's barrier
 
-// Decodes one symbol for coefficient index k (0: the DC symbol) (with kPairs, a
-// pair where HuffLut::fastp has one; see decode_step), in the reference's order of checks (decoder.rs:501-546). On success returns true,
-// moves k (1 after the DC difference, past an AC level, 16 on for ZRL, 64 at
-// EOB) and sets val: the DC difference or the AC level, 0 for EOB and ZRL, to be
-// stored at zigzag index k - 1 (a zero stored past the last level changes
-// nothing). On failure returns false with err (kBarrierErr when the symbol runs
-// into the barrier) and errbit, the reader position the reference reports.
+// Decodes one symbol for coefficient index k (0: the DC symbol), in the
+// reference's order of checks (decoder.rs:501-546); with kPairs, two where
+// HuffLut::fastp holds a pair (see decode_step). On success returns true, moves k
+// (1 after the DC difference, past an AC level, 16 on for ZRL, 64 at EOB) and sets
+// val: the DC difference or the AC level, 0 for EOB and ZRL, to be stored at
+// zigzag index k - 1 (a zero stored past the last level changes nothing). On
+// failure returns false with err (kBarrierErr when the symbol runs into the
+// barrier) and errbit, the reader position the reference reports.
 template <bool kPairs>
 __device__ __forceinline__ bool decode_symbol_t(Bits &r, uint32_t avail, uint32_t stop, const HuffLut *__restrict__ T,
                                                 const uint8_t *__restrict__ symbols, int &k, int32_t &val,
