@@ -29,6 +29,7 @@
 #include <math.h>
 #include <stdint.h>
 
+#include "common.h"
 #include "tables.h"
 
 namespace mmr {
@@ -79,8 +80,9 @@ inline void build_dv_fixed(long long *w88, long long *w248) {
         }
 }
 
-// --------------------------------------------------------------- device ---
+// ------------------------------------------------------------ evaluation ---
 
+#if defined(__CUDACC__)
 // T = sum_i W_i c_i over the 64 coefficients of a block, every lane of the warp
 // taking part (all 32 call it with the same wrow and c); the result in every lane.
 __device__ __forceinline__ long long fixed_sum(const long long *__restrict__ wrow, const int32_t *c) {
@@ -90,10 +92,12 @@ __device__ __forceinline__ long long fixed_sum(const long long *__restrict__ wro
     for (int o = 16; o > 0; o >>= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
     return p;
 }
+#endif
 
 // The clamped sample of T / 2^40 + offset when no half-integer lies within
-// (c1 + 2) / 2^40 of it, else -1 (decide in the reference order).
-__device__ __forceinline__ int fixed_round(long long t, int32_t c1, int offset) {
+// (c1 + 2) / 2^40 of it, else -1 (decide in the reference order). Host and
+// device: the CPU tests check it against the reference's rounding.
+MMR_HD int fixed_round(long long t, int32_t c1, int offset) {
     const long long one = 1ll << kFixShift, half = one >> 1;
     const long long d = (t & (one - 1)) - half;  // T mod 2^40, centred on the half-integer
     if ((d < 0 ? -d : d) <= (long long)c1 + 2) return -1;
