@@ -60,7 +60,7 @@ def test_static_entry_point_matches_mmr_dv_decode_on_two_calls_in_a_row():
 
 
 def _device_free_bytes() -> int:
-    """Free device memory as the driver reports it for the current context."""
+    """Free device memory as cuMemGetInfo reports it for the current context."""
     cuda = ctypes.CDLL("libcuda.so.1")
     free, total = ctypes.c_size_t(0), ctypes.c_size_t(0)
     assert cuda.cuMemGetInfo_v2(ctypes.byref(free), ctypes.byref(total)) == 0
