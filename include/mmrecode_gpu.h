@@ -335,6 +335,62 @@ MMR_API mmr_status mmr_gpu_server_set_tuning(mmr_gpu_server *server, const mmr_g
                                              size_t count);
 
 /*
+ * Decoder sessions: the reference's Decoder trait (crates/core/src/codec.rs:102-130)
+ * as MjpegDecoder (crates/codecs/mjpeg/src/codec.rs:16-71) and DvDecoder
+ * (crates/codecs/dv/src/codec.rs:16-66) implement it, decoding on the GPU. A sent
+ * packet is copied and queued at once on a continuous-batching server that all
+ * sessions of the process share (created with the first packet, on device 0), so
+ * packets of many sessions decode in the same batches; each session receives its
+ * frames in the order it sent the packets.
+ *
+ * States and messages are the reference's: send_packet, receive_frame and flush
+ * fail with MMR_STATUS_INVALID_STATE until configure has succeeded, and configure
+ * checks the descriptor. One difference: the reference's send_packet decodes
+ * before it returns, so a decode error comes back from send_packet; here it comes
+ * back, with the same status and message, from the receive_frame call that reaches
+ * that packet. Calls on one session must not overlap; different sessions may be
+ * used from different threads.
+ */
+typedef struct mmr_gpu_decoder mmr_gpu_decoder;
+
+/* A session for MMR_CODEC_MJPEG or MMR_CODEC_DV; it starts unconfigured. */
+MMR_API mmr_status mmr_gpu_decoder_create(uint32_t codec, mmr_gpu_decoder **out_decoder);
+
+/* Waits for the session's packets still being decoded, frees its queued frames and
+   the session; NULL is ignored. */
+MMR_API void mmr_gpu_decoder_destroy(mmr_gpu_decoder *decoder);
+
+/* configure: codec_id must be the session's ("video/mjpeg" or "video/dv") and
+   media_type "video", else MMR_STATUS_INVALID_DATA with the reference's message.
+   Discards the queued frames. */
+MMR_API mmr_status mmr_gpu_decoder_configure(mmr_gpu_decoder *decoder, const char *codec_id,
+                                             const char *media_type);
+
+/* send_packet: copies the packet, queues it for decode and returns. user_tag comes
+   back with the packet's frame (the reference carries the packet's pts and duration
+   into the frame's timing; a caller keeps them by tag). */
+MMR_API mmr_status mmr_gpu_decoder_send_packet(mmr_gpu_decoder *decoder, const uint8_t *data, size_t len,
+                                               uint64_t user_tag);
+
+/*
+ * receive_frame: the frame of the oldest queued packet, waiting up to wait_ns for it
+ * (< 0: without limit; 0: only if it is done). *out_frame is initialised by the
+ * caller as for mmr_mjpeg_decode and freed with mmr_video_frame_free.
+ * *out_has_frame = 1: the frame is in *out_frame and the packet's tag in
+ * *out_user_tag (NULL allowed). *out_has_frame = 0 with MMR_STATUS_OK: nothing is
+ * queued, or the oldest packet is not done within wait_ns (the reference's Ok(None)).
+ * A packet that failed to decode leaves the queue here: the call returns its status
+ * and message, the frame stays empty and *out_user_tag is set.
+ */
+MMR_API mmr_status mmr_gpu_decoder_receive_frame(mmr_gpu_decoder *decoder, int64_t wait_ns,
+                                                 mmr_video_frame *out_frame, uint64_t *out_user_tag,
+                                                 int *out_has_frame);
+
+/* flush: end of input. Returns when every queued packet is decoded, so that
+   receive_frame with wait_ns 0 then drains the session. */
+MMR_API mmr_status mmr_gpu_decoder_flush(mmr_gpu_decoder *decoder);
+
+/*
  * Whole-stream decode to Y4M: the reference CLI's `mmrecode decode <in> <out>`
  * for MJPEG and raw DV input (crates/cli/src/main.rs:1533-1580, 1605-1633), with
  * the stream uploaded once and framed on the GPU, every frame decoded in one

@@ -786,3 +786,69 @@ class DvDecoder(_GpuDecoder):
 
     def _decode_single(self, data: bytes) -> VideoFrame:
         return decode_dv(data)
+
+
+class DecoderSession:
+    """The C session API (``mmr_gpu_decoder_*``): the Decoder trait
+    (crates/core/src/codec.rs:102-130) with packets queued on a server that every
+    session of the process shares. ``send_packet`` returns at once; a packet's decode
+    error is raised by the ``receive_frame`` that reaches it (``MmrError.tag`` is the
+    packet's tag)."""
+
+    def __init__(self, codec: int):
+        lib = _lib.load()
+        h = ctypes.c_void_p()
+        st = lib.mmr_gpu_decoder_create(codec, ctypes.byref(h))
+        if st != STATUS_OK:
+            raise MmrError(st, _lib.last_error())
+        self._h = h  # send_packet copies each packet: the caller's bytes need not stay alive
+
+    def close(self) -> None:
+        """Waits for the packets still being decoded and frees the session."""
+        h = getattr(self, "_h", None)
+        if h:
+            self._h = None
+            _lib.load().mmr_gpu_decoder_destroy(h)
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        self.close()
+
+    def _check(self, st: int) -> None:
+        if st != STATUS_OK:
+            raise MmrError(st, _lib.last_error())
+
+    def configure(self, descriptor: CodecDescriptor) -> None:
+        self._check(_lib.load().mmr_gpu_decoder_configure(self._h, descriptor.codec_id.encode(),
+                                                           descriptor.media_type.encode()))
+
+    def send_packet(self, data: bytes, tag: int = 0) -> None:
+        buf = bytes(data)
+        self._check(_lib.load().mmr_gpu_decoder_send_packet(self._h, buf, len(buf), tag))
+
+    def receive_frame(self, wait_ns: int = -1):
+        """(frame, tag), or None when nothing is queued or the oldest packet is not
+        decoded within wait_ns (< 0: wait without limit)."""
+        lib = _lib.load()
+        fr = _lib.VideoFrameC()
+        fr.struct_size = ctypes.sizeof(_lib.VideoFrameC)
+        tag, has = ctypes.c_uint64(0), ctypes.c_int(0)
+        st = lib.mmr_gpu_decoder_receive_frame(self._h, wait_ns, ctypes.byref(fr), ctypes.byref(tag), ctypes.byref(has))
+        if st != STATUS_OK:
+            e = MmrError(st, _lib.last_error())
+            e.tag = tag.value
+            raise e
+        if not has.value:
+            return None
+        try:
+            return _frame_from_c(fr), tag.value
+        finally:
+            lib.mmr_video_frame_free(ctypes.byref(fr))
+
+    def flush(self) -> None:
+        self._check(_lib.load().mmr_gpu_decoder_flush(self._h))

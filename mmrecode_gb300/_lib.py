@@ -169,6 +169,14 @@ SIGNATURES = {
     "mmr_gpu_server_stats_get": ([ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ServerStats)], ctypes.c_int32),
     "mmr_gpu_server_set_slice_bits": ([ctypes.c_void_p, ctypes.c_uint32], ctypes.c_int32),
     "mmr_gpu_server_set_tuning": ([ctypes.c_void_p, ctypes.POINTER(TuneEntry), ctypes.c_size_t], ctypes.c_int32),
+    "mmr_gpu_decoder_create": ([ctypes.c_uint32, ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int32),
+    "mmr_gpu_decoder_destroy": ([ctypes.c_void_p], None),
+    "mmr_gpu_decoder_configure": ([ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p], ctypes.c_int32),
+    "mmr_gpu_decoder_send_packet": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_uint64],
+                                    ctypes.c_int32),
+    "mmr_gpu_decoder_receive_frame": ([ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(VideoFrameC),
+                                       ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_int)], ctypes.c_int32),
+    "mmr_gpu_decoder_flush": ([ctypes.c_void_p], ctypes.c_int32),
     "mmr_gpu_server_replay": ([ctypes.c_void_p, ctypes.POINTER(GpuItem), ctypes.c_size_t,
                               ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_double),
                               ctypes.POINTER(ctypes.c_int64)], ctypes.c_int32),

@@ -5,6 +5,8 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <deque>
+#include <memory>
 #include <mutex>
 #include <new>
 #include <string>
@@ -79,48 +81,29 @@ void free_frame_planes(mmr_video_frame *f) {
     for (size_t i = 0; i < n; i++) free(f->planes[i].data);
 }
 
-// mjpeg_decode_impl / dv_decode_impl (lib.rs:594-642) on the GPU.
-mmr_status decode_one(uint32_t codec, const uint8_t *data, size_t len, mmr_video_frame *out) {
-    if (!out) return invalid_argument("out_frame is null");
-    if (out->struct_size != sizeof(mmr_video_frame)) {
-        char m[128];
-        snprintf(m, sizeof m, "out_frame struct_size is %zu, expected %zu", out->struct_size, sizeof(mmr_video_frame));
-        return invalid_argument(m);
-    }
-    reset_frame(out);
-    if (len > 0 && !data) return invalid_argument("data is null while length is nonzero");
-    mmr::Probe pr = mmr::probe_packet(codec, data, len);
-    Item it;
-    it.data = data;
-    it.len = len;
-    it.codec = codec;
-    it.output = mmr::kOutPlanar;
-    uint8_t *planes[3] = {nullptr, nullptr, nullptr};
-    bool sized = pr.status == MMR_STATUS_OK && pr.format != 0 && pr.plane_count <= 3;
-    if (sized) {
-        for (size_t c = 0; c < pr.plane_count; c++) {
-            size_t bytes = pr.plane_width[c] * pr.plane_height[c];
-            planes[c] = (uint8_t *)malloc(bytes ? bytes : 1);
-            if (!planes[c]) {
-                for (size_t k = 0; k < c; k++) free(planes[k]);
-                return finish(MMR_STATUS_INTERNAL_ERROR, "out of host memory");
-            }
-            it.plane_out[c] = planes[c];
+// Host planes for a packet whose headers give its geometry, set as the item's
+// planar outputs (one malloc'd buffer per plane, as mmr_video_frame_free expects);
+// planes stay null when the headers fail (the decode then reports why). False
+// when the host is out of memory.
+bool alloc_planes(const mmr::Probe &pr, Item &it, uint8_t *planes[3]) {
+    planes[0] = planes[1] = planes[2] = nullptr;
+    if (pr.status != MMR_STATUS_OK || pr.format == 0 || pr.plane_count > 3) return true;
+    for (size_t c = 0; c < pr.plane_count; c++) {
+        size_t bytes = pr.plane_width[c] * pr.plane_height[c];
+        planes[c] = (uint8_t *)malloc(bytes ? bytes : 1);
+        if (!planes[c]) {
+            for (size_t k = 0; k < c; k++) free(planes[k]);
+            planes[0] = planes[1] = planes[2] = nullptr;
+            return false;
         }
-        it.out_capacity = pr.planar_bytes;
+        it.plane_out[c] = planes[c];
     }
-    std::string err;
-    Engine *engine = acquire_engine(err);
-    if (!engine) {
-        for (auto p : planes) free(p);
-        return finish(MMR_STATUS_INTERNAL_ERROR, err);
-    }
-    engine->decode(&it, 1);
-    release_engine(engine);
-    if (it.status != MMR_STATUS_OK) {
-        for (auto p : planes) free(p);
-        return finish(it.status, with_prefix(it.status, it.message));
-    }
+    it.out_capacity = pr.planar_bytes;
+    return true;
+}
+
+// Hands the decoded planes to the caller's frame (which owns them from here on).
+void fill_frame(const Item &it, uint8_t *const planes[3], mmr_video_frame *out) {
     out->format = it.format;
     out->range = it.range;
     out->width = it.width;
@@ -133,6 +116,46 @@ mmr_status decode_one(uint32_t codec, const uint8_t *data, size_t len, mmr_video
         out->planes[c].stride = it.plane_width[c];
         out->planes[c].data_len = it.plane_width[c] * it.plane_height[c];
     }
+}
+
+// The v1 convention for a caller's frame (lib.rs:604-611): non-null, its
+// struct_size this library's (else INVALID_ARGUMENT and the frame is untouched).
+mmr_status check_frame(mmr_video_frame *out) {
+    if (!out) return invalid_argument("out_frame is null");
+    if (out->struct_size != sizeof(mmr_video_frame)) {
+        char m[128];
+        snprintf(m, sizeof m, "out_frame struct_size is %zu, expected %zu", out->struct_size, sizeof(mmr_video_frame));
+        return invalid_argument(m);
+    }
+    return MMR_STATUS_OK;
+}
+
+// mjpeg_decode_impl / dv_decode_impl (lib.rs:594-642) on the GPU.
+mmr_status decode_one(uint32_t codec, const uint8_t *data, size_t len, mmr_video_frame *out) {
+    if (mmr_status st = check_frame(out)) return st;
+    reset_frame(out);
+    if (len > 0 && !data) return invalid_argument("data is null while length is nonzero");
+    mmr::Probe pr = mmr::probe_packet(codec, data, len);
+    Item it;
+    it.data = data;
+    it.len = len;
+    it.codec = codec;
+    it.output = mmr::kOutPlanar;
+    uint8_t *planes[3];
+    if (!alloc_planes(pr, it, planes)) return finish(MMR_STATUS_INTERNAL_ERROR, "out of host memory");
+    std::string err;
+    Engine *engine = acquire_engine(err);
+    if (!engine) {
+        for (auto p : planes) free(p);
+        return finish(MMR_STATUS_INTERNAL_ERROR, err);
+    }
+    engine->decode(&it, 1);
+    release_engine(engine);
+    if (it.status != MMR_STATUS_OK) {
+        for (auto p : planes) free(p);
+        return finish(it.status, with_prefix(it.status, it.message));
+    }
+    fill_frame(it, planes, out);
     return finish(MMR_STATUS_OK, "");
 }
 
@@ -254,6 +277,87 @@ struct mmr_gpu_server {
 struct mmr_gpu_stream {
     mmr::Stream *stream;
 };
+
+namespace {
+
+// One packet of a decoder session, from send_packet until receive_frame hands
+// its frame over: the packet copy and the output planes stay put (the entry is
+// heap-held) while the server's engine reads and writes them.
+struct SessionEntry {
+    std::vector<uint8_t> packet;
+    uint8_t *planes[3] = {nullptr, nullptr, nullptr};
+    uint64_t tag = 0;
+    uint64_t ticket = 0;
+    bool done = false;  // result holds the outcome (the server has forgotten the ticket)
+    Item result;
+};
+
+// The server the sessions of the process share (device 0), created with the
+// first packet and kept until the process ends, like the v1 engine pool.
+std::mutex g_session_server_mu;
+mmr::Server *g_session_server = nullptr;
+
+mmr::Server *session_server(std::string &err) {
+    std::lock_guard<std::mutex> lock(g_session_server_mu);
+    if (g_session_server) return g_session_server;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        err = "no CUDA device is available to the GPU decoder";
+        return nullptr;
+    }
+    try {
+        mmr::ServerConfig c;
+        c.device = 0;
+        c.engines = 4;
+        c.max_batch = 16;
+        c.memory_budget = 0;
+        g_session_server = new mmr::Server(c);
+    } catch (const std::exception &e) {
+        err = std::string("could not initialise the GPU decoder: ") + e.what();
+        return nullptr;
+    }
+    return g_session_server;
+}
+
+}  // namespace
+
+// Decoder trait state (mjpeg/src/codec.rs:16-19, dv/src/codec.rs:16-19): the
+// configured flag and the queue of frames, here of packets on their way to frames.
+struct mmr_gpu_decoder {
+    uint32_t codec;
+    bool configured = false;
+    std::deque<std::unique_ptr<SessionEntry>> queue;
+    mmr::Server *server = nullptr;  // set by the first packet
+
+    const char *kind() const { return codec == MMR_CODEC_DV ? "DV" : "Motion JPEG"; }
+
+    // Waits until the entry's decode is over and keeps its outcome.
+    void settle(SessionEntry &e) {
+        if (e.done) return;
+        server->wait(e.ticket, -1, &e.result, nullptr);
+        e.done = true;
+    }
+
+    // Drops every queued packet (after its decode is over) with its planes.
+    void clear() {
+        for (auto &e : queue) {
+            settle(*e);
+            for (auto p : e->planes) free(p);
+        }
+        queue.clear();
+    }
+};
+
+namespace {
+
+// The reference's InvalidState texts (mjpeg/src/codec.rs:39-71, dv/src/codec.rs:33-65).
+mmr_status unconfigured(const mmr_gpu_decoder *d, const char *what) {
+    return finish(MMR_STATUS_INVALID_STATE,
+                  std::string("invalid state: ") + d->kind() + " decoder must be configured before " + what);
+}
+
+}  // namespace
 
 namespace {
 
@@ -726,6 +830,126 @@ MMR_API mmr_status mmr_gpu_server_set_tuning(mmr_gpu_server *server, const mmr_g
     if (const char *err = to_table(entries, count, table)) return invalid_argument(err);
     try {
         server->server->set_tuning(table);
+        return finish(MMR_STATUS_OK, "");
+    } catch (...) {
+        return finish(MMR_STATUS_INTERNAL_ERROR, "panic contained at MMRecode C API boundary");
+    }
+}
+
+MMR_API mmr_status mmr_gpu_decoder_create(uint32_t codec, mmr_gpu_decoder **out_decoder) {
+    if (!out_decoder) return invalid_argument("out_decoder is null");
+    *out_decoder = nullptr;
+    if (codec != MMR_CODEC_MJPEG && codec != MMR_CODEC_DV) return invalid_argument("unknown codec");
+    mmr_gpu_decoder *d = new (std::nothrow) mmr_gpu_decoder();
+    if (!d) return finish(MMR_STATUS_INTERNAL_ERROR, "out of host memory");
+    d->codec = codec;
+    *out_decoder = d;
+    return finish(MMR_STATUS_OK, "");
+}
+
+MMR_API void mmr_gpu_decoder_destroy(mmr_gpu_decoder *decoder) {
+    if (!decoder) return;
+    decoder->clear();
+    delete decoder;
+}
+
+// configure (mjpeg/src/codec.rs:22-37, dv/src/codec.rs:22-31).
+MMR_API mmr_status mmr_gpu_decoder_configure(mmr_gpu_decoder *decoder, const char *codec_id, const char *media_type) {
+    if (!decoder || !codec_id || !media_type) return invalid_argument("decoder, codec_id or media_type is null");
+    const bool video = strcmp(media_type, "video") == 0;
+    if (decoder->codec == MMR_CODEC_DV) {
+        if (strcmp(codec_id, "video/dv") != 0 || !video)
+            return finish(MMR_STATUS_INVALID_DATA, "invalid data: DV decoder requires a video/dv video descriptor");
+    } else {
+        if (strcmp(codec_id, "video/mjpeg") != 0)
+            return finish(MMR_STATUS_INVALID_DATA,
+                          std::string("invalid data: expected video/mjpeg, received ") + codec_id);
+        if (!video)
+            return finish(MMR_STATUS_INVALID_DATA,
+                          "invalid data: Motion JPEG decoder requires a video stream descriptor");
+    }
+    try {
+        decoder->clear();
+    } catch (...) {
+        return finish(MMR_STATUS_INTERNAL_ERROR, "panic contained at MMRecode C API boundary");
+    }
+    decoder->configured = true;
+    return finish(MMR_STATUS_OK, "");
+}
+
+// send_packet (mjpeg/src/codec.rs:39-53, dv/src/codec.rs:33-47), queued instead of
+// decoded before returning.
+MMR_API mmr_status mmr_gpu_decoder_send_packet(mmr_gpu_decoder *decoder, const uint8_t *data, size_t len,
+                                               uint64_t user_tag) {
+    if (!decoder) return invalid_argument("decoder is null");
+    if (!decoder->configured) return unconfigured(decoder, "receiving packets");
+    if (len > 0 && !data) return invalid_argument("data is null while length is nonzero");
+    try {
+        if (!decoder->server) {
+            std::string err;
+            decoder->server = session_server(err);
+            if (!decoder->server) return finish(MMR_STATUS_INTERNAL_ERROR, err);
+        }
+        auto e = std::make_unique<SessionEntry>();
+        e->packet.assign(data, data + len);
+        e->tag = user_tag;
+        Item it;
+        it.data = e->packet.data();
+        it.len = len;
+        it.codec = decoder->codec;
+        it.output = mmr::kOutPlanar;
+        mmr::Probe pr = mmr::probe_packet(decoder->codec, it.data, len);
+        if (!alloc_planes(pr, it, e->planes)) return finish(MMR_STATUS_INTERNAL_ERROR, "out of host memory");
+        if (decoder->server->submit(it, &e->ticket) != mmr::kOk) {  // only a memory budget refuses; this one has none
+            for (auto p : e->planes) free(p);
+            return finish(MMR_STATUS_INTERNAL_ERROR, "the GPU decoder refused the packet");
+        }
+        decoder->queue.push_back(std::move(e));
+        return finish(MMR_STATUS_OK, "");
+    } catch (...) {
+        return finish(MMR_STATUS_INTERNAL_ERROR, "panic contained at MMRecode C API boundary");
+    }
+}
+
+// receive_frame (mjpeg/src/codec.rs:55-62, dv/src/codec.rs:49-56).
+MMR_API mmr_status mmr_gpu_decoder_receive_frame(mmr_gpu_decoder *decoder, int64_t wait_ns,
+                                                 mmr_video_frame *out_frame, uint64_t *out_user_tag,
+                                                 int *out_has_frame) {
+    if (!decoder || !out_has_frame) return invalid_argument("decoder or out_has_frame is null");
+    *out_has_frame = 0;
+    if (!decoder->configured) return unconfigured(decoder, "receiving frames");
+    if (mmr_status st = check_frame(out_frame)) return st;
+    reset_frame(out_frame);
+    if (decoder->queue.empty()) return finish(MMR_STATUS_OK, "");
+    try {
+        SessionEntry &e = *decoder->queue.front();
+        if (!e.done) {
+            if (!decoder->server->wait(e.ticket, wait_ns, &e.result, nullptr)) return finish(MMR_STATUS_OK, "");
+            e.done = true;
+        }
+        std::unique_ptr<SessionEntry> owned = std::move(decoder->queue.front());
+        decoder->queue.pop_front();
+        if (out_user_tag) *out_user_tag = owned->tag;
+        const Item &it = owned->result;
+        if (it.status != MMR_STATUS_OK) {
+            for (auto p : owned->planes) free(p);
+            return finish(it.status, with_prefix(it.status, it.message));
+        }
+        fill_frame(it, owned->planes, out_frame);
+        *out_has_frame = 1;
+        return finish(MMR_STATUS_OK, "");
+    } catch (...) {
+        return finish(MMR_STATUS_INTERNAL_ERROR, "panic contained at MMRecode C API boundary");
+    }
+}
+
+// flush (mjpeg/src/codec.rs:64-71, dv/src/codec.rs:58-65): the reference has no
+// delayed frames; here it waits until every queued packet is decoded.
+MMR_API mmr_status mmr_gpu_decoder_flush(mmr_gpu_decoder *decoder) {
+    if (!decoder) return invalid_argument("decoder is null");
+    if (!decoder->configured) return unconfigured(decoder, "flushing");
+    try {
+        for (auto &e : decoder->queue) decoder->settle(*e);
         return finish(MMR_STATUS_OK, "");
     } catch (...) {
         return finish(MMR_STATUS_INTERNAL_ERROR, "panic contained at MMRecode C API boundary");
