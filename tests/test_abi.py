@@ -173,3 +173,25 @@ def test_own_c_smoke_compiles(tmp_path):
            _lib.LIB_PATH, f"-Wl,-rpath,{os.path.dirname(_lib.LIB_PATH)}"]
     p = subprocess.run(cmd, capture_output=True, text=True)
     assert p.returncode == 0, p.stderr
+
+
+@pytest.mark.parametrize("compiler,std", [("gcc", "-std=c11"), ("g++", "-std=c++17")])
+def test_gpu_header_is_clean_c_and_cpp(tmp_path, compiler, std):
+    """include/mmrecode_gpu.h for C and C++ callers: it compiles with every warning as an
+    error, and every function it declares links against the library."""
+    names = declared_functions()
+    src = tmp_path / ("use_gpu_header.c" if compiler == "gcc" else "use_gpu_header.cpp")
+    body = ",\n    ".join(f"(void (*)(void))&{n}" for n in names)
+    src.write_text('#include "mmrecode_gpu.h"\n#include <stdio.h>\n\n'
+                   f"static void (*const entries[])(void) = {{\n    {body}\n}};\n\n"
+                   "int main(void) {\n"
+                   "    printf(\"%zu\\n\", sizeof entries / sizeof entries[0]);\n"
+                   "    return 0;\n}\n")
+    exe = tmp_path / "use_gpu_header"
+    flags = ["-Wall", "-Wextra", "-Werror", "-pedantic"] + (["-Wno-cast-function-type"] if compiler == "g++" else [])
+    cmd = [compiler, std, *flags, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe), _lib.LIB_PATH,
+           f"-Wl,-rpath,{os.path.dirname(_lib.LIB_PATH)}"]
+    p = subprocess.run(cmd, capture_output=True, text=True)
+    assert p.returncode == 0, p.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0 and int(out.stdout) == len(names)
