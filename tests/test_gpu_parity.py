@@ -17,7 +17,7 @@ import pytest
 import mmrecode_gb300 as m
 import oracle
 from mmrecode_gb300 import _lib, synth
-from helpers import (DV_FIXTURES, GOLDEN, JPEG_FIXTURES, SIMPLE_AC, SIMPLE_DC, BitWriter, assert_same_decode,
+from helpers import (DV_FIXTURES, GOLDEN, JPEG_FIXTURES, SIMPLE_AC, SIMPLE_DC, assert_same_decode,
                      encode_blocks, fixture, frame_planes_gpu, jpeg, prefixed, stuff, report)
 
 pytestmark = pytest.mark.gpu

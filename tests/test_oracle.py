@@ -10,7 +10,7 @@ import os
 import pytest
 
 import oracle
-from helpers import GOLDEN, JPEG_FIXTURES, DV_FIXTURES, fixture, jpeg, encode_blocks, SIMPLE_DC
+from helpers import GOLDEN, JPEG_FIXTURES, DV_FIXTURES, fixture, jpeg
 
 
 # transform.rs:140-149 reconstructs_constant_dc_blocks
