@@ -391,6 +391,43 @@ MMR_API mmr_status mmr_gpu_decoder_receive_frame(mmr_gpu_decoder *decoder, int64
 MMR_API mmr_status mmr_gpu_decoder_flush(mmr_gpu_decoder *decoder);
 
 /*
+ * Where a session delivers its frames: MMR_SESSION_HOST_FRAMES (the default;
+ * receive_frame) or MMR_SESSION_DEVICE_FRAMES (receive_device_frame: the planes stay
+ * in device memory of device 0, nothing is downloaded). Changes only while no packet
+ * is queued (else MMR_STATUS_INVALID_STATE); receiving with the other call is
+ * MMR_STATUS_INVALID_STATE.
+ */
+#define MMR_SESSION_HOST_FRAMES 0u
+#define MMR_SESSION_DEVICE_FRAMES 1u
+MMR_API mmr_status mmr_gpu_decoder_set_output(mmr_gpu_decoder *decoder, uint32_t where);
+
+/* A decoded frame in device memory. The planes are one library-owned buffer,
+   valid until mmr_gpu_device_frame_release; each plane's stride is its width. */
+typedef struct mmr_gpu_device_frame {
+    size_t struct_size;
+    mmr_pixel_format format;
+    mmr_color_range range;
+    size_t width, height;
+    size_t plane_count;
+    const uint8_t *planes[MMR_MAX_PLANES]; /* device pointers */
+    size_t plane_width[MMR_MAX_PLANES], plane_height[MMR_MAX_PLANES];
+    void *buffer;        /* the library's: handed back by the release call */
+    size_t buffer_bytes;
+} mmr_gpu_device_frame;
+
+/* receive_frame for a session set to MMR_SESSION_DEVICE_FRAMES; the same waiting,
+   tag and error rules. *out_frame needs its struct_size set and is reset by the call. */
+MMR_API mmr_status mmr_gpu_decoder_receive_device_frame(mmr_gpu_decoder *decoder, int64_t wait_ns,
+                                                        mmr_gpu_device_frame *out_frame, uint64_t *out_user_tag,
+                                                        int *out_has_frame);
+
+/* Gives a device frame's buffer back to the library (reused by later frames) and
+   resets the frame to empty; NULL, empty frames and frames of another struct_size are
+   ignored. The work reading the frame on the device must be complete (synchronise the
+   streams that read it first). */
+MMR_API void mmr_gpu_device_frame_release(mmr_gpu_device_frame *frame);
+
+/*
  * Whole-stream decode to Y4M: the reference CLI's `mmrecode decode <in> <out>`
  * for MJPEG and raw DV input (crates/cli/src/main.rs:1533-1580, 1605-1633), with
  * the stream uploaded once and framed on the GPU, every frame decoded in one

@@ -30,6 +30,7 @@ STATUS_OK, INVALID_ARGUMENT, INVALID_DATA, UNSUPPORTED, INVALID_STATE, IO_ERROR,
 GRAY8, YUV420P8, YUV422P8, YUV444P8, YUV411P8 = 1, 2, 3, 4, 5
 RANGE_UNSPECIFIED, RANGE_FULL, RANGE_LIMITED = 0, 1, 2
 CODEC_MJPEG, CODEC_DV = 1, 2
+SESSION_HOST_FRAMES, SESSION_DEVICE_FRAMES = 0, 1  # mmr_gpu_decoder_set_output
 OUTPUT_PLANAR, OUTPUT_RGB24 = 0, 1
 ITEM_CONCEAL, ITEM_OUT_DEVICE, ITEM_IN_DEVICE = 1, 2, 4
 DV_MODE_88, DV_MODE_ACTIVITY = 0, 1
@@ -795,13 +796,15 @@ class DecoderSession:
     error is raised by the ``receive_frame`` that reaches it (``MmrError.tag`` is the
     packet's tag)."""
 
-    def __init__(self, codec: int):
+    def __init__(self, codec: int, device_frames: bool = False):
         lib = _lib.load()
         h = ctypes.c_void_p()
         st = lib.mmr_gpu_decoder_create(codec, ctypes.byref(h))
         if st != STATUS_OK:
             raise MmrError(st, _lib.last_error())
         self._h = h  # send_packet copies each packet: the caller's bytes need not stay alive
+        if device_frames:
+            self._check(lib.mmr_gpu_decoder_set_output(h, SESSION_DEVICE_FRAMES))
 
     def close(self) -> None:
         """Waits for the packets still being decoded and frees the session."""
@@ -852,3 +855,41 @@ class DecoderSession:
 
     def flush(self) -> None:
         self._check(_lib.load().mmr_gpu_decoder_flush(self._h))
+
+    def receive_device_frame(self, wait_ns: int = -1):
+        """For a session made with ``device_frames=True``: (DeviceFrame, tag), or None
+        as for ``receive_frame``. Release the frame when done with its planes."""
+        fr = _lib.DeviceFrame()
+        fr.struct_size = ctypes.sizeof(_lib.DeviceFrame)
+        tag, has = ctypes.c_uint64(0), ctypes.c_int(0)
+        st = _lib.load().mmr_gpu_decoder_receive_device_frame(self._h, wait_ns, ctypes.byref(fr), ctypes.byref(tag),
+                                                              ctypes.byref(has))
+        if st != STATUS_OK:
+            e = MmrError(st, _lib.last_error())
+            e.tag = tag.value
+            raise e
+        if not has.value:
+            return None
+        return DeviceFrame(fr), tag.value
+
+
+class DeviceFrame:
+    """A session's frame in device memory (device 0): ``planes`` lists (device address,
+    width, height) per plane, stride = width. ``release()`` hands the buffer back."""
+
+    def __init__(self, raw: "_lib.DeviceFrame"):
+        self._raw = raw
+        self.format, self.range, self.width, self.height = raw.format, raw.range, raw.width, raw.height
+        self.planes = [(raw.planes[c], raw.plane_width[c], raw.plane_height[c]) for c in range(raw.plane_count)]
+
+    def release(self) -> None:
+        if self._raw is not None:
+            _lib.load().mmr_gpu_device_frame_release(ctypes.byref(self._raw))
+            self._raw = None
+            self.planes = []
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.release()

@@ -38,6 +38,13 @@ class VideoFrameC(ctypes.Structure):
                 ("planes", OwnedPlane * 3)]
 
 
+class DeviceFrame(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_size_t), ("format", ctypes.c_uint32), ("range", ctypes.c_uint32),
+                ("width", ctypes.c_size_t), ("height", ctypes.c_size_t), ("plane_count", ctypes.c_size_t),
+                ("planes", ctypes.c_void_p * 3), ("plane_width", ctypes.c_size_t * 3),
+                ("plane_height", ctypes.c_size_t * 3), ("buffer", ctypes.c_void_p), ("buffer_bytes", ctypes.c_size_t)]
+
+
 class Buffer(ctypes.Structure):
     _fields_ = [("struct_size", ctypes.c_size_t), ("data", u8p), ("len", ctypes.c_size_t)]
 
@@ -177,6 +184,11 @@ SIGNATURES = {
     "mmr_gpu_decoder_receive_frame": ([ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(VideoFrameC),
                                        ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_int)], ctypes.c_int32),
     "mmr_gpu_decoder_flush": ([ctypes.c_void_p], ctypes.c_int32),
+    "mmr_gpu_decoder_set_output": ([ctypes.c_void_p, ctypes.c_uint32], ctypes.c_int32),
+    "mmr_gpu_decoder_receive_device_frame": ([ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(DeviceFrame),
+                                              ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_int)],
+                                             ctypes.c_int32),
+    "mmr_gpu_device_frame_release": ([ctypes.POINTER(DeviceFrame)], None),
     "mmr_gpu_server_replay": ([ctypes.c_void_p, ctypes.POINTER(GpuItem), ctypes.c_size_t,
                               ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_double),
                               ctypes.POINTER(ctypes.c_int64)], ctypes.c_int32),

@@ -6,6 +6,7 @@
 #include <string.h>
 
 #include <deque>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <new>
@@ -286,6 +287,8 @@ namespace {
 struct SessionEntry {
     std::vector<uint8_t> packet;
     uint8_t *planes[3] = {nullptr, nullptr, nullptr};
+    void *dev = nullptr;  // device output of a session that delivers device frames
+    size_t dev_bytes = 0;
     uint64_t tag = 0;
     uint64_t ticket = 0;
     bool done = false;  // result holds the outcome (the server has forgotten the ticket)
@@ -320,6 +323,62 @@ mmr::Server *session_server(std::string &err) {
     return g_session_server;
 }
 
+// Device buffers of the sessions' device frames (device 0): released frames keep
+// their buffers here, up to kDevKeepBytes, for later frames of about the same size,
+// so that steady decoding allocates nothing.
+std::mutex g_devbuf_mu;
+std::multimap<size_t, void *> g_devbuf_free;  // capacity -> buffer
+size_t g_devbuf_free_bytes = 0;
+constexpr size_t kDevKeepBytes = size_t(1) << 30;
+
+// Runs f with device 0 current on this thread, then restores the caller's device.
+template <class F>
+cudaError_t on_device0(F &&f) {
+    int prev = 0;
+    cudaError_t e = cudaGetDevice(&prev);
+    if (e != cudaSuccess) return e;
+    if ((e = cudaSetDevice(0)) != cudaSuccess) return e;
+    e = f();
+    cudaSetDevice(prev);
+    return e;
+}
+
+// A buffer of at least `need` bytes (at most 1.5x that when reused); null when
+// the device is out of memory.
+void *devbuf_take(size_t need, size_t *capacity) {
+    {
+        std::lock_guard<std::mutex> lock(g_devbuf_mu);
+        auto it = g_devbuf_free.lower_bound(need);
+        if (it != g_devbuf_free.end() && it->first <= need + need / 2) {
+            void *p = it->second;
+            *capacity = it->first;
+            g_devbuf_free_bytes -= it->first;
+            g_devbuf_free.erase(it);
+            return p;
+        }
+    }
+    void *p = nullptr;
+    if (on_device0([&] { return cudaMalloc(&p, need); }) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    *capacity = need;
+    return p;
+}
+
+void devbuf_give(void *p, size_t capacity) {
+    if (!p) return;
+    {
+        std::lock_guard<std::mutex> lock(g_devbuf_mu);
+        if (g_devbuf_free_bytes + capacity <= kDevKeepBytes) {
+            g_devbuf_free.emplace(capacity, p);
+            g_devbuf_free_bytes += capacity;
+            return;
+        }
+    }
+    on_device0([&] { return cudaFree(p); });
+}
+
 }  // namespace
 
 // Decoder trait state (mjpeg/src/codec.rs:16-19, dv/src/codec.rs:16-19): the
@@ -327,6 +386,7 @@ mmr::Server *session_server(std::string &err) {
 struct mmr_gpu_decoder {
     uint32_t codec;
     bool configured = false;
+    bool device_frames = false;  // MMR_SESSION_DEVICE_FRAMES
     std::deque<std::unique_ptr<SessionEntry>> queue;
     mmr::Server *server = nullptr;  // set by the first packet
 
@@ -344,6 +404,7 @@ struct mmr_gpu_decoder {
         for (auto &e : queue) {
             settle(*e);
             for (auto p : e->planes) free(p);
+            devbuf_give(e->dev, e->dev_bytes);
         }
         queue.clear();
     }
@@ -899,9 +960,20 @@ MMR_API mmr_status mmr_gpu_decoder_send_packet(mmr_gpu_decoder *decoder, const u
         it.codec = decoder->codec;
         it.output = mmr::kOutPlanar;
         mmr::Probe pr = mmr::probe_packet(decoder->codec, it.data, len);
-        if (!alloc_planes(pr, it, e->planes)) return finish(MMR_STATUS_INTERNAL_ERROR, "out of host memory");
+        if (decoder->device_frames) {
+            if (pr.status == MMR_STATUS_OK && pr.format != 0 && pr.planar_bytes) {
+                e->dev = devbuf_take(pr.planar_bytes, &e->dev_bytes);
+                if (!e->dev) return finish(MMR_STATUS_INTERNAL_ERROR, "out of device memory");
+                it.out = static_cast<uint8_t *>(e->dev);
+                it.out_capacity = e->dev_bytes;
+                it.out_on_device = true;
+            }
+        } else if (!alloc_planes(pr, it, e->planes)) {
+            return finish(MMR_STATUS_INTERNAL_ERROR, "out of host memory");
+        }
         if (decoder->server->submit(it, &e->ticket) != mmr::kOk) {  // only a memory budget refuses; this one has none
             for (auto p : e->planes) free(p);
+            devbuf_give(e->dev, e->dev_bytes);
             return finish(MMR_STATUS_INTERNAL_ERROR, "the GPU decoder refused the packet");
         }
         decoder->queue.push_back(std::move(e));
@@ -920,6 +992,9 @@ MMR_API mmr_status mmr_gpu_decoder_receive_frame(mmr_gpu_decoder *decoder, int64
     if (!decoder->configured) return unconfigured(decoder, "receiving frames");
     if (mmr_status st = check_frame(out_frame)) return st;
     reset_frame(out_frame);
+    if (decoder->device_frames)
+        return finish(MMR_STATUS_INVALID_STATE,
+                      "invalid state: the session delivers device frames (mmr_gpu_decoder_receive_device_frame)");
     if (decoder->queue.empty()) return finish(MMR_STATUS_OK, "");
     try {
         SessionEntry &e = *decoder->queue.front();
@@ -954,6 +1029,70 @@ MMR_API mmr_status mmr_gpu_decoder_flush(mmr_gpu_decoder *decoder) {
     } catch (...) {
         return finish(MMR_STATUS_INTERNAL_ERROR, "panic contained at MMRecode C API boundary");
     }
+}
+
+MMR_API mmr_status mmr_gpu_decoder_set_output(mmr_gpu_decoder *decoder, uint32_t where) {
+    if (!decoder) return invalid_argument("decoder is null");
+    if (where != MMR_SESSION_HOST_FRAMES && where != MMR_SESSION_DEVICE_FRAMES)
+        return invalid_argument("unknown session output");
+    if (!decoder->queue.empty())
+        return finish(MMR_STATUS_INVALID_STATE, "invalid state: the session output changes only with no packet queued");
+    decoder->device_frames = where == MMR_SESSION_DEVICE_FRAMES;
+    return finish(MMR_STATUS_OK, "");
+}
+
+MMR_API mmr_status mmr_gpu_decoder_receive_device_frame(mmr_gpu_decoder *decoder, int64_t wait_ns,
+                                                        mmr_gpu_device_frame *out_frame, uint64_t *out_user_tag,
+                                                        int *out_has_frame) {
+    if (!decoder || !out_has_frame) return invalid_argument("decoder or out_has_frame is null");
+    *out_has_frame = 0;
+    if (!decoder->configured) return unconfigured(decoder, "receiving frames");
+    if (!out_frame) return invalid_argument("out_frame is null");
+    if (out_frame->struct_size != sizeof(mmr_gpu_device_frame)) return invalid_argument("out_frame struct_size mismatch");
+    memset(out_frame, 0, sizeof(*out_frame));
+    out_frame->struct_size = sizeof(mmr_gpu_device_frame);
+    if (!decoder->device_frames)
+        return finish(MMR_STATUS_INVALID_STATE,
+                      "invalid state: the session delivers host frames (mmr_gpu_decoder_receive_frame)");
+    if (decoder->queue.empty()) return finish(MMR_STATUS_OK, "");
+    try {
+        SessionEntry &e = *decoder->queue.front();
+        if (!e.done) {
+            if (!decoder->server->wait(e.ticket, wait_ns, &e.result, nullptr)) return finish(MMR_STATUS_OK, "");
+            e.done = true;
+        }
+        std::unique_ptr<SessionEntry> owned = std::move(decoder->queue.front());
+        decoder->queue.pop_front();
+        if (out_user_tag) *out_user_tag = owned->tag;
+        const Item &it = owned->result;
+        if (it.status != MMR_STATUS_OK) {
+            devbuf_give(owned->dev, owned->dev_bytes);
+            return finish(it.status, with_prefix(it.status, it.message));
+        }
+        out_frame->format = it.format;
+        out_frame->range = it.range;
+        out_frame->width = it.width;
+        out_frame->height = it.height;
+        out_frame->plane_count = it.plane_count;
+        for (size_t c = 0; c < it.plane_count && c < MMR_MAX_PLANES; c++) {
+            out_frame->planes[c] = static_cast<const uint8_t *>(owned->dev) + it.plane_offset[c];
+            out_frame->plane_width[c] = it.plane_width[c];
+            out_frame->plane_height[c] = it.plane_height[c];
+        }
+        out_frame->buffer = owned->dev;
+        out_frame->buffer_bytes = owned->dev_bytes;
+        *out_has_frame = 1;
+        return finish(MMR_STATUS_OK, "");
+    } catch (...) {
+        return finish(MMR_STATUS_INTERNAL_ERROR, "panic contained at MMRecode C API boundary");
+    }
+}
+
+MMR_API void mmr_gpu_device_frame_release(mmr_gpu_device_frame *frame) {
+    if (!frame || frame->struct_size != sizeof(mmr_gpu_device_frame)) return;
+    devbuf_give(frame->buffer, frame->buffer_bytes);
+    memset(frame, 0, sizeof(*frame));
+    frame->struct_size = sizeof(mmr_gpu_device_frame);
 }
 
 MMR_API mmr_status mmr_gpu_server_set_slice_bits(mmr_gpu_server *server, uint32_t bits) {

@@ -126,3 +126,56 @@ def test_python_session_mirror_states():
     with pytest.raises(m.MmrError) as e:
         m.DecoderSession(0)
     assert e.value.status == m.INVALID_ARGUMENT
+
+
+def device_frame():
+    fr = _lib.DeviceFrame()
+    fr.struct_size = ctypes.sizeof(_lib.DeviceFrame)
+    return fr
+
+
+def test_device_frame_output_states():
+    lib = _lib.load()
+    h = create(m.CODEC_MJPEG)
+    try:
+        assert lib.mmr_gpu_decoder_set_output(h, 2) == m.INVALID_ARGUMENT
+        assert lib.mmr_gpu_decoder_set_output(None, 1) == m.INVALID_ARGUMENT
+        assert lib.mmr_gpu_decoder_configure(h, b"video/mjpeg", b"video") == m.STATUS_OK
+        tag, has = ctypes.c_uint64(3), ctypes.c_int(9)
+        # host frames by default: the device call is the wrong one
+        fr = device_frame()
+        fr.width = 5
+        assert lib.mmr_gpu_decoder_receive_device_frame(h, 0, ctypes.byref(fr), ctypes.byref(tag),
+                                                        ctypes.byref(has)) == m.INVALID_STATE
+        assert _lib.last_error() == "invalid state: the session delivers host frames (mmr_gpu_decoder_receive_frame)"
+        assert has.value == 0 and fr.width == 0  # reset
+        assert lib.mmr_gpu_decoder_set_output(h, m.SESSION_DEVICE_FRAMES) == m.STATUS_OK
+        st, has_frame, _ = receive(h)
+        assert (st, has_frame) == (m.INVALID_STATE, 0)
+        assert _lib.last_error() == \
+            "invalid state: the session delivers device frames (mmr_gpu_decoder_receive_device_frame)"
+        fr = device_frame()
+        assert lib.mmr_gpu_decoder_receive_device_frame(h, 0, ctypes.byref(fr), ctypes.byref(tag),
+                                                        ctypes.byref(has)) == m.STATUS_OK
+        assert has.value == 0 and tag.value == 3 and not fr.buffer  # nothing queued: Ok(None)
+        bad = device_frame()
+        bad.struct_size = 16
+        bad.width = 5
+        assert lib.mmr_gpu_decoder_receive_device_frame(h, 0, ctypes.byref(bad), ctypes.byref(tag),
+                                                        ctypes.byref(has)) == m.INVALID_ARGUMENT
+        assert bad.width == 5  # untouched
+        assert lib.mmr_gpu_decoder_receive_device_frame(h, 0, None, ctypes.byref(tag),
+                                                        ctypes.byref(has)) == m.INVALID_ARGUMENT
+        # release: NULL, an empty frame and a frame of another size are ignored
+        lib.mmr_gpu_device_frame_release(None)
+        lib.mmr_gpu_device_frame_release(ctypes.byref(fr))
+        lib.mmr_gpu_device_frame_release(ctypes.byref(bad))
+        assert bad.width == 5 and fr.struct_size == ctypes.sizeof(_lib.DeviceFrame)
+    finally:
+        lib.mmr_gpu_decoder_destroy(h)
+    with m.DecoderSession(m.CODEC_DV, device_frames=True) as s:
+        s.configure(m.CodecDescriptor(m.DV_CODEC_NAME))
+        assert s.receive_device_frame(0) is None
+        with pytest.raises(m.MmrError) as e:
+            s.receive_frame(0)
+        assert e.value.status == m.INVALID_STATE

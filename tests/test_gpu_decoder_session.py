@@ -2,13 +2,14 @@
 over a server shared by the process) on the GPU against the oracle: every frame's samples,
 every failed packet's status and message, tags and send order; packets received one by one
 and drained after a flush; two sessions of both codecs interleaved on the shared server;
-configure discarding queued packets; destroy with packets still queued."""
+configure discarding queued packets; destroy with packets still queued; frames left in
+device memory (read back through torch), released one by one and held together."""
 import pytest
 
 import mmrecode_gb300 as m
 import oracle
 from helpers import DV_FIXTURES, assert_same_decode, fixture, frame_planes_gpu, prefixed
-from mmrecode_gb300 import synth
+from mmrecode_gb300 import _lib, synth
 
 pytestmark = pytest.mark.gpu
 
@@ -117,3 +118,62 @@ def test_configure_discards_and_destroy_waits():
     for i, p in enumerate(jp):
         s.send_packet(p, i)
     s.close()  # packets still on the GPU: destroy waits for them
+
+
+class _DevicePlane:
+    """A device plane as a CUDA array (read through torch)."""
+
+    def __init__(self, ptr, n):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": "|u1", "data": (ptr, False), "version": 2}
+
+
+def device_planes(torch, frame):
+    return [(w, h, torch.as_tensor(_DevicePlane(ptr, w * h), device="cuda").cpu().numpy().tobytes())
+            for ptr, w, h in frame.planes]
+
+
+@pytest.mark.parametrize("codec", [m.CODEC_MJPEG, m.CODEC_DV], ids=["mjpeg", "dv"])
+def test_device_frames(codec):
+    torch = pytest.importorskip("torch")
+    packets = (mjpeg_packets() if codec == m.CODEC_MJPEG else dv_packets()) * 2
+    s = m.DecoderSession(codec, device_frames=True)
+    s.configure(m.CodecDescriptor(m.MJPEG_CODEC_NAME if codec == m.CODEC_MJPEG else m.DV_CODEC_NAME))
+    try:
+        half = len(packets) // 2
+        for i, p in enumerate(packets[:half]):  # one by one: buffers are reused after release
+            s.send_packet(p, i)
+            try:
+                got = s.receive_device_frame(-1)
+            except m.MmrError as e:
+                assert e.tag == i
+                check(codec, p, e, f"packet {i}")
+                continue
+            frame, tag = got
+            assert tag == i
+            with frame:
+                ref = oracle_of(codec, p)
+                assert_same_decode(0, "", device_planes(torch, frame), ref, f"packet {i}")
+                assert (frame.format, frame.width, frame.height) == (ref.frame.format, ref.frame.width,
+                                                                     ref.frame.height)
+        for i, p in enumerate(packets[half:], half):
+            s.send_packet(p, i)
+        # the output changes only with nothing queued
+        assert _lib.load().mmr_gpu_decoder_set_output(s._h, m.SESSION_HOST_FRAMES) == m.INVALID_STATE
+        s.flush()
+        held = []
+        for i, p in enumerate(packets[half:], half):  # held frames keep distinct buffers
+            try:
+                frame, tag = s.receive_device_frame(0)
+            except m.MmrError as e:
+                check(codec, p, e, f"packet {i}")
+                continue
+            assert tag == i
+            held.append((p, frame))
+        for i, (p, frame) in enumerate(held):
+            assert_same_decode(0, "", device_planes(torch, frame), oracle_of(codec, p), f"held {i}")
+            frame.release()
+        assert s.receive_device_frame(0) is None
+        for i, p in enumerate(packets[:3]):
+            s.send_packet(p, i)
+    finally:
+        s.close()  # with packets queued: their buffers go back to the pool
