@@ -7,6 +7,7 @@ import json
 import math
 import os
 
+import numpy as np
 import pytest
 
 import oracle
@@ -148,3 +149,61 @@ def test_rgb_conversion_known_answer():
                      [(2, 2, bytes([16, 235, 81, 145])), (1, 1, bytes([128])), (1, 1, bytes([128]))])
     rgb = oracle.rgb24(f)
     assert rgb[0:3] == bytes([0, 0, 0]) and rgb[3:6] == bytes([255, 255, 255])
+
+
+def _rgb_reference(fmt, rng_kind, w, h, planes):
+    """video_frame_image at 1:1 (terminal_preview.rs:7159-7236) and ycbcr_to_rgb
+    (:7308-7330), restated here in numpy from the reference source."""
+    if fmt == oracle.FMT_GRAY8:
+        y = np.frombuffer(planes[0][2], np.uint8).reshape(h, w)
+        return np.repeat(y[:, :, None], 3, axis=2).tobytes()
+    (yw, yh, yb), (bw, bh, bb), (rw, rh, rb) = planes
+    xs, ys = np.arange(w), np.arange(h)
+
+    def sample(pw, ph, data):
+        a = np.frombuffer(data, np.uint8).reshape(ph, pw).astype(np.int64)
+        cx = np.minimum(xs * pw // w, pw - 1)
+        cy = np.minimum(ys * ph // h, ph - 1)
+        return a[cy][:, cx]
+
+    y, cb, cr = sample(yw, yh, yb), sample(bw, bh, bb) - 128, sample(rw, rh, rb) - 128
+    if rng_kind == oracle.RANGE_LIMITED:
+        y = np.maximum(y - 16, 0)
+        r = (298 * y + 409 * cr + 128) >> 8
+        g = (298 * y - 100 * cb - 208 * cr + 128) >> 8
+        b = (298 * y + 516 * cb + 128) >> 8
+    else:
+        r = y + ((359 * cr + 128) >> 8)
+        g = y - ((88 * cb + 183 * cr + 128) >> 8)
+        b = y + ((454 * cb + 128) >> 8)
+    return np.clip(np.stack([r, g, b], axis=2), 0, 255).astype(np.uint8).tobytes()
+
+
+@pytest.mark.parametrize("rng_kind", [oracle.RANGE_FULL, oracle.RANGE_LIMITED], ids=["full", "limited"])
+def test_rgb_conversion_every_triple(rng_kind):
+    """All 2^24 (Y, Cb, Cr) triples through the oracle's conversion at 4:4:4 against the
+    restatement: pins the full-range formula, which the reference's tests leave unpinned."""
+    v = np.arange(1 << 24, dtype=np.uint32)
+    planes = [(4096, 4096, (v >> 16).astype(np.uint8).tobytes()), (4096, 4096, ((v >> 8) & 255).astype(np.uint8).tobytes()),
+              (4096, 4096, (v & 255).astype(np.uint8).tobytes())]
+    f = oracle.Frame(oracle.FMT_YUV444P8, rng_kind, 4096, 4096, planes)
+    assert oracle.rgb24(f) == _rgb_reference(oracle.FMT_YUV444P8, rng_kind, 4096, 4096, planes)
+
+
+def test_rgb_conversion_subsampled_layouts():
+    """Gray and every chroma layout, odd sizes, both ranges: the nearest-sample chroma
+    index min(x * cw / W, cw - 1) and the row index alike."""
+    rng = np.random.default_rng(12)
+    layouts = {oracle.FMT_YUV420P8: (2, 2), oracle.FMT_YUV422P8: (2, 1), oracle.FMT_YUV444P8: (1, 1),
+               oracle.FMT_YUV411P8: (4, 1), oracle.FMT_GRAY8: None}
+    for i in range(60):
+        fmt = list(layouts)[i % 5]
+        w, h = int(rng.integers(1, 70)), int(rng.integers(1, 50))
+        planes = [(w, h, rng.integers(0, 256, w * h, dtype=np.uint8).tobytes())]
+        if layouts[fmt]:
+            sx, sy = layouts[fmt]
+            cw, ch = (w + sx - 1) // sx, (h + sy - 1) // sy
+            planes += [(cw, ch, rng.integers(0, 256, cw * ch, dtype=np.uint8).tobytes()) for _ in range(2)]
+        for rk in (oracle.RANGE_FULL, oracle.RANGE_LIMITED):
+            f = oracle.Frame(fmt, rk, w, h, planes)
+            assert oracle.rgb24(f) == _rgb_reference(fmt, rk, w, h, planes), (i, fmt, w, h, rk)
