@@ -55,6 +55,25 @@ def read_y4m_420(data: bytes):
     return frames
 
 
+
+def dv_restamped(frame, rng):
+    """Every macroblock's quantisation number (byte 3, low nibble) and every block's
+    mode bit and class (bits 9..11 of its region) set at random: the VLC parse is
+    unchanged, the dequantisation runs through every QUANT_SHIFTS row, class offset
+    and class-3 shift, and 8-8 and 2-4-8 blocks mix in every macroblock."""
+    b = bytearray(frame)  # frames of intact DIF structure (120000 or 144000 bytes)
+    starts = np.cumsum((0, 112, 112, 112, 112, 80))
+    for seq in range(len(frame) // 12000):
+        for vn in range(135):
+            base = (seq * 150 + 7 + (vn // 15) * 16 + vn % 15) * 80
+            b[base + 3] = (b[base + 3] & 0xF0) | int(rng.integers(0, 16))
+            for start in starts:
+                for off, bit in zip(range(9, 12), rng.integers(0, 2, 3)):
+                    pos = 32 + int(start) + off
+                    mask = 0x80 >> (pos & 7)
+                    b[base + pos // 8] = (b[base + pos // 8] & ~mask) | (mask if bit else 0)
+    return bytes(b)
+
 # ------------------------------------------------------------------ JPEG assembly
 
 class BitWriter:

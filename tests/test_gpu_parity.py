@@ -18,7 +18,7 @@ import mmrecode_gb300 as m
 import oracle
 from mmrecode_gb300 import _lib, synth
 from helpers import (DV_FIXTURES, GOLDEN, JPEG_FIXTURES, SIMPLE_AC, SIMPLE_DC, assert_same_decode,
-                     encode_blocks, fixture, frame_planes_gpu, jpeg, prefixed, stuff, report)
+                     dv_restamped, encode_blocks, fixture, frame_planes_gpu, jpeg, prefixed, stuff, report)
 
 pytestmark = pytest.mark.gpu
 
@@ -186,6 +186,19 @@ def test_dv_spill_levels_extreme_content(ctx, pal):
     check_batch(ctx, m.CODEC_DV, bad, "dv extreme damaged")
     check_batch(ctx, m.CODEC_DV, bad, "dv extreme damaged conceal", conceal=True)
     report("dv spill levels", frames=len(packets) + 2 * len(bad))
+
+
+@pytest.mark.parametrize("pal", [False, True])
+def test_dv_every_class_quantiser_and_mode(ctx, pal):
+    """Frames whose macroblock quantisation numbers and block classes and modes are set
+    at random (helpers.dv_restamped): the dequantisation through every QUANT_SHIFTS
+    row, class offset and the class-3 shift (decoder.rs:290-310), 8-8 and 2-4-8 blocks
+    of every class mixed in each macroblock."""
+    rng = np.random.Generator(np.random.PCG64(140 + pal))
+    packets = [dv_restamped(f, rng) for f in synth.dv_stream(141 + pal, 2, pal=pal)]
+    check_batch(ctx, m.CODEC_DV, packets, "dv restamped")
+    check_batch(ctx, m.CODEC_DV, packets[:1], "dv restamped rgb", m.OUTPUT_RGB24)
+    report("dv classes and quantisers", frames=len(packets))
 
 
 def test_mixed_sizes_subsampling_quality_restart(ctx):
