@@ -97,3 +97,10 @@ def test_encoder_streams_and_entropy_mutations():
             st = compare(d, f"stream {i} mutation {j}")
             outcomes[st] = outcomes.get(st, 0) + 1
     assert outcomes.get(0, 0) > 20 and outcomes.get(2, 0) > 100, outcomes
+
+
+def test_benchmark_frames():
+    """The first frame of the 1080p 4:2:2 q90 workload (restart interval 120 MCUs,
+    135 intervals) and of the 640x480 4:2:0 q75 one (no restart markers)."""
+    compare(synth.mjpeg_stream(20261203, 1, 1920, 1080, "422", 90, 120, annex_k=True)[0], "1080p 4:2:2")
+    compare(synth.mjpeg_stream(20261201, 1, 640, 480, "420", 75, 0, annex_k=True)[0], "640x480 4:2:0")
