@@ -8,7 +8,6 @@ restart intervals, and seeded mutations of their entropy-coded bytes and restart
 markers. The reference's own tests pin no pixel values of a non-trivial decode, no
 Annex K table decode, 4:2:2 or multi-interval restart decode."""
 import numpy as np
-import pytest
 
 import mmrecode_gb300 as m
 import oracle
