@@ -925,7 +925,7 @@ int32_t Engine::decode(Item *items, size_t n, EngineTimes *times) {
                     r.first = blocks + p.comps[c].blk_base;
                     r.frame = (uint32_t)jframes.size();
                     r.comp = c;
-                    if (p.comps[c].bw * p.comps[c].bh) {
+                    if (p.comps[c].bw != 0 && p.comps[c].bh != 0) {
                         ranges.push_back(r);
                         idct_cta.push_back(idct_cta.back() + idct_ctas(p.comps[c].bw * p.comps[c].bh));
                     }
