@@ -155,6 +155,26 @@ def _reference_smoke() -> str:
 
 
 REFERENCE_SMOKE = _reference_smoke()
+REFERENCE_HEADER = os.path.join(os.path.dirname(os.path.dirname(REFERENCE_SMOKE)), "include", "mmrecode.h")
+
+
+def _declarations(path):
+    """#define lines and C statements (typedefs, prototypes) of a header, with
+    comments dropped and whitespace normalised."""
+    text = open(path).read()
+    text = re.sub(r"/\*.*?\*/", " ", text, flags=re.S)
+    text = re.sub(r"//[^\n]*", " ", text)
+    defines = sorted(re.sub(r"\s+", " ", l.strip()) for l in text.splitlines() if l.strip().startswith("#define"))
+    body = re.sub(r"\s+", " ", "\n".join(l for l in text.splitlines() if not l.strip().startswith("#")))
+    body = re.sub(r"\s*([(),;{}*\[\]])\s*", r"\1", body)
+    return defines, sorted(x.strip() for x in body.split(";") if x.strip())
+
+
+@pytest.mark.skipif(not os.path.exists(REFERENCE_HEADER), reason="reference checkout absent")
+def test_v1_header_declares_what_the_reference_header_declares():
+    """include/mmrecode.h against crates/capi/include/mmrecode.h: the same macros, types
+    and prototypes (only comments and line breaks differ), so callers compile unchanged."""
+    assert _declarations(os.path.join(ROOT, "include", "mmrecode.h")) == _declarations(REFERENCE_HEADER)
 
 
 @pytest.mark.skipif(not os.path.exists(REFERENCE_SMOKE) or not shutil.which("gcc"), reason="reference smoke.c absent")
