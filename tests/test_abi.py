@@ -186,6 +186,19 @@ def test_reference_smoke_c_compiles_and_links_unchanged(tmp_path):
     assert p.returncode == 0, p.stderr
 
 
+def test_session_c_caller_compiles(tmp_path):
+    """tests/c/session_decode.c, a C caller of the decoder session API, compiles with
+    every warning as an error and links (it runs on a GPU)."""
+    src = os.path.join(ROOT, "tests", "c", "session_decode.c")
+    exe = tmp_path / "session_decode"
+    cmd = ["gcc", "-std=c11", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"), src, "-o", str(exe),
+           _lib.LIB_PATH, f"-Wl,-rpath,{os.path.dirname(_lib.LIB_PATH)}"]
+    p = subprocess.run(cmd, capture_output=True, text=True)
+    assert p.returncode == 0, p.stderr
+    usage = subprocess.run([str(exe)], capture_output=True, text=True)  # no arguments: usage, exit 2
+    assert usage.returncode == 2 and "usage" in usage.stderr
+
+
 def test_own_c_smoke_compiles(tmp_path):
     src = os.path.join(ROOT, "tests", "c", "smoke_decode.c")
     exe = tmp_path / "smoke_decode"
